@@ -1,0 +1,99 @@
+"""CPU oracle for the canvas_ity render path -- TEST INFRASTRUCTURE ONLY.
+
+`oracle/cy_oracle.cpp` restates the reference CPU algorithm
+(src/canvas_ity.hpp); this module builds it with g++ and replays recorded
+call lists through it.  `oracle/ref/` builds the reference itself from its
+own sources when they are present (not on the GPU host) for pinning.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+use this package; the product library never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import List, Optional, Tuple
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+ORACLE_SO = os.path.join(BUILD_DIR, "libcy_oracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_SO = os.path.join(REF_DIR, "libcy_ref.so")
+REFERENCE_ROOT = os.environ.get("CY_REFERENCE_ROOT", "/root/reference")
+
+_FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle restatement (fast: one translation unit)."""
+    src = os.path.join(HERE, "cy_oracle.cpp")
+    hdrs = [os.path.join(HERE, "..", "include", h) for h in ("cy_trace.h", "cy_replay.hpp")]
+    newest = max(os.path.getmtime(p) for p in [src] + hdrs)
+    if not force and os.path.exists(ORACLE_SO) and os.path.getmtime(ORACLE_SO) >= newest:
+        return ORACLE_SO
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = ORACLE_SO + ".tmp"
+    subprocess.check_call(["g++", *_FLAGS, "-o", tmp, src])
+    os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_reference(force: bool = False) -> Optional[str]:
+    """Build the reference tools from the read-only sources, if present."""
+    if not os.path.isfile(os.path.join(REFERENCE_ROOT, "src", "canvas_ity.hpp")):
+        return None
+    if force or not os.path.exists(REF_SO):
+        subprocess.check_call(["sh", os.path.join(HERE, "ref", "build_ref.sh"), REFERENCE_ROOT])
+    return REF_SO
+
+
+class _Lib:
+    def __init__(self, path: str, symbol: str):
+        self.lib = ctypes.CDLL(path)
+        self.fn = getattr(self.lib, symbol)
+        self.fn.restype = ctypes.c_int
+        self.fn.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                            ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_float),
+                            ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+
+    def replay(self, trace: bytes) -> Tuple[bytes, List[float]]:
+        cap, rcap = 1 << 20, 1024
+        while True:
+            img = ctypes.create_string_buffer(cap)
+            res = (ctypes.c_float * rcap)()
+            n_img, n_res = ctypes.c_size_t(0), ctypes.c_int(0)
+            rc = self.fn(trace, len(trace), img, cap, ctypes.byref(n_img), res, rcap, ctypes.byref(n_res))
+            if rc == -2:
+                cap, rcap = max(cap, n_img.value), max(rcap, n_res.value)
+                continue
+            if rc != 0:
+                raise ValueError(f"replay failed with status {rc}")
+            return img.raw[: n_img.value], [res[i] for i in range(n_res.value)]
+
+
+_oracle: Optional[_Lib] = None
+_ref: Optional[_Lib] = None
+
+
+def replay(trace: bytes) -> Tuple[bytes, List[float]]:
+    """Replay through the oracle: (concatenated get_image_data bytes, results)."""
+    global _oracle
+    if _oracle is None:
+        _oracle = _Lib(build(), "cyo_replay")
+    return _oracle.replay(trace)
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO) or build_reference() is not None
+
+
+def reference_replay(trace: bytes) -> Tuple[bytes, List[float]]:
+    """Replay through the reference header itself (needs its sources)."""
+    global _ref
+    if _ref is None:
+        path = build_reference()
+        if path is None:
+            raise RuntimeError("reference sources are not available here")
+        _ref = _Lib(path, "cyr_replay")
+    return _ref.replay(trace)

@@ -1,0 +1,27 @@
+#!/bin/sh
+# Build the reference-side test tools from the read-only reference sources,
+# where they lie (no copy is made), into oracle/_ref/:
+#   libcy_ref.so   reference canvas + call-list replay (cyr_replay)
+#   ref_recorder   the reference's own test/test.cpp compiled against the
+#                  recording canvas (oracle/ref/recorder.hpp)
+# Usage: oracle/ref/build_ref.sh [reference_root]   (default /root/reference)
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT=$HERE/../_ref
+if [ ! -f "$REF/src/canvas_ity.hpp" ]; then
+    echo "reference sources not found under $REF" >&2
+    exit 2
+fi
+mkdir -p "$OUT/rec/src" "$OUT/rec/cwd"
+FLAGS="-O3 -ffp-contract=off -fPIC"
+g++ $FLAGS -shared -DCY_REFERENCE_HEADER="\"$REF/src/canvas_ity.hpp\"" \
+    -o "$OUT/libcy_ref.so" "$HERE/ref_replay.cpp"
+# test/test.cpp includes "../src/canvas_ity.hpp"; it is compiled from standard
+# input inside $OUT/rec/cwd so that this include resolves to the recording
+# header instead of the library header.
+printf '#include "%s/recorder.hpp"\n' "$HERE" > "$OUT/rec/src/canvas_ity.hpp"
+( cd "$OUT/rec/cwd" && g++ $FLAGS -Dmain=cy_test_main -x c++ -c -o "$OUT/rec/test.o" - < "$REF/test/test.cpp" )
+g++ $FLAGS -DCY_REFERENCE_HEADER="\"$REF/src/canvas_ity.hpp\"" -c -o "$OUT/rec/recorder.o" "$HERE/recorder.cpp"
+g++ -o "$OUT/ref_recorder" "$OUT/rec/test.o" "$OUT/rec/recorder.o"
+echo "built $OUT/libcy_ref.so $OUT/ref_recorder"
