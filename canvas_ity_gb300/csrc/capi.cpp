@@ -1,0 +1,159 @@
+// capi.cpp -- flat C binding of canvas_ity::canvas and the call-list replay
+// entry point (include/canvas_ity_c.h).
+#include <cstring>
+#include <memory>
+#include <new>
+
+#include "../../include/canvas_ity.hpp"
+#include "../../include/canvas_ity_c.h"
+#include "../../include/cy_replay.hpp"
+
+using canvas_ity::canvas;
+
+struct cy_canvas {
+    canvas impl;
+    cy_canvas(int w, int h) : impl(w, h) {}
+};
+
+namespace {
+struct traits {
+    typedef canvas canvas_type;
+    typedef canvas_ity::brush_type brush_type;
+    typedef canvas_ity::composite_operation composite_operation;
+    typedef canvas_ity::cap_style cap_style;
+    typedef canvas_ity::join_style join_style;
+    typedef canvas_ity::repetition_style repetition_style;
+    typedef canvas_ity::align_style align_style;
+    typedef canvas_ity::baseline_style baseline_style;
+    static std::unique_ptr<canvas> make(int w, int h) { return std::unique_ptr<canvas>(new canvas(w, h)); }
+};
+inline canvas_ity::brush_type bt(int t) { return static_cast<canvas_ity::brush_type>(t); }
+}  // namespace
+
+extern "C" {
+
+cy_canvas *cy_canvas_new(int w, int h) {
+    if (w < 1 || h < 1 || w > 32768 || h > 32768) return nullptr;
+    return new (std::nothrow) cy_canvas(w, h);
+}
+void cy_canvas_delete(cy_canvas *c) { delete c; }
+int cy_canvas_status(const cy_canvas *c) { return c ? c->impl.gpu_status() : -1; }
+void cy_canvas_scale(cy_canvas *c, float x, float y) { c->impl.scale(x, y); }
+void cy_canvas_rotate(cy_canvas *c, float a) { c->impl.rotate(a); }
+void cy_canvas_translate(cy_canvas *c, float x, float y) { c->impl.translate(x, y); }
+void cy_canvas_transform(cy_canvas *c, float a, float b, float cc, float d, float e, float f) {
+    c->impl.transform(a, b, cc, d, e, f);
+}
+void cy_canvas_set_transform(cy_canvas *c, float a, float b, float cc, float d, float e, float f) {
+    c->impl.set_transform(a, b, cc, d, e, f);
+}
+void cy_canvas_set_global_alpha(cy_canvas *c, float a) { c->impl.set_global_alpha(a); }
+void cy_canvas_set_global_composite_operation(cy_canvas *c, int op) {
+    c->impl.global_composite_operation = static_cast<canvas_ity::composite_operation>(op);
+}
+void cy_canvas_set_shadow_color(cy_canvas *c, float r, float g, float b, float a) {
+    c->impl.set_shadow_color(r, g, b, a);
+}
+void cy_canvas_set_shadow_offset_x(cy_canvas *c, float v) { c->impl.shadow_offset_x = v; }
+void cy_canvas_set_shadow_offset_y(cy_canvas *c, float v) { c->impl.shadow_offset_y = v; }
+void cy_canvas_set_shadow_blur(cy_canvas *c, float v) { c->impl.set_shadow_blur(v); }
+void cy_canvas_set_line_width(cy_canvas *c, float v) { c->impl.set_line_width(v); }
+void cy_canvas_set_line_cap(cy_canvas *c, int v) { c->impl.line_cap = static_cast<canvas_ity::cap_style>(v); }
+void cy_canvas_set_line_join(cy_canvas *c, int v) { c->impl.line_join = static_cast<canvas_ity::join_style>(v); }
+void cy_canvas_set_miter_limit(cy_canvas *c, float v) { c->impl.set_miter_limit(v); }
+void cy_canvas_set_line_dash_offset(cy_canvas *c, float v) { c->impl.line_dash_offset = v; }
+void cy_canvas_set_line_dash(cy_canvas *c, const float *s, int n) { c->impl.set_line_dash(s, n); }
+void cy_canvas_set_color(cy_canvas *c, int t, float r, float g, float b, float a) {
+    c->impl.set_color(bt(t), r, g, b, a);
+}
+void cy_canvas_set_linear_gradient(cy_canvas *c, int t, float x0, float y0, float x1, float y1) {
+    c->impl.set_linear_gradient(bt(t), x0, y0, x1, y1);
+}
+void cy_canvas_set_radial_gradient(cy_canvas *c, int t, float x0, float y0, float r0, float x1, float y1,
+                                   float r1) {
+    c->impl.set_radial_gradient(bt(t), x0, y0, r0, x1, y1, r1);
+}
+void cy_canvas_add_color_stop(cy_canvas *c, int t, float o, float r, float g, float b, float a) {
+    c->impl.add_color_stop(bt(t), o, r, g, b, a);
+}
+void cy_canvas_set_pattern(cy_canvas *c, int t, const unsigned char *img, int w, int h, int stride, int rep) {
+    c->impl.set_pattern(bt(t), img, w, h, stride, static_cast<canvas_ity::repetition_style>(rep));
+}
+void cy_canvas_begin_path(cy_canvas *c) { c->impl.begin_path(); }
+void cy_canvas_move_to(cy_canvas *c, float x, float y) { c->impl.move_to(x, y); }
+void cy_canvas_close_path(cy_canvas *c) { c->impl.close_path(); }
+void cy_canvas_line_to(cy_canvas *c, float x, float y) { c->impl.line_to(x, y); }
+void cy_canvas_quadratic_curve_to(cy_canvas *c, float cx, float cy, float x, float y) {
+    c->impl.quadratic_curve_to(cx, cy, x, y);
+}
+void cy_canvas_bezier_curve_to(cy_canvas *c, float a, float b, float cc, float d, float x, float y) {
+    c->impl.bezier_curve_to(a, b, cc, d, x, y);
+}
+void cy_canvas_arc_to(cy_canvas *c, float vx, float vy, float x, float y, float r) { c->impl.arc_to(vx, vy, x, y, r); }
+void cy_canvas_arc(cy_canvas *c, float x, float y, float r, float a0, float a1, int ccw) {
+    c->impl.arc(x, y, r, a0, a1, ccw != 0);
+}
+void cy_canvas_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->impl.rectangle(x, y, w, h); }
+void cy_canvas_fill(cy_canvas *c) { c->impl.fill(); }
+void cy_canvas_stroke(cy_canvas *c) { c->impl.stroke(); }
+void cy_canvas_clip(cy_canvas *c) { c->impl.clip(); }
+int cy_canvas_is_point_in_path(cy_canvas *c, float x, float y) { return c->impl.is_point_in_path(x, y) ? 1 : 0; }
+void cy_canvas_clear_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->impl.clear_rectangle(x, y, w, h); }
+void cy_canvas_fill_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->impl.fill_rectangle(x, y, w, h); }
+void cy_canvas_stroke_rectangle(cy_canvas *c, float x, float y, float w, float h) {
+    c->impl.stroke_rectangle(x, y, w, h);
+}
+void cy_canvas_set_text_align(cy_canvas *c, int v) { c->impl.text_align = static_cast<canvas_ity::align_style>(v); }
+void cy_canvas_set_text_baseline(cy_canvas *c, int v) {
+    c->impl.text_baseline = static_cast<canvas_ity::baseline_style>(v);
+}
+int cy_canvas_set_font(cy_canvas *c, const unsigned char *f, int n, float s) { return c->impl.set_font(f, n, s) ? 1 : 0; }
+void cy_canvas_fill_text(cy_canvas *c, const char *t, float x, float y, float m) { c->impl.fill_text(t, x, y, m); }
+void cy_canvas_stroke_text(cy_canvas *c, const char *t, float x, float y, float m) { c->impl.stroke_text(t, x, y, m); }
+float cy_canvas_measure_text(cy_canvas *c, const char *t) { return c->impl.measure_text(t); }
+void cy_canvas_draw_image(cy_canvas *c, const unsigned char *img, int w, int h, int stride, float x, float y,
+                          float tw, float th) {
+    c->impl.draw_image(img, w, h, stride, x, y, tw, th);
+}
+void cy_canvas_get_image_data(cy_canvas *c, unsigned char *img, int w, int h, int stride, int x, int y) {
+    c->impl.get_image_data(img, w, h, stride, x, y);
+}
+void cy_canvas_put_image_data(cy_canvas *c, const unsigned char *img, int w, int h, int stride, int x, int y) {
+    c->impl.put_image_data(img, w, h, stride, x, y);
+}
+void cy_canvas_save(cy_canvas *c) { c->impl.save(); }
+void cy_canvas_restore(cy_canvas *c) { c->impl.restore(); }
+
+int cy_take_thread_status(void);
+
+int cy_replay(const void *trace, size_t trace_len, void *images, size_t images_cap, size_t *images_len,
+              float *results, int results_cap, int *results_len) {
+    cy_take_thread_status();
+    int rc = cy_trace::replay_to_buffers<traits>(trace, trace_len, images, images_cap, images_len, results,
+                                                 results_cap, results_len);
+    int gpu = cy_take_thread_status();
+    return gpu ? gpu : rc;
+}
+
+int cy_replay_linear(const void *trace, size_t trace_len, float *out, size_t out_floats, int *width,
+                     int *height) {
+    cy_take_thread_status();
+    cy_trace::output sink;
+    std::unique_ptr<canvas> keep;
+    int rc = cy_trace::replay<traits>(static_cast<const uint8_t *>(trace), trace_len, sink, &keep);
+    if (rc == 0 && !keep) rc = -1;
+    if (rc == 0) {
+        int w = 0, h = 0;
+        const uint8_t *t = static_cast<const uint8_t *>(trace);
+        std::memcpy(&w, t + 12, 4);
+        std::memcpy(&h, t + 16, 4);
+        if (width) *width = w;
+        if (height) *height = h;
+        if (static_cast<size_t>(w) * h * 4 > out_floats) rc = -2;
+        else rc = keep->read_linear(out);
+    }
+    int gpu = cy_take_thread_status();
+    return gpu ? gpu : rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,441 @@
+// device.cuh -- device-side restatement of the reference's per-pixel math.
+//
+// Everything here is compiled with --fmad=false and IEEE division/sqrt so
+// that each float operation rounds exactly like the reference's x86-64 SSE
+// code (no fused multiply-add).  hpp = src/canvas_ity.hpp.
+#ifndef CY_DEVICE_CUH
+#define CY_DEVICE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "engine_types.h"
+
+namespace cyg {
+
+// std::min / std::max semantics (first argument wins ties and NaN cases).
+__device__ __forceinline__ float lo(float a, float b) { return b < a ? b : a; }
+__device__ __forceinline__ float hi(float a, float b) { return a < b ? b : a; }
+
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return f2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 scl2(float s, float2 a) { return f2(a.x * s, a.y * s); }
+__device__ __forceinline__ float dot2(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ float2 perp2(float2 a) { return f2(-a.y, a.x); }
+__device__ __forceinline__ float2 mix2(float2 a, float2 b, float t) { return add2(a, scl2(t, sub2(b, a))); }
+
+static constexpr float kVisible = 1.0f / 8160.0f;   // hpp:2433, 2571
+static constexpr float kFixedOne = 4294967296.0f;   // coverage fixed point: 2^32
+static constexpr float kFixedInv = 1.0f / 4294967296.0f;
+
+// ------------------------------------------------------------ flattening
+// Fill-mode flattening of one cubic, hpp:1331-1387 (add_tessellation with
+// angular = -1) and hpp:1398-1487 (add_bezier).  The recursion becomes an
+// explicit depth-first stack; EMIT=false only counts the points.
+struct tess_frame { float2 p1, c1, c2, p2; int limit; };
+
+template <bool EMIT>
+__device__ int tessellate_fill(float2 p1, float2 c1, float2 c2, float2 p2, float2 *out, int cap) {
+    const float flat = 0.125f * 0.125f;
+    tess_frame stack[22];
+    int depth = 0, n = 0;
+    stack[depth++] = {p1, c1, c2, p2, 20};
+    while (depth > 0) {
+        tess_frame f = stack[--depth];
+        for (;;) {
+            float2 seg = sub2(f.p2, f.p1);
+            float2 e1 = sub2(f.c1, f.p1), e3 = sub2(f.p2, f.c2);
+            float lsq = hi(1.0e-4f, dot2(seg, seg));
+            float t1 = lo(hi(dot2(e1, seg) / lsq, 0.0f), 1.0f);
+            float t2 = lo(hi(dot2(e3, seg) / lsq, 0.0f), 1.0f);
+            float2 d1 = sub2(add2(f.p1, scl2(t1, seg)), f.c1);
+            float2 d2 = sub2(sub2(f.p2, scl2(t2, seg)), f.c2);
+            if ((dot2(d1, d1) <= flat && dot2(d2, d2) <= flat) || !f.limit) {
+                if (EMIT && n < cap) out[n] = f.p2;
+                ++n;
+                break;
+            }
+            float2 l1 = mix2(f.p1, f.c1, 0.5f), m = mix2(f.c1, f.c2, 0.5f), r2 = mix2(f.c2, f.p2, 0.5f);
+            float2 l2 = mix2(l1, m, 0.5f), r1 = mix2(m, r2, 0.5f), sp = mix2(l2, r1, 0.5f);
+            stack[depth++] = {sp, r1, r2, f.p2, f.limit - 1};
+            f = {f.p1, l1, l2, sp, f.limit - 1};
+        }
+    }
+    return n;
+}
+
+__device__ __forceinline__ void axis_extrema(float a, float b, float c, float *at, int &cuts) {
+    const float eps = 1.0e-4f;   // hpp:1420-1447
+    if (fabsf(a) > eps) {
+        float disc = b * b - 4.0f * a * c;
+        if (disc >= 0.0f) {
+            float sign = b > 0.0f ? 1.0f : -1.0f;
+            float term = -b - sign * sqrtf(disc);
+            float r1 = term / (2.0f * a);
+            at[cuts++] = r1;
+            at[cuts++] = c / (a * r1);
+        }
+    } else if (fabsf(b) > eps) {
+        at[cuts++] = -c / b;
+    }
+}
+
+template <bool EMIT>
+__device__ int flatten_cubic(float2 p1, float2 c1, float2 c2, float2 p2, float2 *out, int cap) {
+    float2 e1 = sub2(c1, p1), e2 = sub2(c2, c1), e3 = sub2(p2, c2);
+    if (dot2(e1, e1) == 0.0f && dot2(e3, e3) == 0.0f) {
+        if (EMIT && cap > 0) out[0] = p2;
+        return 1;
+    }
+    float at[7] = {0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    int cuts = 2;
+    float2 ea = add2(scl2(-9.0f, e2), scl2(3.0f, sub2(p2, p1)));
+    float2 eb = sub2(scl2(6.0f, add2(p1, c2)), scl2(12.0f, c1));
+    float2 ec = scl2(3.0f, e1);
+    axis_extrema(ea.x, eb.x, ec.x, at, cuts);
+    axis_extrema(ea.y, eb.y, ec.y, at, cuts);
+    float k1 = dot2(perp2(e1), e2), k2 = dot2(perp2(e1), e3), k3 = dot2(perp2(e2), e3);
+    float ca = k1 - k2 + k3, cb = -2.0f * k1 + k2;
+    if (fabsf(ca) > 1.0e-4f && fabsf(cb) > 1.0e-4f) at[cuts++] = -0.5f * cb / ca;
+    for (int i = 1; i < cuts; ++i) {   // insertion sort, hpp:1458-1465
+        float v = at[i];
+        int j = i - 1;
+        for (; 0 <= j && v < at[j]; --j) at[j + 1] = at[j];
+        at[j + 1] = v;
+    }
+    int n = 0;
+    float2 s1 = p1;
+    for (int i = 0; i < cuts - 1; ++i) {
+        if (!(0.0f <= at[i] && at[i + 1] <= 1.0f && at[i] != at[i + 1])) continue;
+        float t = at[i + 1], ratio = at[i] / t;
+        float2 q1 = mix2(p1, c1, t), q2 = mix2(c1, c2, t), q3 = mix2(c2, p2, t);
+        float2 q4 = mix2(q1, q2, t), q5 = mix2(q2, q3, t), q6 = mix2(q1, q4, ratio);
+        float2 s2 = mix2(q4, q5, t);
+        float2 sc2 = mix2(q4, s2, ratio);
+        float2 sc1 = mix2(q6, sc2, ratio);
+        n += tessellate_fill<EMIT>(s1, sc1, sc2, s2, out + (EMIT ? n : 0), cap - n);
+        s1 = s2;
+    }
+    return n;
+}
+
+// ------------------------------------------------------ scan conversion
+// A segment piece inside the (padded) canvas, prepared for the row-by-row
+// restatement of add_runs (hpp:2109-2170).  The reference walks the pixel
+// cells of a segment left to right with a DDA; each row of that walk only
+// depends on values the reference computes directly from the segment
+// (crossing points at integer x and integer y), so any row can be
+// reconstructed independently and rows can be processed in parallel with
+// results identical to the sequential walk.
+struct dda_piece {
+    float fx, fy, tx, ty;   // endpoints ordered by x (from.x <= to.x)
+    float sx, sy;           // slope.x = dx/dy, slope.y = dy/dx
+    float sign, ystep;
+    float px0, py0;         // floor(from)
+    bool up, vert;
+    int nrows;
+};
+
+__device__ __forceinline__ bool dda_setup(float2 a, float2 b, dda_piece &p) {
+    if (!(fabsf(b.y - a.y) >= 2.0e-5f)) return false;   // hpp:2113-2115 (NaN-safe)
+    p.sign = b.y > a.y ? 1.0f : -1.0f;
+    if (a.x > b.x) { float2 t = a; a = b; b = t; }
+    p.fx = a.x; p.fy = a.y; p.tx = b.x; p.ty = b.y;
+    p.up = b.y > a.y;
+    p.px0 = floorf(a.x);
+    p.py0 = floorf(a.y);
+    p.sx = (b.x - a.x) / (b.y - a.y);
+    p.sy = (b.y - a.y) / (b.x - a.x);
+    p.vert = b.x - a.x < 2.0e-5f;
+    p.ystep = p.up ? 1.0f : -1.0f;
+    int last = p.up ? static_cast<int>(ceilf(b.y)) - static_cast<int>(p.py0) - 1
+                    : static_cast<int>(p.py0) - static_cast<int>(floorf(b.y));
+    p.nrows = (last < 0 ? 0 : last) + 1;
+    return true;
+}
+
+// Exit point of row k (the reference's next_y for that row).
+__device__ __forceinline__ float2 dda_exit(const dda_piece &p, int k) {
+    float corner = p.py0 + (p.up ? 1.0f : 0.0f) + static_cast<float>(k) * p.ystep;
+    bool reached = p.up ? (p.ty < corner) : (p.ty > corner);
+    if (reached) return f2(p.tx, p.ty);
+    return f2((corner - p.fy) * p.sx + p.fx, corner);
+}
+
+// Number of lattice crossings x = px0 + m (m >= 1) strictly left of e.
+__device__ __forceinline__ int crossings_before(const dda_piece &p, float e) {
+    int c = static_cast<int>(ceilf(e)) - 1 - static_cast<int>(p.px0);
+    return c < 0 ? 0 : c;
+}
+
+// Emit the signed-area deltas of row k of the piece through `emit(x, y, d)`.
+template <class Emit>
+__device__ __forceinline__ void dda_row(const dda_piece &p, int k, Emit &emit) {
+    float2 entry = k == 0 ? f2(p.fx, p.fy) : dda_exit(p, k - 1);
+    float2 ex = dda_exit(p, k);
+    int ps, pe;
+    if (!p.vert) {
+        int before = k == 0 ? 0 : crossings_before(p, entry.x);
+        int upto = crossings_before(p, ex.x);
+        ps = static_cast<int>(p.px0) + before;
+        pe = static_cast<int>(p.px0) + (upto > before ? upto : before);
+    } else {
+        bool consumed_before = k > 0 && p.tx < entry.x;
+        bool consumed_now = !consumed_before && p.tx < ex.x;
+        ps = static_cast<int>(p.px0) + (consumed_before ? 1 : 0);
+        pe = ps + (consumed_now ? 1 : 0);
+    }
+    int row = static_cast<int>(p.py0) + (p.up ? k : -k);
+    float2 now = entry;
+    float carry = 0.0f;
+    for (int m = ps; m < pe; ++m) {
+        float2 X;
+        if (!p.vert) {
+            float cx = static_cast<float>(m + 1);
+            X = f2(cx, (cx - p.fx) * p.sy + p.fy);
+        } else {
+            X = f2(p.tx, p.ty);
+        }
+        float strip = lo(hi((X.y - now.y) * p.ystep, 0.0f), 1.0f);
+        float mid = (X.x + now.x) * 0.5f;
+        float area = (mid - static_cast<float>(m)) * strip;
+        emit(m, row, (carry + strip - area) * p.sign);
+        carry = area;
+        now = X;
+    }
+    float strip = lo(hi((ex.y - now.y) * p.ystep, 0.0f), 1.0f);
+    float mid = (ex.x + now.x) * 0.5f;
+    float area = (mid - static_cast<float>(pe)) * strip;
+    emit(pe, row, (carry + strip - area) * p.sign);
+    emit(pe + 1, row, area * p.sign);
+}
+
+// Clip one polyline segment to [0,width] x [0,height] the way the
+// reference's Sutherland-Hodgman pass and clamp do (hpp:2204-2239): the part
+// left of x = 0 (right of x = width) is replaced by its projection onto that
+// edge; parts above y = 0 or below y = height contribute nothing.  Returns
+// up to three pieces (main, left edge, right edge).
+__device__ __forceinline__ int clip_segment(float2 a, float2 b, float width, float height, float2 *pa,
+                                            float2 *pb) {
+    if (!(isfinite(a.x) && isfinite(a.y) && isfinite(b.x) && isfinite(b.y))) return 0;
+    float2 ma = a, mb = b;
+    bool has_main = true, has_left = false, has_right = false;
+    float2 la, lb, ra, rb;
+    // x >= 0
+    {
+        float fs = ma.x, ts = mb.x;
+        if (fs < 0.0f && ts < 0.0f) {
+            has_main = false;
+            has_left = true;
+            la = f2(0.0f, ma.y);
+            lb = f2(0.0f, mb.y);
+        } else if (fs * ts < 0.0f) {
+            float2 I = mix2(ma, mb, fs / (fs - ts));
+            has_left = true;
+            if (fs < 0.0f) { la = f2(0.0f, ma.y); lb = f2(0.0f, I.y); ma = I; }
+            else { la = f2(0.0f, I.y); lb = f2(0.0f, mb.y); mb = I; }
+        }
+    }
+    // y >= 0 (parts above project onto a horizontal edge: no coverage)
+    auto clip_y0 = [](bool &has, float2 &u, float2 &v) {
+        if (!has) return;
+        float fs = u.y, ts = v.y;
+        if (fs < 0.0f && ts < 0.0f) { has = false; return; }
+        if (fs * ts < 0.0f) {
+            float2 I = mix2(u, v, fs / (fs - ts));
+            if (fs < 0.0f) u = I; else v = I;
+        }
+    };
+    clip_y0(has_main, ma, mb);
+    clip_y0(has_left, la, lb);
+    // x <= width
+    if (has_main) {
+        float fs = width - ma.x, ts = width - mb.x;
+        if (fs < 0.0f && ts < 0.0f) {
+            has_main = false;
+            has_right = true;
+            ra = f2(width, ma.y);
+            rb = f2(width, mb.y);
+        } else if (fs * ts < 0.0f) {
+            float2 I = mix2(ma, mb, fs / (fs - ts));
+            has_right = true;
+            if (fs < 0.0f) { ra = f2(width, ma.y); rb = f2(width, I.y); ma = I; }
+            else { ra = f2(width, I.y); rb = f2(width, mb.y); mb = I; }
+        }
+    }
+    // y <= height
+    auto clip_yh = [height](bool &has, float2 &u, float2 &v) {
+        if (!has) return;
+        float fs = height - u.y, ts = height - v.y;
+        if (fs < 0.0f && ts < 0.0f) { has = false; return; }
+        if (fs * ts < 0.0f) {
+            float2 I = mix2(u, v, fs / (fs - ts));
+            if (fs < 0.0f) u = I; else v = I;
+        }
+    };
+    clip_yh(has_main, ma, mb);
+    clip_yh(has_left, la, lb);
+    clip_yh(has_right, ra, rb);
+    int n = 0;
+    auto put = [&](float2 u, float2 v) {
+        pa[n] = f2(lo(hi(u.x, 0.0f), width), lo(hi(u.y, 0.0f), height));
+        pb[n] = f2(lo(hi(v.x, 0.0f), width), lo(hi(v.y, 0.0f), height));
+        ++n;
+    };
+    if (has_main) put(ma, mb);
+    if (has_left) put(la, lb);
+    if (has_right) put(ra, rb);
+    return n;
+}
+
+// ------------------------------------------------------------------ paint
+__device__ __forceinline__ float4 premul(float4 c) { return make_float4(c.x * c.w, c.y * c.w, c.z * c.w, c.w); }
+
+__device__ __forceinline__ float keys_weight(float t) {
+    return t < 1.0f ? (1.5f * t - 2.5f) * t * t + 1.0f : ((-0.5f * t + 2.5f) * t - 4.0f) * t + 2.0f;
+}
+
+struct paint_src {
+    const float *stop_off;
+    const float4 *stop_col;
+    const float4 *texels;
+};
+
+// paint_pixel (hpp:2265-2377) at pixel-centre point (px, py).
+__device__ float4 paint_at(const command &c, const paint_src &s, float px, float py) {
+    const float4 none = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (c.paint == 0) return none;
+    if (c.paint == 1) return make_float4(c.color[0], c.color[1], c.color[2], c.color[3]);
+    float x = c.inv[0] * px + c.inv[2] * py + c.inv[4];
+    float y = c.inv[1] * px + c.inv[3] * py + c.inv[5];
+    if (c.paint == 4) {
+        float width = static_cast<float>(c.pat_w), height = static_cast<float>(c.pat_h);
+        if (((c.pat_rep & 2) && (x < 0.0f || width <= x)) || ((c.pat_rep & 1) && (y < 0.0f || height <= y)))
+            return none;
+        float scale_x = fabsf(c.inv[0]) + fabsf(c.inv[2]);
+        float scale_y = fabsf(c.inv[1]) + fabsf(c.inv[3]);
+        scale_x = hi(1.0f, lo(scale_x, width * 0.25f));
+        scale_y = hi(1.0f, lo(scale_y, height * 0.25f));
+        float rx = 1.0f / scale_x, ry = 1.0f / scale_y;
+        x = x - 0.5f;
+        y = y - 0.5f;
+        int left = static_cast<int>(ceilf(x - scale_x * 2.0f));
+        int top = static_cast<int>(ceilf(y - scale_y * 2.0f));
+        int right = static_cast<int>(ceilf(x + scale_x * 2.0f));
+        int bottom = static_cast<int>(ceilf(y + scale_y * 2.0f));
+        float4 total = none;
+        float wsum = 0.0f;
+        const float4 *tex = s.texels + c.pat_first;
+        for (int py_ = top; py_ < bottom; ++py_) {
+            float wy = keys_weight(fabsf(ry * (static_cast<float>(py_) - y)));
+            int yy = py_ % c.pat_h;
+            if (yy < 0) yy += c.pat_h;
+            if (c.clamp) yy = py_ < 0 ? 0 : (py_ > c.pat_h - 1 ? c.pat_h - 1 : py_);
+            const float4 *rowp = tex + static_cast<size_t>(yy) * c.pat_w;
+            for (int px_ = left; px_ < right; ++px_) {
+                float wx = keys_weight(fabsf(rx * (static_cast<float>(px_) - x)));
+                int xx = px_ % c.pat_w;
+                if (xx < 0) xx += c.pat_w;
+                if (c.clamp) xx = px_ < 0 ? 0 : (px_ > c.pat_w - 1 ? c.pat_w - 1 : px_);
+                float w = wx * wy;
+                float4 t = rowp[xx];
+                total.x = total.x + t.x * w;
+                total.y = total.y + t.y * w;
+                total.z = total.z + t.z * w;
+                total.w = total.w + t.w * w;
+                wsum += w;
+            }
+        }
+        float r = 1.0f / wsum;
+        return make_float4(total.x * r, total.y * r, total.z * r, total.w * r);
+    }
+    float rx = x - c.p0x, ry = y - c.p0y;
+    float lx = c.p1x - c.p0x, ly = c.p1y - c.p0y;
+    float grad = rx * lx + ry * ly;
+    float span = lx * lx + ly * ly;
+    float offset;
+    if (c.paint == 2) {
+        if (span == 0.0f) return none;
+        offset = grad / span;
+    } else {
+        float initial = c.r0;
+        float change = c.r1 - initial;
+        float a = span - change * change;
+        float b = -2.0f * (grad + initial * change);
+        float cc = (rx * rx + ry * ry) - initial * initial;
+        float disc = b * b - 4.0f * a * cc;
+        if (disc < 0.0f || (span == 0.0f && change == 0.0f)) return none;
+        float root = sqrtf(disc);
+        float recip = 1.0f / (2.0f * a);
+        float o1 = (-b - root) * recip;
+        float o2 = (-b + root) * recip;
+        float rad1 = initial + change * o1;
+        float rad2 = initial + change * o2;
+        if (rad2 >= 0.0f) offset = o2;
+        else if (rad1 >= 0.0f) offset = o1;
+        else return none;
+    }
+    const float *stops = s.stop_off + c.stop_first;
+    const float4 *cols = s.stop_col + c.stop_first;
+    int n = c.stop_count, k = 0;
+    while (k < n && !(offset < stops[k])) ++k;   // std::upper_bound
+    if (k == 0) return premul(cols[0]);
+    if (k == n) return premul(cols[n - 1]);
+    float t = (offset - stops[k - 1]) / (stops[k] - stops[k - 1]);
+    float4 c0 = cols[k - 1], c1 = cols[k];
+    float4 m = make_float4(c0.x + t * (c1.x - c0.x), c0.y + t * (c1.y - c0.y), c0.z + t * (c1.z - c0.z),
+                           c0.w + t * (c1.w - c0.w));
+    return premul(m);
+}
+
+// Composite `fore` into `back` with a 4-bit operation code and clip
+// visibility (hpp:2522-2533, 2583-2591).
+__device__ __forceinline__ float4 blend(float4 back, float4 fore, int op, float vis) {
+    float mf = op & 1 ? back.w : 0.0f;
+    if (op & 2) mf = 1.0f - mf;
+    float mb = op & 4 ? fore.w : 0.0f;
+    if (op & 8) mb = 1.0f - mb;
+    float4 b = make_float4(fore.x * mf + back.x * mb, fore.y * mf + back.y * mb, fore.z * mf + back.z * mb,
+                           fore.w * mf + back.w * mb);
+    b.w = lo(b.w, 1.0f);
+    float iv = 1.0f - vis;
+    return make_float4(b.x * vis + back.x * iv, b.y * vis + back.y * iv, b.z * vis + back.z * iv,
+                       b.w * vis + back.w * iv);
+}
+
+// get_image_data's per-pixel conversion (hpp:3348-3381): unpremultiply,
+// clamp, delinearize, x255 plus the 4x4 Bayer threshold, truncate.
+__device__ __forceinline__ float delinearize(float v) {
+    return v < 0.0031308f ? 12.92f * v : 1.055f * powf(v, 1.0f / 2.4f) - 0.055f;
+}
+__device__ __forceinline__ uchar4 to_srgb8(float4 c, int cx, int cy) {
+    const float bayer[4][4] = {{0.03125f, 0.53125f, 0.15625f, 0.65625f},
+                               {0.78125f, 0.28125f, 0.90625f, 0.40625f},
+                               {0.21875f, 0.71875f, 0.09375f, 0.59375f},
+                               {0.96875f, 0.46875f, 0.84375f, 0.34375f}};
+    float4 u;
+    if (c.w < kVisible) {
+        u = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    } else {
+        float r = 1.0f / c.w;
+        u = make_float4(r * c.x, r * c.y, r * c.z, c.w);
+    }
+    u.x = lo(hi(u.x, 0.0f), 1.0f);
+    u.y = lo(hi(u.y, 0.0f), 1.0f);
+    u.z = lo(hi(u.z, 0.0f), 1.0f);
+    u.w = lo(hi(u.w, 0.0f), 1.0f);
+    float t = bayer[cy & 3][cx & 3];
+    float r = t + 255.0f * delinearize(u.x);
+    float g = t + 255.0f * delinearize(u.y);
+    float b = t + 255.0f * delinearize(u.z);
+    float a = t + 255.0f * u.w;
+    return make_uchar4(static_cast<unsigned char>(__float2int_rz(r) & 0xff),
+                       static_cast<unsigned char>(__float2int_rz(g) & 0xff),
+                       static_cast<unsigned char>(__float2int_rz(b) & 0xff),
+                       static_cast<unsigned char>(__float2int_rz(a) & 0xff));
+}
+
+}  // namespace cyg
+
+#endif

@@ -1,0 +1,627 @@
+// kernels.cuh -- CUDA kernels of the per-canvas ("plain") render path.
+//
+// The reference renders sparsely: sorted per-pixel signed-area runs are
+// walked row by row with float running sums.  Rows are independent, so each
+// step here is row-parallel and reproduces the reference's per-row float
+// operation order: runs are bucketed per row, each row is sorted, coalesced
+// and prefix-summed by one thread, and the pixels of the row are then
+// painted and composited in parallel by a warp carrying the row's running
+// sums forward.  Shadows, clip masks and the blur follow the same rule.
+// Fills and clips of Bezier paths are flattened on the GPU first, for the
+// whole flush at once.
+#ifndef CY_KERNELS_CUH
+#define CY_KERNELS_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device.cuh"
+
+namespace cyg {
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ int warp_id_global() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ int warps_total() { return (gridDim.x * blockDim.x) >> 5; }
+
+__device__ __forceinline__ long long warp_inclusive_scan(long long v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        long long n = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+// --------------------------------------------------------------- patterns
+// set_pattern / draw_image texels: premultiplied(linearized(rgba8 / 255))
+// (hpp:2841-2864).  `lut` holds linearized(i / 255) computed on the host.
+__global__ void k_pattern_prep(const uchar4 *__restrict__ src, float4 *__restrict__ dst, int n,
+                               const float *__restrict__ lut) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uchar4 c = src[i];
+    float a = static_cast<float>(c.w) / 255.0f;
+    dst[i] = make_float4(lut[c.x] * a, lut[c.y] * a, lut[c.z] * a, a);
+}
+
+// ------------------------------------------------------------- flattening
+__global__ void k_flat_count(const float2 *__restrict__ bez, const flat_item *__restrict__ items, int n,
+                             int32_t *__restrict__ counts) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flat_item it = items[i];
+    if (it.sub_end >= 0) { counts[i] = 1; return; }
+    counts[i] = flatten_cubic<false>(bez[it.pt], bez[it.pt + 1], bez[it.pt + 2], bez[it.pt + 3], nullptr, 0);
+}
+
+__global__ void k_flat_emit(const float2 *__restrict__ bez, const flat_item *__restrict__ items, int n,
+                            const int32_t *__restrict__ offs, float2 *__restrict__ pts,
+                            int32_t *__restrict__ prev, int64_t cap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flat_item it = items[i];
+    int o = offs[i];
+    int cnt = offs[i + 1] - o;
+    if (o < 0 || static_cast<int64_t>(o) + cnt > cap) return;
+    if (it.sub_end >= 0) {
+        pts[o] = bez[it.pt];
+        prev[o] = offs[it.sub_end] - 1;   // closing segment from the subpath's last point
+        return;
+    }
+    flatten_cubic<true>(bez[it.pt], bez[it.pt + 1], bez[it.pt + 2], bez[it.pt + 3], pts + o, cnt);
+    for (int k = 0; k < cnt; ++k) prev[o + k] = o + k - 1;
+}
+
+// ------------------------------------------------------------------- scan
+// Exclusive scan of int32 in tiles of 4096 (1024 threads x 4).
+__global__ void k_scan_tiles(const int32_t *__restrict__ in, int32_t *__restrict__ out, int n,
+                             int32_t *__restrict__ tile_sums) {
+    __shared__ int32_t warp_sums[32];
+    int base = blockIdx.x * 4096 + threadIdx.x * 4;
+    int32_t v[4];
+    int32_t local = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        v[j] = base + j < n ? in[base + j] : 0;
+        local += v[j];
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_sums[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int32_t s = warp_sums[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        warp_sums[lane] = s;
+    }
+    __syncthreads();
+    int32_t run = incl - local + (w > 0 ? warp_sums[w - 1] : 0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (base + j < n) out[base + j] = run;
+        run += v[j];
+    }
+    if (threadIdx.x == 1023 && tile_sums) tile_sums[blockIdx.x] = warp_sums[31];
+}
+
+__global__ void k_scan_add(int32_t *__restrict__ out, int n, const int32_t *__restrict__ tile_offs) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] += tile_offs[i >> 12];
+}
+
+// ------------------------------------------------------- scan conversion
+// lines_to_runs (hpp:2193-2253), row-parallel.  Every queued scan
+// conversion (a draw, its shadow, a clip) is a "job".  Pass 1 counts the
+// nonzero signed-area changes per job row and the job's exact bounds; pass 2
+// writes them into per-row buckets; then every row of every job is sorted,
+// coalesced and prefix-summed independently.
+struct scan_job {
+    int32_t geom;          // 0: host polylines, 1: GPU-flattened polylines
+    int32_t line_first;    // first polyline point
+    int32_t seg_first;     // prefix of segment counts over jobs
+    int32_t seg_count;
+    int32_t row_base;      // first row of this job in the shared row arrays
+    int32_t rows, cols;    // rows and cells per row of the (padded) canvas
+    float width, height;   // clip rectangle [0,width] x [0,height]
+    float offx, offy;      // added to every point first (shadow offset)
+    int32_t pad[2];
+};
+
+struct job_tables {
+    const scan_job *jobs;
+    int n_jobs;
+    const float2 *pts[2];
+    const int32_t *prev[2];
+    cover_box *boxes;       // one per job
+    int32_t *row_cnt;       // count pass: nonzero runs per row (all jobs)
+    const int32_t *row_off; // emit pass: bucket offsets
+    int32_t *row_cur;       // emit pass: bucket cursors
+    run *runs;
+};
+
+template <bool EMIT>
+struct run_emit {
+    const job_tables *t;
+    const scan_job *j;
+    int x0, x1, y0, y1;
+    long long first;
+    __device__ void operator()(int x, int y, float d) {
+        if (y < 0 || y >= j->rows || x < 0 || x >= j->cols) return;
+        if (!EMIT) {
+            long long key = (static_cast<long long>(y) << 32) | static_cast<long long>(x);
+            if (key < first) first = key;
+        }
+        if (d == 0.0f) return;
+        int row = j->row_base + y;
+        if (EMIT) {
+            int k = atomicAdd(t->row_cur + row, 1);
+            int n = t->row_off[row + 1] - t->row_off[row];
+            if (k < n) t->runs[t->row_off[row] + k] = run{x, d};
+        } else {
+            atomicAdd(t->row_cnt + row, 1);
+            x0 = x < x0 ? x : x0;
+            x1 = x > x1 ? x : x1;
+            y0 = y < y0 ? y : y0;
+            y1 = y > y1 ? y : y1;
+        }
+    }
+};
+
+__device__ __forceinline__ int job_of_segment(const job_tables &t, int s) {
+    int lo_i = 0, hi_i = t.n_jobs;   // last job with seg_first <= s
+    while (hi_i - lo_i > 1) {
+        int mid = (lo_i + hi_i) >> 1;
+        if (t.jobs[mid].seg_first <= s) lo_i = mid; else hi_i = mid;
+    }
+    return lo_i;
+}
+
+// One warp per segment, one lane per pixel row of each clipped piece.
+template <bool EMIT>
+__global__ void k_runs(job_tables t, int total_segments) {
+    int lane = threadIdx.x & 31;
+    for (int s = warp_id_global(); s < total_segments; s += warps_total()) {
+        int ji = job_of_segment(t, s);
+        const scan_job &j = t.jobs[ji];
+        int k = j.line_first + (s - j.seg_first);
+        int g = j.geom ? 1 : 0;
+        float2 b = t.pts[g][k];
+        float2 a = t.pts[g][t.prev[g][k]];
+        a = f2(j.offx + a.x, j.offy + a.y);
+        b = f2(j.offx + b.x, j.offy + b.y);
+        run_emit<EMIT> e;
+        e.t = &t;
+        e.j = &j;
+        e.x0 = 0x7fffffff; e.x1 = -0x7fffffff; e.y0 = 0x7fffffff; e.y1 = -0x7fffffff;
+        e.first = 0x7fffffffffffffffll;
+        float2 pa[3], pb[3];
+        int np = clip_segment(a, b, j.width, j.height, pa, pb);
+        for (int q = 0; q < np; ++q) {
+            dda_piece p;
+            if (!dda_setup(pa[q], pb[q], p)) continue;
+            int nrows = p.nrows < j.rows + 2 ? p.nrows : j.rows + 2;
+            for (int r = lane; r < nrows; r += 32) dda_row(p, r, e);
+        }
+        if (!EMIT) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                e.x0 = min(e.x0, __shfl_xor_sync(0xffffffffu, e.x0, o));
+                e.x1 = max(e.x1, __shfl_xor_sync(0xffffffffu, e.x1, o));
+                e.y0 = min(e.y0, __shfl_xor_sync(0xffffffffu, e.y0, o));
+                e.y1 = max(e.y1, __shfl_xor_sync(0xffffffffu, e.y1, o));
+                e.first = min(e.first, __shfl_xor_sync(0xffffffffu, e.first, o));
+            }
+            if (lane == 0) {
+                cover_box *box = t.boxes + ji;
+                if (e.x0 <= e.x1) {
+                    atomicMin(&box->x0, e.x0);
+                    atomicMax(&box->x1, e.x1);
+                    atomicMin(&box->y0, e.y0);
+                    atomicMax(&box->y1, e.y1);
+                }
+                if (e.first != 0x7fffffffffffffffll)
+                    atomicMin(reinterpret_cast<long long *>(&box->first_key), e.first);
+            }
+        }
+    }
+}
+
+__global__ void k_box_init(cover_box *boxes, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    boxes[i].x0 = 0x7fffffff;
+    boxes[i].x1 = -0x7fffffff;
+    boxes[i].y0 = 0x7fffffff;
+    boxes[i].y1 = -0x7fffffff;
+    boxes[i].first_key = 0x7fffffffffffffffll;
+}
+
+// The reference's run order within a row (hpp:2172-2181), with ties of equal
+// magnitude broken by sign so the order does not depend on arrival order.
+__device__ __forceinline__ bool run_less(const run &a, const run &b) {
+    if (a.x != b.x) return a.x < b.x;
+    float fa = fabsf(a.delta), fb = fabsf(b.delta);
+    if (fa != fb) return fa < fb;
+    return a.delta < b.delta;
+}
+
+__device__ void sort_runs(run *r, int n) {
+    // Shell sort with Ciura's gaps (plain insertion sort for short rows).
+    const int gaps[] = {1750, 701, 301, 132, 57, 23, 10, 4, 1};
+    for (int gi = 0; gi < 9; ++gi) {
+        int g = gaps[gi];
+        if (g >= n) continue;
+        for (int i = g; i < n; ++i) {
+            run v = r[i];
+            int j = i;
+            for (; j >= g && run_less(v, r[j - g]); j -= g) r[j] = r[j - g];
+            r[j] = v;
+        }
+    }
+}
+
+// Sort and coalesce one row's runs exactly as the reference does after its
+// std::sort (hpp:2243-2252), then store the running coverage sum after each
+// coalesced cell (the value render_main's walk holds from that cell on).
+// One thread per row over all rows of all jobs.
+__global__ void k_rows(const int32_t *__restrict__ row_off, int32_t *__restrict__ row_cnt,
+                       int32_t *__restrict__ row_cur, int32_t *__restrict__ row_len, run *__restrict__ runs,
+                       float *__restrict__ sums, int total_rows) {
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= total_rows) return;
+    int n = row_cnt[y];
+    int cap = row_off[y + 1] - row_off[y];
+    if (n > cap) n = cap;
+    run *r = runs + row_off[y];
+    float *sm = sums + row_off[y];
+    sort_runs(r, n);
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+        if (m > 0 && r[m - 1].x == r[i].x) r[m - 1].delta += r[i].delta;
+        else r[m++] = r[i];
+    }
+    float sum = 0.0f;
+    for (int k = 0; k < m; ++k) {
+        sum += r[k].delta;
+        sm[k] = sum;
+    }
+    row_len[y] = m;
+    row_cnt[y] = 0;
+    row_cur[y] = 0;
+}
+
+// Running sum in force at pixel x: the sum after the last coalesced run at or
+// left of x (0 before the first run).
+__device__ __forceinline__ float sum_at(const run *r, const float *sm, int n, int x) {
+    int lo_i = 0, hi_i = n;
+    while (lo_i < hi_i) {
+        int mid = (lo_i + hi_i) >> 1;
+        if (r[mid].x <= x) lo_i = mid + 1; else hi_i = mid;
+    }
+    return lo_i > 0 ? sm[lo_i - 1] : 0.0f;
+}
+
+struct row_view {
+    const int32_t *row_off;
+    const int32_t *row_len;
+    const run *runs;
+    const float *sums;
+};
+
+// ---------------------------------------------------------- main render
+struct paint_args {
+    const command *cmd;
+    float4 *bitmap;
+    int W, H;
+    row_view rv;
+    int row_base;
+    const float *vis;    // dense clip visibility, null for the whole canvas
+    int y_begin, y_end;
+    paint_src src;
+};
+
+// render_main's span walk (hpp:2551-2605) as a dense pass: each pixel takes
+// the row's running coverage sum in force at its x, is painted, and is
+// composited through the clip visibility.  Warp per row.
+__global__ void k_paint(paint_args a) {
+    int lane = threadIdx.x & 31;
+    const command &c = *a.cmd;
+    const int op = c.op;
+    const bool clearing = !(op & 8);
+    for (int y = a.y_begin + warp_id_global(); y < a.y_end; y += warps_total()) {
+        int row = a.row_base + y;
+        int n = a.rv.row_len[row];
+        if (!clearing && n == 0) continue;
+        const run *r = a.rv.runs + a.rv.row_off[row];
+        const float *sm = a.rv.sums + a.rv.row_off[row];
+        int xs = clearing ? 0 : r[0].x;
+        int xe = clearing ? a.W - 1 : min(r[n - 1].x, a.W - 1);
+        for (int x = xs + lane; x <= xe; x += 32) {
+            float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+            float vis = a.vis ? a.vis[static_cast<size_t>(y) * a.W + x] : 1.0f;
+            if ((cov >= kVisible || clearing) && vis >= kVisible) {
+                float4 *px = a.bitmap + static_cast<size_t>(y) * a.W + x;
+                float4 back = *px;
+                float4 p = paint_at(c, a.src, static_cast<float>(x) + 0.5f, static_cast<float>(y) + 0.5f);
+                float k = cov * c.alpha;
+                float4 fore = make_float4(p.x * k, p.y * k, p.z * k, p.w * k);
+                *px = blend(back, fore, op, vis);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ clip
+struct clip_args {
+    // path runs (sorted, coalesced) of this clip, rows from p_base
+    const int32_t *p_off, *p_len;
+    const run *p_runs;
+    int p_base;
+    // old mask (null runs = the whole canvas: per row {0,+1}, {W,-1})
+    const int32_t *o_off, *o_len;
+    const run *o_runs;
+    const int *o_last_row;   // last row holding old-mask runs (null: H-1)
+    const cover_box *p_box;  // bounds of the path runs
+    // new mask
+    const int32_t *n_off;
+    int32_t *n_len;
+    run *n_runs;
+    int *n_last_row;
+    int W, H;
+};
+
+// clip() (hpp:3057-3099) for one row: merge the path runs with the old mask
+// runs in the reference's order and emit changes of the product coverage.
+// The reference stops its single merge loop when either list runs out, so
+// the row where that happens is cut short and later rows stay empty.
+__global__ void k_clip_rows(clip_args a) {
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= a.H) return;
+    int o_last = a.o_last_row ? *a.o_last_row : a.H - 1;
+    int p_last = a.p_box->x0 <= a.p_box->x1 ? a.p_box->y1 : -1;
+    int stop_row = min(p_last, o_last);
+    int m = 0;
+    run *out = a.n_runs + a.n_off[y];
+    int cap = a.n_off[y + 1] - a.n_off[y];
+    if (y <= stop_row) {
+        const run *p = a.p_runs + a.p_off[a.p_base + y];
+        int pn = a.p_len[a.p_base + y];
+        run dflt[2] = {run{0, 1.0f}, run{a.W, -1.0f}};
+        const run *o = a.o_runs ? a.o_runs + a.o_off[y] : dflt;
+        int on = a.o_runs ? a.o_len[y] : 2;
+        bool path_ends = y == p_last, mask_ends = y == o_last;
+        int i1 = 0, i2 = 0;
+        float last = 0.0f, s1 = 0.0f, s2 = 0.0f;
+        for (;;) {
+            bool p_left = i1 < pn, o_left = i2 < on;
+            if (y == stop_row) {
+                if ((path_ends && !p_left) || (mask_ends && !o_left)) break;
+            }
+            if (!p_left && !o_left) break;
+            bool which;
+            if (!p_left) which = false;
+            else if (!o_left) which = true;
+            else which = p[i1].x < o[i2].x || (p[i1].x == o[i2].x && fabsf(p[i1].delta) < fabsf(o[i2].delta));
+            int nx = which ? p[i1].x : o[i2].x;
+            if (which) s1 += p[i1++].delta;
+            else s2 += o[i2++].delta;
+            float vis = lo(fabsf(s1), 1.0f) * lo(fabsf(s2), 1.0f);
+            if (vis == last) continue;
+            if (m > 0 && out[m - 1].x == nx) out[m - 1].delta += vis - last;
+            else if (m < cap) out[m++] = run{nx, vis - last};
+            last = vis;
+        }
+    }
+    a.n_len[y] = m;
+    if (m > 0) atomicMax(a.n_last_row, y);
+}
+
+// Run capacity of each row of a new clip mask: the path's raw runs plus the
+// old mask's runs (2 per row for the whole canvas).
+__global__ void k_clip_caps(const int32_t *path_off, const int32_t *old_off, int H, int32_t *caps) {
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= H) return;
+    int p = path_off[y + 1] - path_off[y];
+    int o = old_off ? old_off[y + 1] - old_off[y] : 2;
+    caps[y] = p + o;
+}
+
+// Running sums of a mask's runs (one thread per row): the clip visibility in
+// force from each run on is min(|sum|, 1) (hpp:2568-2570).
+__global__ void k_mask_prefix(const int32_t *off, const int32_t *len, const run *runs, float *sums, int H) {
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= H) return;
+    const run *r = runs + off[y];
+    float *sm = sums + off[y];
+    int n = len[y];
+    float sum = 0.0f;
+    for (int j = 0; j < n; ++j) {
+        sum += r[j].delta;
+        sm[j] = sum;
+    }
+}
+
+// Dense visibility from the mask runs (warp per row).  Pixels outside the
+// row's first..last run are never visited by the reference's walks: 0.
+__global__ void k_mask_fill(const int32_t *off, const int32_t *len, const run *runs, const float *sums, int W,
+                            int H, float *vis) {
+    int lane = threadIdx.x & 31;
+    for (int y = warp_id_global(); y < H; y += warps_total()) {
+        const run *r = runs + off[y];
+        const float *sm = sums + off[y];
+        int n = len[y];
+        int first = n ? r[0].x : 0x7fffffff, last = n ? r[n - 1].x : -1;
+        for (int x = lane; x < W; x += 32) {
+            float v = 0.0f;
+            if (x >= first && x <= last) v = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+            vis[static_cast<size_t>(y) * W + x] = v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- shadows
+struct shadow_rect { int left, right, top, bottom, width, height; };
+
+// Working rectangle of render_shadow (hpp:2409-2426) from the exact bounds of
+// the padded scan conversion, including the reference's quirk that the
+// first run after sorting is kept even when its delta is zero.
+__global__ void k_shadow_rect(const cover_box *box, int W, int H, int border, shadow_rect *out) {
+    int ext_w = W + 2 * border, ext_h = H + 2 * border;
+    int left = ext_w, right = 0, top = ext_h, bottom = 0;
+    cover_box b = *box;
+    if (b.x0 <= b.x1) {
+        left = min(left, b.x0); right = max(right, b.x1);
+        top = min(top, b.y0); bottom = max(bottom, b.y1);
+    }
+    if (b.first_key != 0x7fffffffffffffffll) {
+        int fx = static_cast<int>(b.first_key & 0xffffffffll), fy = static_cast<int>(b.first_key >> 32);
+        left = min(left, fx); right = max(right, fx);
+        top = min(top, fy); bottom = max(bottom, fy);
+    }
+    left = max(left - border, 0);
+    right = min(right + border, ext_w) + 1;
+    top = max(top - border, 0);
+    bottom = min(bottom + border, ext_h);
+    shadow_rect r;
+    r.left = left; r.right = right; r.top = top; r.bottom = bottom;
+    r.width = max(right - left, 0);
+    r.height = max(bottom - top, 0);
+    *out = r;
+}
+
+// Alpha raster of the shadow (hpp:2430-2452), warp per working row: pixels
+// between the row's first and last run get coverage times paint alpha.
+__global__ void k_shadow_raster(const command *cmd, paint_src src, row_view rv, int row_base,
+                                const shadow_rect *rect, float *__restrict__ out) {
+    int lane = threadIdx.x & 31;
+    const command &c = *cmd;
+    const shadow_rect rc = *rect;
+    for (int y = rc.top + warp_id_global(); y < rc.bottom; y += warps_total()) {
+        int row = row_base + y;
+        int n = rv.row_len[row];
+        const run *r = rv.runs + rv.row_off[row];
+        const float *sm = rv.sums + rv.row_off[row];
+        int first = n ? r[0].x : 0x7fffffff, last = n ? r[n - 1].x : -1;
+        for (int x = rc.left + lane; x < rc.right; x += 32) {
+            float val = 0.0f;
+            if (x >= first && x <= last) {
+                float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+                if (cov >= kVisible) {
+                    float px = (static_cast<float>(x) + 0.5f) - c.sh_offx;
+                    float py = (static_cast<float>(y) + 0.5f) - c.sh_offy;
+                    val = cov * paint_at(c, src, px, py).w;
+                }
+            }
+            out[static_cast<size_t>(y - rc.top) * rc.width + (x - rc.left)] = val;
+        }
+    }
+}
+
+// The reference's extended box blur (Gwosdek et al., hpp:2453-2503): three
+// running-sum passes along each row, then along each column, with the same
+// float operation order (one thread per row, then per column).  `tmp` holds
+// one working copy per row/column.
+__global__ void k_blur_rows(float *s, float *tmp, const shadow_rect *rect, int radius, float w1, float w2) {
+    const shadow_rect rc = *rect;
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= rc.height) return;
+    size_t width = rc.width, r = radius;
+    float *row = s + static_cast<size_t>(y) * width;
+    float *t = tmp + static_cast<size_t>(y) * width;
+    for (int pass = 0; pass < 3; ++pass) {
+        for (size_t x = 0; x < width; ++x) t[x] = row[x];
+        float run = r + 1 < width ? w1 * t[r + 1] : 0.0f;
+        for (size_t x = 0; x <= r && x < width; ++x) run += (w1 + w2) * t[x];
+        row[0] = run;
+        for (size_t x = 1; x < width; ++x) {
+            if (x >= r + 1) run -= w2 * t[x - r - 1];
+            if (x >= r + 2) run -= w1 * t[x - r - 2];
+            if (x + r < width) run += w2 * t[x + r];
+            if (x + r + 1 < width) run += w1 * t[x + r + 1];
+            row[x] = run;
+        }
+    }
+}
+
+__global__ void k_blur_cols(float *s, float *tmp, const shadow_rect *rect, int radius, float w1, float w2) {
+    const shadow_rect rc = *rect;
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= rc.width) return;
+    size_t width = rc.width, height = rc.height, r = radius;
+    for (int pass = 0; pass < 3; ++pass) {
+        for (size_t y = 0; y < height; ++y) tmp[y * width + x] = s[y * width + x];
+        float run = r + 1 < height ? w1 * tmp[(r + 1) * width + x] : 0.0f;
+        for (size_t y = 0; y <= r && y < height; ++y) run += (w1 + w2) * tmp[y * width + x];
+        if (height > 0) s[x] = run;
+        for (size_t y = 1; y < height; ++y) {
+            if (y >= r + 1) run -= w2 * tmp[(y - r - 1) * width + x];
+            if (y >= r + 2) run -= w1 * tmp[(y - r - 2) * width + x];
+            if (y + r < height) run += w2 * tmp[(y + r) * width + x];
+            if (y + r + 1 < height) run += w1 * tmp[(y + r + 1) * width + x];
+            s[y * width + x] = run;
+        }
+    }
+}
+
+// Shadow composite through the clip visibility (hpp:2504-2538); nothing is
+// cleared outside the working rectangle.
+__global__ void k_shadow_composite(const command *cmd, float4 *bitmap, int W, int H, const float *visp,
+                                   const shadow_rect *rect, const float *__restrict__ sh) {
+    const command &c = *cmd;
+    const shadow_rect r = *rect;
+    if (r.width <= 0 || r.height <= 0) return;
+    int b = c.sh_border;
+    int x0 = max(0, r.left - b), x1 = min(W, r.right - b);
+    int y0 = max(0, r.top - b), y1 = min(H, r.bottom - b);
+    int x = x0 + blockIdx.x * blockDim.x + threadIdx.x;
+    int y = y0 + blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= x1 || y >= y1) return;
+    float vis = visp ? visp[static_cast<size_t>(y) * W + x] : 1.0f;
+    if (vis < kVisible) return;
+    float s = sh[static_cast<size_t>(y + b - r.top) * r.width + (x + b - r.left)];
+    float k = c.alpha * s;
+    float4 fore = make_float4(c.sh_color[0] * k, c.sh_color[1] * k, c.sh_color[2] * k, c.sh_color[3] * k);
+    float4 *px = bitmap + static_cast<size_t>(y) * W + x;
+    *px = blend(*px, fore, c.op, vis);
+}
+
+// ------------------------------------------------------------ pixel I/O
+// put_image_data (hpp:3383-3408).
+__global__ void k_put(const command *cmd, const uint8_t *__restrict__ pixels, float4 *__restrict__ bitmap, int W,
+                      int H, const float *__restrict__ lut) {
+    const command &c = *cmd;
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= c.put_w || iy >= c.put_h) return;
+    int cx = c.put_x + ix, cy = c.put_y + iy;
+    if (cx < 0 || W <= cx || cy < 0 || H <= cy) return;
+    const uint8_t *p = pixels + c.put_first + (static_cast<size_t>(iy) * c.put_w + ix) * 4;
+    float a = static_cast<float>(p[3]) / 255.0f;
+    bitmap[static_cast<size_t>(cy) * W + cx] = make_float4(lut[p[0]] * a, lut[p[1]] * a, lut[p[2]] * a, a);
+}
+
+// get_image_data (hpp:3348-3381) into a compact w x h RGBA8 buffer.
+__global__ void k_get(const float4 *__restrict__ bitmap, int W, int H, uchar4 *__restrict__ out, int w, int h,
+                      int x0, int y0) {
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= w || iy >= h) return;
+    int cx = x0 + ix, cy = y0 + iy;
+    float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (0 <= cx && cx < W && 0 <= cy && cy < H) c = bitmap[static_cast<size_t>(cy) * W + cx];
+    out[static_cast<size_t>(iy) * w + ix] = to_srgb8(c, cx, cy);
+}
+
+}  // namespace cyg
+
+#endif

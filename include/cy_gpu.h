@@ -1,0 +1,128 @@
+/*
+ * cy_gpu.h -- C ABI of the GB300 render engine behind canvas_ity::canvas.
+ *
+ * The reference library renders on the CPU inside the canvas class; the
+ * host class of this library (include/canvas_ity.hpp) keeps the state and
+ * geometry work and hands each draw to these entry points.  Every function
+ * names the reference code it replaces (hpp = src/canvas_ity.hpp).
+ *
+ * Plain pointers and sizes only.  All input buffers are copied before the
+ * call returns.  Work is queued per context, in call order, on the
+ * context's own CUDA stream, and runs when pixels are read (cy_get_image),
+ * on cy_flush, or when the queue grows large.  Status codes: 0 success,
+ * negative on failure (CY_E*).  A context is not thread-safe; separate
+ * contexts may be used from separate threads.
+ */
+#ifndef CY_GPU_H
+#define CY_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CY_OK 0
+#define CY_EINVAL (-1)    /* invalid argument                               */
+#define CY_ENOMEM (-2)    /* device or pinned host allocation failed        */
+#define CY_ECUDA (-3)     /* a CUDA call failed                             */
+#define CY_ENODEV (-4)    /* no usable CUDA device                          */
+#define CY_EBUDGET (-5)   /* request exceeds the admission memory budget     */
+
+typedef struct cy_ctx cy_ctx;
+
+/* Paint of one draw: the reference's paint_brush (hpp:165-168) resolved at
+ * draw time, plus the canvas inverse transform used to map pixel centres
+ * into pattern / gradient space (paint_pixel, hpp:2265-2377). */
+enum cy_paint_kind {
+    CY_PAINT_NONE = 0,     /* empty brush: transparent black            */
+    CY_PAINT_SOLID = 1,    /* color[] premultiplied linear              */
+    CY_PAINT_LINEAR = 2,
+    CY_PAINT_RADIAL = 3,
+    CY_PAINT_PATTERN = 4
+};
+
+typedef struct cy_paint {
+    int kind;                  /* enum cy_paint_kind                           */
+    int clamp_edges;           /* 1 for draw_image (clamp), 0 for patterns (wrap) */
+    float inverse[6];          /* a b c d e f of the inverse canvas transform  */
+    float color[4];            /* SOLID: premultiplied linear RGBA             */
+    float start[2], end[2];    /* gradient geometry                            */
+    float start_radius, end_radius;
+    const float *stop_offsets; /* n_stops offsets, sorted ascending            */
+    const float *stop_colors;  /* n_stops * 4, linear straight-alpha RGBA      */
+    int n_stops;
+    const unsigned char *pattern; /* PATTERN: sRGB RGBA8, width*4 row stride   */
+    int pattern_width, pattern_height;
+    int repetition;            /* repeat, repeat_x, repeat_y, no_repeat        */
+} cy_paint;
+
+/* Compositing state of one draw (hpp:2395-2605). */
+typedef struct cy_draw_state {
+    int operation;             /* composite_operation value                   */
+    float global_alpha;
+    int mask;                  /* clip mask id; 0 = whole canvas              */
+    float shadow_color[4];     /* premultiplied linear                        */
+    float shadow_blur;
+    float shadow_offset_x, shadow_offset_y;
+} cy_draw_state;
+
+/* canvas::canvas (hpp:2607-2644): transparent W x H canvas, full clip. */
+int cy_ctx_create(int width, int height, cy_ctx **out);
+
+/* canvas::~canvas (hpp:2646-2655). */
+void cy_ctx_destroy(cy_ctx *ctx);
+
+/* fill() of a Bezier path: path_to_lines(false) + render_main
+ * (hpp:3044-3048, 1495-1524, 2551-2605).  `points` holds device-space x,y
+ * pairs laid out as the reference's bezier_path: each subpath is one start
+ * point followed by 3 points per cubic; subpath_counts[i] is its point count
+ * (1 + 3k).  Flattening happens on the GPU. */
+int cy_fill_path(cy_ctx *ctx, const float *points, const int *subpath_counts, int n_subpaths,
+                 const cy_paint *paint, const cy_draw_state *state);
+
+/* render_main on ready polylines (hpp:2551-2605): strokes after host stroke
+ * expansion, rectangles, images and text.  Every subpath is implicitly
+ * closed, as in lines_to_runs (hpp:2193-2253). */
+int cy_fill_lines(cy_ctx *ctx, const float *points, const int *subpath_counts, int n_subpaths,
+                  const cy_paint *paint, const cy_draw_state *state);
+
+/* clip() (hpp:3057-3099): intersects mask `mask_in` with the nonzero
+ * coverage of the Bezier path; the new mask id is written to *mask_out.
+ * Mask ids are reference counted: a new mask starts with one reference. */
+int cy_clip_path(cy_ctx *ctx, const float *points, const int *subpath_counts, int n_subpaths,
+                 int mask_in, int *mask_out);
+
+/* Reference counting of mask ids for save()/restore() (hpp:3410-3465). */
+int cy_mask_retain(cy_ctx *ctx, int mask);
+int cy_mask_release(cy_ctx *ctx, int mask);
+
+/* get_image_data (hpp:3348-3381): runs queued work, then converts the
+ * rectangle to unpremultiplied sRGB RGBA8 with the 4x4 ordered dither. */
+int cy_get_image(cy_ctx *ctx, unsigned char *image, int width, int height, int stride, int x, int y);
+
+/* put_image_data (hpp:3383-3408), ordered with queued draws. */
+int cy_put_image(cy_ctx *ctx, const unsigned char *image, int width, int height, int stride,
+                 int x, int y);
+
+/* Extension, no reference counterpart: runs queued work, then copies the
+ * canvas's premultiplied linear float RGBA pixels (the reference's private
+ * `bitmap`, hpp:1171) into out[W*H*4].  Used to check coverage exactly. */
+int cy_read_linear(cy_ctx *ctx, float *out);
+
+/* Run all queued work and wait for it. */
+int cy_flush(cy_ctx *ctx);
+
+/* First failure seen by the context (0 if none). */
+int cy_ctx_status(const cy_ctx *ctx);
+
+/* Engine selection for contexts created afterwards in this thread:
+ * 0 = tile engine (whole flush in one persistent launch, default),
+ * 1 = plain engine (per-draw launches over the float canvas). */
+void cy_set_engine(int engine);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CY_GPU_H */

@@ -53,7 +53,8 @@ struct output {
 
 // Returns 0 on success, -1 on a malformed or truncated trace.
 template <class Traits>
-int replay(const uint8_t *data, size_t size, output &out) {
+int replay(const uint8_t *data, size_t size, output &out,
+           std::unique_ptr<typename Traits::canvas_type> *keep = nullptr) {
     typedef typename Traits::canvas_type canvas_type;
     typedef typename Traits::brush_type brush_type;
     reader in(data, size);
@@ -301,6 +302,7 @@ int replay(const uint8_t *data, size_t size, output &out) {
         }
         if (!in.ok) return -1;
     }
+    if (keep) *keep = std::move(c);
     return 0;
 }
 

@@ -84,6 +84,25 @@ def replay(trace: bytes) -> Tuple[bytes, List[float]]:
     return _oracle.replay(trace)
 
 
+def replay_linear(trace: bytes, width: int, height: int):
+    """Replay through the oracle; return the final float canvas (H, W, 4)."""
+    import numpy as np
+    global _oracle
+    if _oracle is None:
+        _oracle = _Lib(build(), "cyo_replay")
+    fn = _oracle.lib.cyo_replay_linear
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t,
+                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    out = np.zeros((height, width, 4), np.float32)
+    w, h = ctypes.c_int(0), ctypes.c_int(0)
+    rc = fn(trace, len(trace), out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), out.size,
+            ctypes.byref(w), ctypes.byref(h))
+    if rc != 0:
+        raise ValueError(f"oracle replay failed with status {rc}")
+    return out
+
+
 def reference_available() -> bool:
     return os.path.exists(REF_SO) or build_reference() is not None
 

@@ -201,6 +201,7 @@ public:
     void put_image_data(const unsigned char *img, int w, int h, int stride, int x, int y);
     void save();
     void restore();
+    const std::vector<col> &pixels() const { return bitmap; }
 
 private:
     struct state {
@@ -1450,4 +1451,21 @@ int cyo_replay(const void *trace, size_t trace_len, void *images, size_t images_
                                                      results, results_cap, results_len);
 }
 
+}
+
+extern "C" int cyo_replay_linear(const void *trace, size_t trace_len, float *out, size_t out_floats, int *width,
+                                 int *height) {
+    cy_trace::output sink;
+    std::unique_ptr<cyo::canvas> keep;
+    int rc = cy_trace::replay<cyo::traits>(static_cast<const uint8_t *>(trace), trace_len, sink, &keep);
+    if (rc != 0 || !keep) return rc ? rc : -1;
+    const std::vector<cyo::col> &px = keep->pixels();
+    int w = 0, h = 0;
+    std::memcpy(&w, static_cast<const uint8_t *>(trace) + 12, 4);
+    std::memcpy(&h, static_cast<const uint8_t *>(trace) + 16, 4);
+    if (width) *width = w;
+    if (height) *height = h;
+    if (px.size() * 4 > out_floats) return -2;
+    std::memcpy(out, px.data(), px.size() * sizeof(cyo::col));
+    return 0;
 }

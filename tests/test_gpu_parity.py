@@ -1,0 +1,140 @@
+"""GPU parity: the GB300 canvas against the reference's own outputs and the oracle.
+
+Tolerances (the contract for this rasteriser):
+  * RGBA8: at most MAX_LSB difference per channel at every pixel, and at least
+    MIN_IDENTICAL of the pixels identical;
+  * float coverage: within COVERAGE_TOL absolute;
+  * the reference test suite's own LSH hash within 5 bits of its golden value.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from canvas_ity_gb300 import native, scenes
+from canvas_ity_gb300 import trace as T
+import cy_hash
+import golden_util as G
+
+pytestmark = pytest.mark.gpu
+
+MAX_LSB = 1
+MIN_IDENTICAL = 0.995
+COVERAGE_TOL = 1e-5
+ENGINES = {"plain": 1}
+MANIFEST = G.manifest()
+
+
+def assert_images_close(got, want, what):
+    assert got.shape == want.shape, what
+    maxd, frac = G.compare(got, want)
+    assert maxd <= MAX_LSB, f"{what}: max channel difference {maxd}"
+    assert frac <= 1.0 - MIN_IDENTICAL, f"{what}: {frac:.4%} of pixels differ"
+
+
+@pytest.fixture(scope="module", params=sorted(ENGINES))
+def engine(request):
+    native.set_engine(ENGINES[request.param])
+    return request.param
+
+
+@pytest.mark.parametrize("entry", MANIFEST, ids=[e["name"] for e in MANIFEST])
+def test_reference_suite(engine, entry):
+    tb = G.load_fixture(entry)
+    t = T.parse(tb)
+    raw, results = native.replay(tb)
+    got = G.split_images(tb, raw)
+    want = [img for _, _, img in t.expected_images()]
+    assert len(got) == len(want)
+    for i, (g, w) in enumerate(zip(got, want)):
+        assert_images_close(g, w, f"{entry['name']} read {i}")
+    assert results == t.expected_results()
+    assert cy_hash.hamming(cy_hash.hash_image(got[-1]), entry["golden_hash"]) <= 5
+
+
+@pytest.mark.parametrize("config", ["c0_small", "c1_small", "c2_small", "mixed_small"])
+@pytest.mark.parametrize("seed", range(4))
+def test_seeded_scene_vs_oracle(engine, config, seed):
+    tb = scenes.small_scene(config, seed)
+    got = G.split_images(tb, native.replay(tb)[0])
+    want = G.split_images(tb, oracle.replay(tb)[0])
+    for g, w in zip(got, want):
+        assert_images_close(g, w, f"{config}/{seed}")
+
+
+@pytest.mark.parametrize("config", ["c0", "c1"])
+def test_full_size_config_vs_oracle(engine, config):
+    tb = scenes.CONFIGS[config]()
+    got = G.split_images(tb, native.replay(tb)[0])[-1]
+    want = G.split_images(tb, oracle.replay(tb)[0])[-1]
+    assert_images_close(got, want, config)
+
+
+def test_c2_size_vs_oracle(engine):
+    """2048x2048 paint/composite scene (clip, 11 ops, gradients, patterns,
+    shadows) with 60 paths so the CPU oracle finishes in seconds."""
+    tb = scenes.c2(paths=60)
+    got = G.split_images(tb, native.replay(tb)[0])[-1]
+    want = G.split_images(tb, oracle.replay(tb)[0])[-1]
+    assert_images_close(got, want, "c2/60")
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_float_coverage(engine, seed):
+    """One opaque white nonzero fill on a blank canvas: the linear alpha is the
+    coverage itself, compared as floats."""
+    rng = np.random.default_rng(seed)
+    w, h = 192, 160
+    t = T.TraceWriter(w, h)
+    t.set_color(T.FILL_STYLE, 1.0, 1.0, 1.0, 1.0)
+    t.begin_path()
+    n = int(rng.integers(3, 24))
+    pts = rng.uniform((-30, -30), (w + 30, h + 30), size=(n, 2))
+    t.move_to(*pts[0])
+    for i in range(1, n):
+        if i % 3 == 0:
+            c = rng.uniform((-30, -30), (w + 30, h + 30), size=(2, 2))
+            t.bezier_curve_to(c[0, 0], c[0, 1], c[1, 0], c[1, 1], *pts[i])
+        else:
+            t.line_to(*pts[i])
+    t.close_path()
+    t.fill()
+    tb = t.finish()
+    got = native.replay_linear(tb, w, h)[..., 3]
+    want = oracle.replay_linear(tb, w, h)[..., 3]
+    assert np.abs(got - want).max() <= COVERAGE_TOL
+
+
+def test_empty_and_degenerate_inputs(engine):
+    t = T.TraceWriter(33, 17)
+    t.fill()                                   # empty path
+    t.begin_path(); t.move_to(5, 5); t.fill()  # single point
+    t.set_global_composite_operation(T.SOURCE_COPY)
+    t.fill_rectangle(2, 2, 0, 5)               # zero width: ignored
+    t.set_global_composite_operation(T.SOURCE_OVER)
+    t.set_color(T.FILL_STYLE, 1, 0, 0, 1)
+    t.fill_rectangle(-10, -10, 20, 20)         # partly off canvas
+    t.scale(0, 1)
+    t.fill_rectangle(0, 0, 10, 10)             # singular transform: nothing drawn
+    t.set_transform(1, 0, 0, 1, 0, 0)
+    t.get_image_data(50, 40, -8, -8)           # read outside the canvas
+    t.put_image_data(None, 4, 4, 0, 0)         # null image: ignored
+    tb = t.finish()
+    got = G.split_images(tb, native.replay(tb)[0])
+    want = G.split_images(tb, oracle.replay(tb)[0])
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+def test_one_by_one_and_large_canvas(engine):
+    for w, h in ((1, 1), (4096, 3)):
+        t = T.TraceWriter(w, h)
+        t.set_color(T.FILL_STYLE, 0.2, 0.6, 0.9, 0.7)
+        t.begin_path()
+        t.move_to(0.3, 0.1)
+        t.line_to(w - 0.2, h * 0.8)
+        t.line_to(0.1, h - 0.1)
+        t.fill()
+        tb = t.finish()
+        got = G.split_images(tb, native.replay(tb)[0])[-1]
+        want = G.split_images(tb, oracle.replay(tb)[0])[-1]
+        assert_images_close(got, want, f"{w}x{h}")
