@@ -780,6 +780,8 @@ int canvas::gpu_status() const {
     return self->ctx ? cy_ctx_status(self->ctx) : CY_ENODEV;
 }
 
+void *canvas::gpu_context() const { return self->ctx; }
+
 int canvas::read_linear(float *rgba) {
     if (!self->ctx) return CY_ENODEV;
     return cy_read_linear(self->ctx, rgba);

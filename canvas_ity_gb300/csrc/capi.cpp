@@ -7,12 +7,13 @@
 #include "../../include/canvas_ity.hpp"
 #include "../../include/canvas_ity_c.h"
 #include "../../include/cy_replay.hpp"
+#include "../../include/cy_batch.h"
 
 using canvas_ity::canvas;
 
 struct cy_canvas {
-    canvas impl;
-    cy_canvas(int w, int h) : impl(w, h) {}
+    std::unique_ptr<canvas> owned;
+    canvas &get() { return *owned; }
 };
 
 namespace {
@@ -34,95 +35,99 @@ extern "C" {
 
 cy_canvas *cy_canvas_new(int w, int h) {
     if (w < 1 || h < 1 || w > 32768 || h > 32768) return nullptr;
-    return new (std::nothrow) cy_canvas(w, h);
+    cy_canvas *c = new (std::nothrow) cy_canvas();
+    if (!c) return nullptr;
+    c->owned.reset(new (std::nothrow) canvas(w, h));
+    if (!c->owned) { delete c; return nullptr; }
+    return c;
 }
 void cy_canvas_delete(cy_canvas *c) { delete c; }
-int cy_canvas_status(const cy_canvas *c) { return c ? c->impl.gpu_status() : -1; }
-void cy_canvas_scale(cy_canvas *c, float x, float y) { c->impl.scale(x, y); }
-void cy_canvas_rotate(cy_canvas *c, float a) { c->impl.rotate(a); }
-void cy_canvas_translate(cy_canvas *c, float x, float y) { c->impl.translate(x, y); }
+int cy_canvas_status(const cy_canvas *c) { return c ? const_cast<cy_canvas *>(c)->get().gpu_status() : -1; }
+void cy_canvas_scale(cy_canvas *c, float x, float y) { c->get().scale(x, y); }
+void cy_canvas_rotate(cy_canvas *c, float a) { c->get().rotate(a); }
+void cy_canvas_translate(cy_canvas *c, float x, float y) { c->get().translate(x, y); }
 void cy_canvas_transform(cy_canvas *c, float a, float b, float cc, float d, float e, float f) {
-    c->impl.transform(a, b, cc, d, e, f);
+    c->get().transform(a, b, cc, d, e, f);
 }
 void cy_canvas_set_transform(cy_canvas *c, float a, float b, float cc, float d, float e, float f) {
-    c->impl.set_transform(a, b, cc, d, e, f);
+    c->get().set_transform(a, b, cc, d, e, f);
 }
-void cy_canvas_set_global_alpha(cy_canvas *c, float a) { c->impl.set_global_alpha(a); }
+void cy_canvas_set_global_alpha(cy_canvas *c, float a) { c->get().set_global_alpha(a); }
 void cy_canvas_set_global_composite_operation(cy_canvas *c, int op) {
-    c->impl.global_composite_operation = static_cast<canvas_ity::composite_operation>(op);
+    c->get().global_composite_operation = static_cast<canvas_ity::composite_operation>(op);
 }
 void cy_canvas_set_shadow_color(cy_canvas *c, float r, float g, float b, float a) {
-    c->impl.set_shadow_color(r, g, b, a);
+    c->get().set_shadow_color(r, g, b, a);
 }
-void cy_canvas_set_shadow_offset_x(cy_canvas *c, float v) { c->impl.shadow_offset_x = v; }
-void cy_canvas_set_shadow_offset_y(cy_canvas *c, float v) { c->impl.shadow_offset_y = v; }
-void cy_canvas_set_shadow_blur(cy_canvas *c, float v) { c->impl.set_shadow_blur(v); }
-void cy_canvas_set_line_width(cy_canvas *c, float v) { c->impl.set_line_width(v); }
-void cy_canvas_set_line_cap(cy_canvas *c, int v) { c->impl.line_cap = static_cast<canvas_ity::cap_style>(v); }
-void cy_canvas_set_line_join(cy_canvas *c, int v) { c->impl.line_join = static_cast<canvas_ity::join_style>(v); }
-void cy_canvas_set_miter_limit(cy_canvas *c, float v) { c->impl.set_miter_limit(v); }
-void cy_canvas_set_line_dash_offset(cy_canvas *c, float v) { c->impl.line_dash_offset = v; }
-void cy_canvas_set_line_dash(cy_canvas *c, const float *s, int n) { c->impl.set_line_dash(s, n); }
+void cy_canvas_set_shadow_offset_x(cy_canvas *c, float v) { c->get().shadow_offset_x = v; }
+void cy_canvas_set_shadow_offset_y(cy_canvas *c, float v) { c->get().shadow_offset_y = v; }
+void cy_canvas_set_shadow_blur(cy_canvas *c, float v) { c->get().set_shadow_blur(v); }
+void cy_canvas_set_line_width(cy_canvas *c, float v) { c->get().set_line_width(v); }
+void cy_canvas_set_line_cap(cy_canvas *c, int v) { c->get().line_cap = static_cast<canvas_ity::cap_style>(v); }
+void cy_canvas_set_line_join(cy_canvas *c, int v) { c->get().line_join = static_cast<canvas_ity::join_style>(v); }
+void cy_canvas_set_miter_limit(cy_canvas *c, float v) { c->get().set_miter_limit(v); }
+void cy_canvas_set_line_dash_offset(cy_canvas *c, float v) { c->get().line_dash_offset = v; }
+void cy_canvas_set_line_dash(cy_canvas *c, const float *s, int n) { c->get().set_line_dash(s, n); }
 void cy_canvas_set_color(cy_canvas *c, int t, float r, float g, float b, float a) {
-    c->impl.set_color(bt(t), r, g, b, a);
+    c->get().set_color(bt(t), r, g, b, a);
 }
 void cy_canvas_set_linear_gradient(cy_canvas *c, int t, float x0, float y0, float x1, float y1) {
-    c->impl.set_linear_gradient(bt(t), x0, y0, x1, y1);
+    c->get().set_linear_gradient(bt(t), x0, y0, x1, y1);
 }
 void cy_canvas_set_radial_gradient(cy_canvas *c, int t, float x0, float y0, float r0, float x1, float y1,
                                    float r1) {
-    c->impl.set_radial_gradient(bt(t), x0, y0, r0, x1, y1, r1);
+    c->get().set_radial_gradient(bt(t), x0, y0, r0, x1, y1, r1);
 }
 void cy_canvas_add_color_stop(cy_canvas *c, int t, float o, float r, float g, float b, float a) {
-    c->impl.add_color_stop(bt(t), o, r, g, b, a);
+    c->get().add_color_stop(bt(t), o, r, g, b, a);
 }
 void cy_canvas_set_pattern(cy_canvas *c, int t, const unsigned char *img, int w, int h, int stride, int rep) {
-    c->impl.set_pattern(bt(t), img, w, h, stride, static_cast<canvas_ity::repetition_style>(rep));
+    c->get().set_pattern(bt(t), img, w, h, stride, static_cast<canvas_ity::repetition_style>(rep));
 }
-void cy_canvas_begin_path(cy_canvas *c) { c->impl.begin_path(); }
-void cy_canvas_move_to(cy_canvas *c, float x, float y) { c->impl.move_to(x, y); }
-void cy_canvas_close_path(cy_canvas *c) { c->impl.close_path(); }
-void cy_canvas_line_to(cy_canvas *c, float x, float y) { c->impl.line_to(x, y); }
+void cy_canvas_begin_path(cy_canvas *c) { c->get().begin_path(); }
+void cy_canvas_move_to(cy_canvas *c, float x, float y) { c->get().move_to(x, y); }
+void cy_canvas_close_path(cy_canvas *c) { c->get().close_path(); }
+void cy_canvas_line_to(cy_canvas *c, float x, float y) { c->get().line_to(x, y); }
 void cy_canvas_quadratic_curve_to(cy_canvas *c, float cx, float cy, float x, float y) {
-    c->impl.quadratic_curve_to(cx, cy, x, y);
+    c->get().quadratic_curve_to(cx, cy, x, y);
 }
 void cy_canvas_bezier_curve_to(cy_canvas *c, float a, float b, float cc, float d, float x, float y) {
-    c->impl.bezier_curve_to(a, b, cc, d, x, y);
+    c->get().bezier_curve_to(a, b, cc, d, x, y);
 }
-void cy_canvas_arc_to(cy_canvas *c, float vx, float vy, float x, float y, float r) { c->impl.arc_to(vx, vy, x, y, r); }
+void cy_canvas_arc_to(cy_canvas *c, float vx, float vy, float x, float y, float r) { c->get().arc_to(vx, vy, x, y, r); }
 void cy_canvas_arc(cy_canvas *c, float x, float y, float r, float a0, float a1, int ccw) {
-    c->impl.arc(x, y, r, a0, a1, ccw != 0);
+    c->get().arc(x, y, r, a0, a1, ccw != 0);
 }
-void cy_canvas_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->impl.rectangle(x, y, w, h); }
-void cy_canvas_fill(cy_canvas *c) { c->impl.fill(); }
-void cy_canvas_stroke(cy_canvas *c) { c->impl.stroke(); }
-void cy_canvas_clip(cy_canvas *c) { c->impl.clip(); }
-int cy_canvas_is_point_in_path(cy_canvas *c, float x, float y) { return c->impl.is_point_in_path(x, y) ? 1 : 0; }
-void cy_canvas_clear_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->impl.clear_rectangle(x, y, w, h); }
-void cy_canvas_fill_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->impl.fill_rectangle(x, y, w, h); }
+void cy_canvas_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->get().rectangle(x, y, w, h); }
+void cy_canvas_fill(cy_canvas *c) { c->get().fill(); }
+void cy_canvas_stroke(cy_canvas *c) { c->get().stroke(); }
+void cy_canvas_clip(cy_canvas *c) { c->get().clip(); }
+int cy_canvas_is_point_in_path(cy_canvas *c, float x, float y) { return c->get().is_point_in_path(x, y) ? 1 : 0; }
+void cy_canvas_clear_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->get().clear_rectangle(x, y, w, h); }
+void cy_canvas_fill_rectangle(cy_canvas *c, float x, float y, float w, float h) { c->get().fill_rectangle(x, y, w, h); }
 void cy_canvas_stroke_rectangle(cy_canvas *c, float x, float y, float w, float h) {
-    c->impl.stroke_rectangle(x, y, w, h);
+    c->get().stroke_rectangle(x, y, w, h);
 }
-void cy_canvas_set_text_align(cy_canvas *c, int v) { c->impl.text_align = static_cast<canvas_ity::align_style>(v); }
+void cy_canvas_set_text_align(cy_canvas *c, int v) { c->get().text_align = static_cast<canvas_ity::align_style>(v); }
 void cy_canvas_set_text_baseline(cy_canvas *c, int v) {
-    c->impl.text_baseline = static_cast<canvas_ity::baseline_style>(v);
+    c->get().text_baseline = static_cast<canvas_ity::baseline_style>(v);
 }
-int cy_canvas_set_font(cy_canvas *c, const unsigned char *f, int n, float s) { return c->impl.set_font(f, n, s) ? 1 : 0; }
-void cy_canvas_fill_text(cy_canvas *c, const char *t, float x, float y, float m) { c->impl.fill_text(t, x, y, m); }
-void cy_canvas_stroke_text(cy_canvas *c, const char *t, float x, float y, float m) { c->impl.stroke_text(t, x, y, m); }
-float cy_canvas_measure_text(cy_canvas *c, const char *t) { return c->impl.measure_text(t); }
+int cy_canvas_set_font(cy_canvas *c, const unsigned char *f, int n, float s) { return c->get().set_font(f, n, s) ? 1 : 0; }
+void cy_canvas_fill_text(cy_canvas *c, const char *t, float x, float y, float m) { c->get().fill_text(t, x, y, m); }
+void cy_canvas_stroke_text(cy_canvas *c, const char *t, float x, float y, float m) { c->get().stroke_text(t, x, y, m); }
+float cy_canvas_measure_text(cy_canvas *c, const char *t) { return c->get().measure_text(t); }
 void cy_canvas_draw_image(cy_canvas *c, const unsigned char *img, int w, int h, int stride, float x, float y,
                           float tw, float th) {
-    c->impl.draw_image(img, w, h, stride, x, y, tw, th);
+    c->get().draw_image(img, w, h, stride, x, y, tw, th);
 }
 void cy_canvas_get_image_data(cy_canvas *c, unsigned char *img, int w, int h, int stride, int x, int y) {
-    c->impl.get_image_data(img, w, h, stride, x, y);
+    c->get().get_image_data(img, w, h, stride, x, y);
 }
 void cy_canvas_put_image_data(cy_canvas *c, const unsigned char *img, int w, int h, int stride, int x, int y) {
-    c->impl.put_image_data(img, w, h, stride, x, y);
+    c->get().put_image_data(img, w, h, stride, x, y);
 }
-void cy_canvas_save(cy_canvas *c) { c->impl.save(); }
-void cy_canvas_restore(cy_canvas *c) { c->impl.restore(); }
+void cy_canvas_save(cy_canvas *c) { c->get().save(); }
+void cy_canvas_restore(cy_canvas *c) { c->get().restore(); }
 
 int cy_take_thread_status(void);
 
@@ -155,5 +160,24 @@ int cy_replay_linear(const void *trace, size_t trace_len, float *out, size_t out
     int gpu = cy_take_thread_status();
     return gpu ? gpu : rc;
 }
+
+cy_canvas *cy_canvas_from_trace(const void *trace, size_t trace_len, int *status) {
+    // Replay with reads deferred: drawing is recorded, nothing runs yet.
+    cy_take_thread_status();
+    cy_set_deferred(1);
+    cy_trace::output sink;
+    std::unique_ptr<canvas> keep;
+    int rc = cy_trace::replay<traits>(static_cast<const uint8_t *>(trace), trace_len, sink, &keep);
+    cy_set_deferred(0);
+    int gpu = cy_take_thread_status();
+    if (status) *status = gpu ? gpu : rc;
+    if (rc != 0 || gpu != 0 || !keep) return nullptr;
+    cy_canvas *c = new (std::nothrow) cy_canvas();
+    if (!c) return nullptr;
+    c->owned.reset(keep.release());
+    return c;
+}
+
+void *cy_canvas_ctx(cy_canvas *c) { return c ? c->get().gpu_context() : nullptr; }
 
 }  // extern "C"

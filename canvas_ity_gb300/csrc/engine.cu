@@ -1,11 +1,20 @@
-// engine.cu -- the GB300 render engine behind include/cy_gpu.h.
+// engine.cu -- the GB300 render engine behind include/cy_gpu.h and
+// include/cy_batch.h.
 //
-// A context owns one canvas on the GPU: the premultiplied linear float RGBA
-// bitmap (hpp:1171), a zeroed fixed-point delta plane for scan conversion,
-// and the clip masks.  Calls queue commands on the host; a flush uploads all
-// queued geometry and paint in one copy, flattens every Bezier path in one
-// launch pair, then runs each command's kernels in call order on the
-// context's stream.
+// A context owns one canvas: the premultiplied linear float RGBA bitmap
+// (the reference's `bitmap`, hpp:1171) and its clip masks.  Calls queue
+// commands on the host.  A frame executes the queued commands of one or many
+// contexts:
+//   prepare  pack every queued geometry/paint buffer into one arena and copy
+//            it up, flatten all Bezier paths, size every buffer (two small
+//            read-backs of counts), then run once;
+//   run      device work only, in stream order: flattening, batched scan
+//            conversion of every draw / shadow / clip, clip masks level by
+//            level, shadow images, then either the strip kernel (tile engine)
+//            or per-draw paint launches (plain engine);
+//   finish   copy get_image_data results out, release resources.
+// After the first run, `run` issues no host synchronisation, so a prepared
+// frame can be re-run (the benchmark times exactly that).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -13,26 +22,35 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <vector>
 
 #include "../../include/cy_gpu.h"
 #include "engine_types.h"
 #include "kernels.cuh"
+#include "strips.cuh"
 
 using namespace cyg;
 
 namespace {
 
-thread_local int g_engine = 1;
-thread_local int g_thread_status = 0;  // first failure in this thread since the last take
+thread_local int g_engine = 0;          // 0 tile (strip) engine, 1 plain per-draw engine
+thread_local int g_deferred = 0;        // contexts created now queue their reads
+thread_local int g_thread_status = 0;   // first failure in this thread since the last take
+int g_strip_pixels = 4096;              // strip size of the tile engine (autotuned)
+int g_strip_threads = 256;
+
+void note_thread_status(int rc) {
+    if (rc && g_thread_status == 0) g_thread_status = rc;
+}
 
 struct dbuf {
     void *p = nullptr;
     size_t cap = 0;
     // Grow to at least `bytes`; contents are not preserved.
     bool ensure(size_t bytes) {
-        if (bytes <= cap) return true;
+        if (bytes <= cap && p) return true;
         size_t n = std::max(std::max(bytes, static_cast<size_t>(256)), cap + cap / 2);
         if (p) cudaFree(p);
         p = nullptr;
@@ -49,7 +67,7 @@ struct hbuf {
     void *p = nullptr;
     size_t cap = 0;
     bool ensure(size_t bytes) {
-        if (bytes <= cap) return true;
+        if (bytes <= cap && p) return true;
         size_t n = std::max(std::max(bytes, static_cast<size_t>(4096)), cap + cap / 2);
         if (p) cudaFreeHost(p);
         p = nullptr;
@@ -61,16 +79,17 @@ struct hbuf {
     void release() { if (p) cudaFreeHost(p); p = nullptr; cap = 0; }
 };
 
-// A clip mask: the reference's sparse runs per row plus the dense
-// visibility they imply.  Created by a queued clip, filled at the flush.
+// A clip mask: the reference's sparse runs per row plus the dense visibility
+// they imply.  Created by a queued clip; its content is made when the frame
+// that holds the clip runs.
 struct mask_slot {
     float *vis = nullptr;       // W*H
     int32_t *off = nullptr;     // H+1
-    int32_t *len = nullptr;     // H
-    run *runs = nullptr;
+    int32_t *len = nullptr;     // H+1
+    cyg::run *runs = nullptr;
     float *sums = nullptr;
     int *last_row = nullptr;    // device int: last row holding runs
-    int64_t cap = 0;            // run capacity
+    int64_t cap = 0;            // run capacity (0 until sized)
     int refs = 0;
     void free_all() {
         cudaFree(vis); cudaFree(off); cudaFree(len); cudaFree(runs); cudaFree(sums); cudaFree(last_row);
@@ -94,18 +113,10 @@ const float *linear_lut_host() {
 
 inline size_t align256(size_t v) { return (v + 255) & ~static_cast<size_t>(255); }
 
-}  // namespace
-
-struct cy_ctx {
-    int W = 0, H = 0;
-    int status = 0;
-    cudaStream_t stream = nullptr;
-    float4 *bitmap = nullptr;
-    float *lut = nullptr;
-    std::vector<mask_slot> masks;   // id 0 unused (whole canvas)
-    std::vector<mask_slot> dead;    // released masks, freed after the next flush
-    // queued work
+// Host-side queue of one context.
+struct queue {
     std::vector<command> cmds;
+    std::vector<int32_t> mask_ids;  // per command: mask_in id, mask_out id
     std::vector<float2> host_pts;
     std::vector<int32_t> host_prev;
     std::vector<float2> bez_pts;
@@ -114,18 +125,111 @@ struct cy_ctx {
     std::vector<float4> stop_col;
     std::vector<uchar4> texels;
     std::vector<uint8_t> put_px;
-    std::vector<int32_t> mask_ids;  // per command: mask_in id, mask_out id
-    size_t queued_bytes = 0;
-    int64_t queued_rows = 0;   // scan-conversion rows the queued commands need
-    // per-flush device scratch
-    dbuf arena, flat_pts, flat_prev, item_cnt, item_off, boxes, pat_f4;
-    dbuf jobs_dev, row_cnt, row_off, row_cur, row_len, runs, sums;
-    dbuf sh_a, sh_b, sh_rect, get_dev;
-    hbuf staging, get_host, offs_host, rowoff_host;
+    std::vector<unsigned char *> get_dst;   // per read: host destination (null: deferred)
+    std::vector<int32_t> get_stride;
+    size_t bytes = 0;
+    int64_t rows = 0;
+    int64_t get_bytes = 0;
+    bool empty() const { return cmds.empty(); }
+    void clear() {
+        cmds.clear(); mask_ids.clear(); host_pts.clear(); host_prev.clear(); bez_pts.clear(); items.clear();
+        stop_off.clear(); stop_col.clear(); texels.clear(); put_px.clear(); get_dst.clear(); get_stride.clear();
+        bytes = 0; rows = 0; get_bytes = 0;
+    }
+};
 
+}  // namespace
+
+struct cy_ctx {
+    int W = 0, H = 0;
+    int status = 0;
+    int engine = 0;
+    bool deferred = false;
+    bool has_content = false;   // bitmap holds more than transparent black
+    cudaStream_t stream = nullptr;
+    float4 *bitmap = nullptr;
+    std::vector<mask_slot> masks;   // id 0 unused (whole canvas)
+    std::vector<mask_slot> dead;    // released masks, freed at the next frame
+    queue q;
+    std::vector<uint8_t> deferred_out;   // results of deferred reads
+    void *cached_frame = nullptr;        // frame reused by this context's flushes
     int fail(int rc) {
         if (status == 0) status = rc;
-        if (g_thread_status == 0) g_thread_status = rc;
+        note_thread_status(rc);
+        return rc;
+    }
+};
+
+// ------------------------------------------------------------------ frame
+struct frame {
+    cudaStream_t stream = nullptr;
+    int engine = 0;
+    int status = 0;
+    std::vector<cy_ctx *> cvs;
+    // combined host data
+    queue all;
+    std::vector<int32_t> cmd_cv;
+    int64_t get_total = 0;
+    std::vector<scan_job> jobs;
+    std::vector<int32_t> main_job, shadow_job;
+    std::vector<cyg::shadow_job> sjobs;
+    int64_t shadow_floats = 0;
+    std::vector<strip_cmd> ext;
+    std::vector<strip_canvas> scv;
+    std::vector<int2> items_host;
+    struct clip_op { int cmd; int cv; int in_id, out_id; int level; };
+    std::vector<clip_op> clips;
+    int max_level = -1;
+    int64_t total_rows = 0, total_segs = 0;
+    int n_items = 0;
+    int strip_pixels = 4096;
+    // device
+    dbuf arena, flat_pts, flat_prev, item_cnt, item_off, pat_f4, jobs_dev, boxes;
+    dbuf row_cnt, row_off, row_cur, row_len, runs, sums;
+    dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
+    hbuf staging, offs_host, rowoff_host, get_host;
+    char *d = nullptr;
+    size_t o_cmd = 0, o_hpts = 0, o_hprev = 0, o_bez = 0, o_items = 0, o_soff = 0, o_scol = 0, o_tex = 0, o_put = 0;
+    bool sized = false;        // run store and masks sized by the first run
+    bool ext_built = false;
+    bool strips_built = false;
+
+    // Forget the previous frame's commands but keep its device buffers.
+    void reset() {
+        status = 0;
+        cvs.clear();
+        all.clear();
+        cmd_cv.clear();
+        get_total = 0;
+        jobs.clear();
+        main_job.clear();
+        shadow_job.clear();
+        sjobs.clear();
+        shadow_floats = 0;
+        ext.clear();
+        scv.clear();
+        items_host.clear();
+        clips.clear();
+        max_level = -1;
+        total_rows = total_segs = 0;
+        n_items = 0;
+        sized = ext_built = strips_built = false;
+    }
+
+    ~frame() {
+        dbuf *b[] = {&arena, &flat_pts, &flat_prev, &item_cnt, &item_off, &pat_f4, &jobs_dev, &boxes, &row_cnt,
+                     &row_off, &row_cur, &row_len, &runs, &sums, &sj_dev, &sh_img, &sh_scratch, &rects,
+                     &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev};
+        for (dbuf *x : b) x->release();
+        staging.release();
+        offs_host.release();
+        rowoff_host.release();
+        get_host.release();
+    }
+    int fail(int rc) {
+        if (status == 0) status = rc;
+        for (cy_ctx *c : cvs) c->fail(rc);
+        note_thread_status(rc);
         return rc;
     }
     bool ok(cudaError_t e) {
@@ -134,11 +238,568 @@ struct cy_ctx {
         fail(e == cudaErrorMemoryAllocation ? CY_ENOMEM : CY_ECUDA);
         return false;
     }
-    int flush();
     int scan(const int32_t *in, int32_t *out, int n);
-    int clip_mask(const command &c, int mask_in, int mask_out, const scan_job &job, int job_index,
-                  const int32_t *rowoff_h);
+    void gather();
+    int prepare();
+    int run();
+    int finish();
 };
+
+int frame::scan(const int32_t *in, int32_t *out, int n) {
+    // Exclusive scan with recursion over tile sums.
+    int tiles = (n + 4095) / 4096;
+    if (tiles <= 0) return CY_OK;
+    if (tiles == 1) {
+        k_scan_tiles<<<1, 1024, 0, stream>>>(in, out, n, nullptr);
+        return ok(cudaGetLastError()) ? CY_OK : status;
+    }
+    int32_t *sums_p = nullptr, *offs_p = nullptr;
+    if (!ok(cudaMallocAsync(reinterpret_cast<void **>(&sums_p), static_cast<size_t>(tiles) * 4, stream)) ||
+        !ok(cudaMallocAsync(reinterpret_cast<void **>(&offs_p), static_cast<size_t>(tiles) * 4, stream)))
+        return status;
+    k_scan_tiles<<<tiles, 1024, 0, stream>>>(in, out, n, sums_p);
+    int rc = scan(sums_p, offs_p, tiles);
+    if (rc == CY_OK) k_scan_add<<<(n + 255) / 256, 256, 0, stream>>>(out, n, offs_p);
+    cudaFreeAsync(sums_p, stream);
+    cudaFreeAsync(offs_p, stream);
+    if (rc == CY_OK && !ok(cudaGetLastError())) rc = status;
+    return rc;
+}
+
+// Concatenate the queues of every canvas of the frame, rebasing indices.
+void frame::gather() {
+    for (size_t ci = 0; ci < cvs.size(); ++ci) {
+        queue &q = cvs[ci]->q;
+        int32_t b_hpts = static_cast<int32_t>(all.host_pts.size());
+        int32_t b_bez = static_cast<int32_t>(all.bez_pts.size());
+        int32_t b_items = static_cast<int32_t>(all.items.size());
+        int32_t b_stop = static_cast<int32_t>(all.stop_off.size());
+        int32_t b_tex = static_cast<int32_t>(all.texels.size());
+        int64_t b_put = static_cast<int64_t>(all.put_px.size());
+        all.host_pts.insert(all.host_pts.end(), q.host_pts.begin(), q.host_pts.end());
+        for (int32_t v : q.host_prev) all.host_prev.push_back(v + b_hpts);
+        all.bez_pts.insert(all.bez_pts.end(), q.bez_pts.begin(), q.bez_pts.end());
+        for (flat_item it : q.items) {
+            it.pt += b_bez;
+            if (it.sub_end >= 0) it.sub_end += b_items;
+            all.items.push_back(it);
+        }
+        all.stop_off.insert(all.stop_off.end(), q.stop_off.begin(), q.stop_off.end());
+        all.stop_col.insert(all.stop_col.end(), q.stop_col.begin(), q.stop_col.end());
+        all.texels.insert(all.texels.end(), q.texels.begin(), q.texels.end());
+        all.put_px.insert(all.put_px.end(), q.put_px.begin(), q.put_px.end());
+        for (size_t k = 0; k < q.cmds.size(); ++k) {
+            command c = q.cmds[k];
+            if (c.kind == CMD_FILL || c.kind == CMD_CLIP) {
+                c.first += c.geom == 0 ? b_hpts : b_items;
+                c.stop_first += b_stop;
+                c.pat_first += b_tex;
+            } else if (c.kind == CMD_PUT) {
+                c.put_first += b_put;
+            } else if (c.kind == CMD_GET) {
+                c.get_out += get_total;
+            }
+            all.cmds.push_back(c);
+            cmd_cv.push_back(static_cast<int32_t>(ci));
+            all.mask_ids.push_back(q.mask_ids[2 * k]);
+            all.mask_ids.push_back(q.mask_ids[2 * k + 1]);
+        }
+        all.get_dst.insert(all.get_dst.end(), q.get_dst.begin(), q.get_dst.end());
+        all.get_stride.insert(all.get_stride.end(), q.get_stride.begin(), q.get_stride.end());
+        get_total += q.get_bytes;
+    }
+}
+
+int frame::prepare() {
+    gather();
+    std::vector<command> &cmds = all.cmds;
+    for (cy_ctx *c : cvs) {
+        for (auto &m : c->dead) m.free_all();
+        c->dead.clear();
+    }
+    // Arena: everything queued goes up in one copy.
+    o_cmd = 0;
+    o_hpts = align256(o_cmd + cmds.size() * sizeof(command));
+    o_hprev = align256(o_hpts + all.host_pts.size() * sizeof(float2));
+    o_bez = align256(o_hprev + all.host_prev.size() * sizeof(int32_t));
+    o_items = align256(o_bez + all.bez_pts.size() * sizeof(float2));
+    o_soff = align256(o_items + all.items.size() * sizeof(flat_item));
+    o_scol = align256(o_soff + all.stop_off.size() * sizeof(float));
+    o_tex = align256(o_scol + all.stop_col.size() * sizeof(float4));
+    o_put = align256(o_tex + all.texels.size() * sizeof(uchar4));
+    size_t total = align256(o_put + all.put_px.size());
+    if (!arena.ensure(total) || !staging.ensure(total)) return fail(CY_ENOMEM);
+    char *h = static_cast<char *>(staging.p);
+    auto put = [&](size_t off, const void *src, size_t n) { if (n) std::memcpy(h + off, src, n); };
+    put(o_hpts, all.host_pts.data(), all.host_pts.size() * sizeof(float2));
+    put(o_hprev, all.host_prev.data(), all.host_prev.size() * sizeof(int32_t));
+    put(o_bez, all.bez_pts.data(), all.bez_pts.size() * sizeof(float2));
+    put(o_items, all.items.data(), all.items.size() * sizeof(flat_item));
+    put(o_soff, all.stop_off.data(), all.stop_off.size() * sizeof(float));
+    put(o_scol, all.stop_col.data(), all.stop_col.size() * sizeof(float4));
+    put(o_tex, all.texels.data(), all.texels.size() * sizeof(uchar4));
+    put(o_put, all.put_px.data(), all.put_px.size());
+    d = static_cast<char *>(arena.p);
+    if (total > o_hpts && !ok(cudaMemcpyAsync(d + o_hpts, h + o_hpts, total - o_hpts, cudaMemcpyHostToDevice, stream)))
+        return status;
+    if (!lut_dev.ensure(256 * sizeof(float))) return fail(CY_ENOMEM);
+    if (!ok(cudaMemcpyAsync(lut_dev.p, linear_lut_host(), 256 * sizeof(float), cudaMemcpyHostToDevice, stream)))
+        return status;
+    // Flattening counts size the polyline store (one read-back).
+    int n_items = static_cast<int>(all.items.size());
+    const int32_t *offs_h = nullptr;
+    if (n_items > 0) {
+        if (!item_cnt.ensure(static_cast<size_t>(n_items + 1) * 4) ||
+            !item_off.ensure(static_cast<size_t>(n_items + 1) * 4) ||
+            !offs_host.ensure(static_cast<size_t>(n_items + 1) * 4))
+            return fail(CY_ENOMEM);
+        const float2 *d_bez = reinterpret_cast<const float2 *>(d + o_bez);
+        const flat_item *d_items = reinterpret_cast<const flat_item *>(d + o_items);
+        k_flat_count<<<(n_items + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items, item_cnt.as<int32_t>());
+        if (!ok(cudaMemsetAsync(item_cnt.as<int32_t>() + n_items, 0, 4, stream))) return status;
+        int rc = scan(item_cnt.as<int32_t>(), item_off.as<int32_t>(), n_items + 1);
+        if (rc) return rc;
+        if (!ok(cudaMemcpyAsync(offs_host.p, item_off.p, static_cast<size_t>(n_items + 1) * 4,
+                                cudaMemcpyDeviceToHost, stream)) ||
+            !ok(cudaStreamSynchronize(stream)))
+            return status;
+        offs_h = static_cast<const int32_t *>(offs_host.p);
+        int64_t nflat = offs_h[n_items];
+        if (nflat < 0 || nflat > (static_cast<int64_t>(1) << 30)) return fail(CY_ENOMEM);
+        if (!flat_pts.ensure(static_cast<size_t>(nflat + 1) * sizeof(float2)) ||
+            !flat_prev.ensure(static_cast<size_t>(nflat + 1) * 4))
+            return fail(CY_ENOMEM);
+    }
+    for (command &c : cmds) {
+        if (c.kind != CMD_FILL && c.kind != CMD_CLIP) continue;
+        if (c.geom == 0) {
+            c.line_first = c.first;
+            c.line_count = c.count;
+        } else if (c.count == 0 || !offs_h) {
+            c.line_first = 0;
+            c.line_count = 0;
+        } else {
+            c.line_first = offs_h[c.first];
+            c.line_count = offs_h[c.first + c.count] - c.line_first;
+        }
+    }
+    if (!cmds.empty()) {
+        std::memcpy(h + o_cmd, cmds.data(), cmds.size() * sizeof(command));
+        if (!ok(cudaMemcpyAsync(d + o_cmd, h + o_cmd, cmds.size() * sizeof(command), cudaMemcpyHostToDevice,
+                                stream)))
+            return status;
+    }
+    // Scan-conversion jobs: shadow pass (padded canvas) and main pass of each
+    // draw, and the path of each clip.
+    auto add_job = [&](const command &c, int rows_n, int cols_n, float wd, float ht, float ox, float oy) {
+        scan_job j;
+        std::memset(&j, 0, sizeof(j));
+        j.geom = c.geom;
+        j.line_first = c.line_first;
+        j.seg_first = static_cast<int32_t>(total_segs);
+        j.seg_count = c.line_count;
+        j.row_base = static_cast<int32_t>(total_rows);
+        j.rows = rows_n;
+        j.cols = cols_n;
+        j.width = wd;
+        j.height = ht;
+        j.offx = ox;
+        j.offy = oy;
+        total_rows += rows_n;
+        total_segs += c.line_count;
+        jobs.push_back(j);
+        return static_cast<int>(jobs.size()) - 1;
+    };
+    main_job.assign(cmds.size(), -1);
+    shadow_job.assign(cmds.size(), -1);
+    std::vector<int> level_of_cv(cvs.size(), 0);
+    for (size_t i = 0; i < cmds.size(); ++i) {
+        const command &c = cmds[i];
+        const cy_ctx *cv = cvs[cmd_cv[i]];
+        int W = cv->W, H = cv->H;
+        if (c.kind == CMD_FILL && c.shadow) {
+            int b = c.sh_border;
+            int ew = W + 2 * b, eh = H + 2 * b;
+            shadow_job[i] = add_job(c, eh, ew + 2, static_cast<float>(ew), static_cast<float>(eh), c.sh_offx,
+                                    c.sh_offy);
+            cyg::shadow_job s;
+            std::memset(&s, 0, sizeof(s));
+            s.cmd = static_cast<int32_t>(i);
+            s.job = shadow_job[i];
+            s.row_base = jobs[shadow_job[i]].row_base;
+            s.W = W;
+            s.H = H;
+            s.border = b;
+            s.img = shadow_floats;
+            s.radius = c.sh_radius;
+            s.w1 = c.sh_w1;
+            s.w2 = c.sh_w2;
+            shadow_floats += static_cast<int64_t>(ew + 1) * eh;
+            sjobs.push_back(s);
+        }
+        if (c.kind == CMD_FILL || c.kind == CMD_CLIP)
+            main_job[i] = add_job(c, H, W + 2, static_cast<float>(W), static_cast<float>(H), 0.0f, 0.0f);
+        if (c.kind == CMD_CLIP) {
+            int lv = level_of_cv[cmd_cv[i]]++;
+            clips.push_back(clip_op{static_cast<int>(i), cmd_cv[i], all.mask_ids[2 * i], all.mask_ids[2 * i + 1], lv});
+            max_level = std::max(max_level, lv);
+        }
+    }
+    if (total_rows > INT32_MAX / 2 || total_segs > INT32_MAX / 2) return fail(CY_ENOMEM);
+    size_t nr = static_cast<size_t>(total_rows);
+    if (!jobs.empty()) {
+        if (!jobs_dev.ensure(jobs.size() * sizeof(scan_job)) || !row_cnt.ensure((nr + 1) * 4) ||
+            !row_off.ensure((nr + 2) * 4) || !row_cur.ensure((nr + 1) * 4) || !row_len.ensure((nr + 1) * 4) ||
+            !boxes.ensure(jobs.size() * sizeof(cover_box)) || !rowoff_host.ensure((nr + 1) * 4))
+            return fail(CY_ENOMEM);
+        if (!ok(cudaMemcpyAsync(jobs_dev.p, jobs.data(), jobs.size() * sizeof(scan_job), cudaMemcpyHostToDevice,
+                                stream)) ||
+            !ok(cudaMemsetAsync(row_cnt.p, 0, (nr + 1) * 4, stream)) ||
+            !ok(cudaMemsetAsync(row_cur.p, 0, (nr + 1) * 4, stream)))
+            return status;
+    }
+    if (!sjobs.empty()) {
+        if (!sj_dev.ensure(sjobs.size() * sizeof(cyg::shadow_job)) ||
+            !sh_img.ensure(static_cast<size_t>(shadow_floats) * 4) ||
+            !sh_scratch.ensure(static_cast<size_t>(shadow_floats) * 4))
+            return fail(CY_ENOMEM);
+        if (!ok(cudaMemcpyAsync(sj_dev.p, sjobs.data(), sjobs.size() * sizeof(cyg::shadow_job),
+                                cudaMemcpyHostToDevice, stream)))
+            return status;
+    }
+    if (!rects.ensure(std::max<size_t>(cmds.size(), 1) * sizeof(shadow_rect))) return fail(CY_ENOMEM);
+    if (!get_dev.ensure(static_cast<size_t>(std::max<int64_t>(get_total, 16))) ||
+        !get_host.ensure(static_cast<size_t>(std::max<int64_t>(get_total, 16))))
+        return fail(CY_ENOMEM);
+    // The first run also sizes the run store and the clip masks.
+    return run();
+}
+
+int frame::run() {
+    if (status) return status;
+    std::vector<command> &cmds = all.cmds;
+    const float2 *d_hpts = reinterpret_cast<const float2 *>(d + o_hpts);
+    const int32_t *d_hprev = reinterpret_cast<const int32_t *>(d + o_hprev);
+    const float2 *d_bez = reinterpret_cast<const float2 *>(d + o_bez);
+    const flat_item *d_items = reinterpret_cast<const flat_item *>(d + o_items);
+    const command *d_cmds = reinterpret_cast<const command *>(d + o_cmd);
+    const float *lut = lut_dev.as<float>();
+    paint_src src;
+    src.stop_off = reinterpret_cast<const float *>(d + o_soff);
+    src.stop_col = reinterpret_cast<const float4 *>(d + o_scol);
+    src.texels = nullptr;
+    if (!all.texels.empty()) {
+        if (!pat_f4.ensure(all.texels.size() * sizeof(float4))) return fail(CY_ENOMEM);
+        int n = static_cast<int>(all.texels.size());
+        k_pattern_prep<<<(n + 255) / 256, 256, 0, stream>>>(reinterpret_cast<const uchar4 *>(d + o_tex),
+                                                            pat_f4.as<float4>(), n, lut);
+        src.texels = pat_f4.as<float4>();
+    }
+    int n_items_flat = static_cast<int>(all.items.size());
+    if (n_items_flat > 0) {
+        const int32_t *offs_h = static_cast<const int32_t *>(offs_host.p);
+        int64_t nflat = offs_h[n_items_flat];
+        k_flat_emit<<<(n_items_flat + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items_flat,
+                                                                    item_off.as<int32_t>(), flat_pts.as<float2>(),
+                                                                    flat_prev.as<int32_t>(), nflat);
+    }
+    size_t nr = static_cast<size_t>(total_rows);
+    int n_jobs = static_cast<int>(jobs.size());
+    row_view rv;
+    rv.row_off = row_off.as<int32_t>();
+    rv.row_len = row_len.as<int32_t>();
+    rv.runs = runs.as<cyg::run>();
+    rv.sums = sums.as<float>();
+    if (n_jobs > 0) {
+        job_tables t;
+        std::memset(&t, 0, sizeof(t));
+        k_box_init<<<(n_jobs + 255) / 256, 256, 0, stream>>>(boxes.as<cover_box>(), n_jobs);
+        t.jobs = jobs_dev.as<scan_job>();
+        t.n_jobs = n_jobs;
+        t.pts[0] = d_hpts;
+        t.prev[0] = d_hprev;
+        t.pts[1] = flat_pts.p ? flat_pts.as<float2>() : d_hpts;
+        t.prev[1] = flat_prev.p ? flat_prev.as<int32_t>() : d_hprev;
+        t.boxes = boxes.as<cover_box>();
+        t.row_cnt = row_cnt.as<int32_t>();
+        t.row_cur = row_cur.as<int32_t>();
+        int segs = static_cast<int>(total_segs);
+        int grid = std::max(1, std::min((segs + 7) / 8, 152 * 32));
+        if (segs > 0) k_runs<false><<<grid, 256, 0, stream>>>(t, segs);
+        int rc = scan(row_cnt.as<int32_t>(), row_off.as<int32_t>(), static_cast<int>(nr) + 1);
+        if (rc) return rc;
+        if (!sized) {
+            sized = true;
+            // First run: size the run store and the new clip masks from the counts.
+            if (!ok(cudaMemcpyAsync(rowoff_host.p, row_off.p, (nr + 1) * 4, cudaMemcpyDeviceToHost, stream)) ||
+                !ok(cudaStreamSynchronize(stream)))
+                return status;
+            const int32_t *rowoff_h = static_cast<const int32_t *>(rowoff_host.p);
+            int64_t nruns = rowoff_h[nr];
+            if (nruns < 0) return fail(CY_ENOMEM);
+            if (!runs.ensure(static_cast<size_t>(nruns + 1) * sizeof(cyg::run)) ||
+                !sums.ensure(static_cast<size_t>(nruns + 1) * sizeof(float)))
+                return fail(CY_ENOMEM);
+            rv.runs = runs.as<cyg::run>();
+            rv.sums = sums.as<float>();
+            for (const clip_op &op : clips) {
+                cy_ctx *cv = cvs[op.cv];
+                mask_slot &nm = cv->masks[op.out_id];
+                const scan_job &j = jobs[main_job[op.cmd]];
+                int64_t path_runs = rowoff_h[j.row_base + j.rows] - rowoff_h[j.row_base];
+                int64_t old_cap = op.in_id > 0 ? cv->masks[op.in_id].cap : 2 * static_cast<int64_t>(cv->H);
+                nm.cap = std::max<int64_t>(path_runs + old_cap, 1);
+                if (nm.cap > INT32_MAX) return fail(CY_ENOMEM);
+                if (!ok(cudaMalloc(&nm.runs, static_cast<size_t>(nm.cap) * sizeof(cyg::run))) ||
+                    !ok(cudaMalloc(&nm.sums, static_cast<size_t>(nm.cap) * sizeof(float))))
+                    return status;
+            }
+        }
+        t.row_off = row_off.as<int32_t>();
+        t.runs = runs.as<cyg::run>();
+        if (segs > 0) k_runs<true><<<grid, 256, 0, stream>>>(t, segs);
+        k_rows<<<static_cast<int>((nr + 127) / 128), 128, 0, stream>>>(
+            row_off.as<int32_t>(), row_cnt.as<int32_t>(), row_cur.as<int32_t>(), row_len.as<int32_t>(),
+            runs.as<cyg::run>(), sums.as<float>(), static_cast<int>(nr));
+        if (!ok(cudaGetLastError())) return status;
+    }
+    // Clip masks, level by level (a clip depends on the previous mask).
+    for (int lv = 0; lv <= max_level; ++lv) {
+        for (const clip_op &op : clips) {
+            if (op.level != lv) continue;
+            cy_ctx *cv = cvs[op.cv];
+            int W = cv->W, H = cv->H;
+            mask_slot &nm = cv->masks[op.out_id];
+            const mask_slot *om = op.in_id > 0 ? &cv->masks[op.in_id] : nullptr;
+            const scan_job &j = jobs[main_job[op.cmd]];
+            k_clip_caps<<<(H + 255) / 256, 256, 0, stream>>>(row_off.as<int32_t>() + j.row_base,
+                                                              om ? om->off : nullptr, H, nm.len);
+            if (!ok(cudaMemsetAsync(nm.len + H, 0, 4, stream))) return status;
+            int rc = scan(nm.len, nm.off, H + 1);
+            if (rc) return rc;
+            if (!ok(cudaMemsetAsync(nm.last_row, 0xff, 4, stream))) return status;
+            clip_args a;
+            a.p_off = row_off.as<int32_t>();
+            a.p_len = row_len.as<int32_t>();
+            a.p_runs = runs.as<cyg::run>();
+            a.p_base = j.row_base;
+            a.p_box = boxes.as<cover_box>() + main_job[op.cmd];
+            a.o_off = om ? om->off : nullptr;
+            a.o_len = om ? om->len : nullptr;
+            a.o_runs = om ? om->runs : nullptr;
+            a.o_last_row = om ? om->last_row : nullptr;
+            a.n_off = nm.off;
+            a.n_len = nm.len;
+            a.n_runs = nm.runs;
+            a.n_last_row = nm.last_row;
+            a.W = W;
+            a.H = H;
+            k_clip_rows<<<(H + 127) / 128, 128, 0, stream>>>(a);
+            k_mask_prefix<<<(H + 127) / 128, 128, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, H);
+            k_mask_fill<<<std::max(1, (H + 7) / 8), 256, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, W, H,
+                                                                      nm.vis);
+            if (!ok(cudaGetLastError())) return status;
+        }
+    }
+    // Shadow images of every shadowed draw.
+    if (!sjobs.empty()) {
+        int ns = static_cast<int>(sjobs.size());
+        int max_w = 0, max_h = 0;
+        for (const auto &s : sjobs) {
+            max_w = std::max(max_w, s.W + 2 * s.border + 1);
+            max_h = std::max(max_h, s.H + 2 * s.border);
+        }
+        const cyg::shadow_job *dsj = sj_dev.as<cyg::shadow_job>();
+        k_shadow_rects<<<(ns + 127) / 128, 128, 0, stream>>>(dsj, ns, boxes.as<cover_box>(), rects.as<shadow_rect>());
+        dim3 rg(std::max(1, std::min((max_h + 7) / 8, 64)), ns);
+        k_shadow_raster_all<<<rg, 256, 0, stream>>>(dsj, d_cmds, src, rv, rects.as<shadow_rect>(), sh_img.as<float>());
+        dim3 bg((max_h + 127) / 128, ns), cg((max_w + 127) / 128, ns);
+        k_blur_rows_all<<<bg, 128, 0, stream>>>(dsj, rects.as<shadow_rect>(), sh_img.as<float>(),
+                                                 sh_scratch.as<float>());
+        k_blur_cols_all<<<cg, 128, 0, stream>>>(dsj, rects.as<shadow_rect>(), sh_img.as<float>(),
+                                                 sh_scratch.as<float>());
+        if (!ok(cudaGetLastError())) return status;
+    }
+    if (get_total > 0 && !ok(cudaMemsetAsync(get_dev.p, 0, static_cast<size_t>(get_total), stream))) return status;
+    const uint8_t *d_put = reinterpret_cast<const uint8_t *>(d + o_put);
+    // Per-command extras.
+    if (!ext_built) {
+        ext_built = true;
+        ext.assign(cmds.size(), strip_cmd());
+        for (size_t i = 0; i < cmds.size(); ++i) {
+            strip_cmd &e = ext[i];
+            std::memset(&e, 0, sizeof(e));
+            const command &c = cmds[i];
+            cy_ctx *cv = cvs[cmd_cv[i]];
+            e.main_row_base = main_job[i] >= 0 ? jobs[main_job[i]].row_base : 0;
+            e.has_shadow = shadow_job[i] >= 0;
+            e.shadow_img = 0;
+            if (e.has_shadow)
+                for (const auto &s : sjobs)
+                    if (s.cmd == static_cast<int32_t>(i)) e.shadow_img = s.img;
+            int in_id = all.mask_ids[2 * i];
+            e.vis = in_id > 0 ? cv->masks[in_id].vis : nullptr;
+            if (c.kind == CMD_GET) {
+                e.get_out = c.get_out;
+                e.get_x = c.get_x; e.get_y = c.get_y; e.get_w = c.get_w; e.get_h = c.get_h;
+            }
+        }
+    }
+    if (engine == 1) {
+        // Plain engine: per-draw launches over each canvas's float bitmap.
+        for (size_t i = 0; i < cmds.size(); ++i) {
+            const command &c = cmds[i];
+            cy_ctx *cv = cvs[cmd_cv[i]];
+            int W = cv->W, H = cv->H;
+            const strip_cmd &e = ext[i];
+            if (c.kind == CMD_CLIP) continue;
+            if (c.kind == CMD_PUT) {
+                dim3 blk(32, 8), grd((c.put_w + 31) / 32, (c.put_h + 7) / 8);
+                k_put<<<grd, blk, 0, stream>>>(d_cmds + i, d_put, cv->bitmap, W, H, lut);
+                continue;
+            }
+            if (c.kind == CMD_GET) {
+                dim3 blk(32, 8), grd((c.get_w + 31) / 32, (c.get_h + 7) / 8);
+                k_get<<<grd, blk, 0, stream>>>(cv->bitmap, W, H,
+                                               reinterpret_cast<uchar4 *>(get_dev.as<uint8_t>() + c.get_out),
+                                               c.get_w, c.get_h, c.get_x, c.get_y);
+                continue;
+            }
+            if (e.has_shadow) {
+                dim3 blk(32, 8), cgrd((W + 31) / 32, (H + 7) / 8);
+                k_shadow_composite<<<cgrd, blk, 0, stream>>>(d_cmds + i, cv->bitmap, W, H, e.vis,
+                                                             rects.as<shadow_rect>() + i,
+                                                             sh_img.as<float>() + e.shadow_img);
+            }
+            bool clearing = !(c.op & 8);
+            int y0 = clearing ? 0 : std::max(0, std::min(H, c.gy0));
+            int y1 = clearing ? H : std::max(0, std::min(H, c.gy1 + 1));
+            if (y1 > y0) {
+                paint_args pa;
+                pa.cmd = d_cmds + i;
+                pa.bitmap = cv->bitmap;
+                pa.W = W;
+                pa.H = H;
+                pa.rv = rv;
+                pa.row_base = e.main_row_base;
+                pa.vis = e.vis;
+                pa.y_begin = y0;
+                pa.y_end = y1;
+                pa.src = src;
+                k_paint<<<std::max(1, (y1 - y0 + 7) / 8), 256, 0, stream>>>(pa);
+            }
+        }
+        return ok(cudaGetLastError()) ? CY_OK : status;
+    }
+    // Tile engine: one persistent launch over (canvas, strip) work items.
+    size_t smem = static_cast<size_t>(strip_pixels) * sizeof(float4);
+    if (!strips_built) {
+        strips_built = true;
+        strip_pixels = g_strip_pixels;
+        smem = static_cast<size_t>(strip_pixels) * sizeof(float4);
+        scv.resize(cvs.size());
+        std::vector<std::pair<int64_t, int2>> work;
+        int cursor = 0;
+        for (size_t ci = 0; ci < cvs.size(); ++ci) {
+            cy_ctx *cv = cvs[ci];
+            if (cv->W > strip_pixels) return fail(CY_EINVAL);   // a row must fit in one strip
+            strip_canvas &s = scv[ci];
+            s.W = cv->W;
+            s.H = cv->H;
+            s.TH = std::max(1, std::min(cv->H, strip_pixels / std::max(1, cv->W)));
+            s.cmd_first = cursor;
+            s.cmd_count = static_cast<int32_t>(cv->q.cmds.size());
+            cursor += s.cmd_count;
+            s.flags = (cv->has_content ? 1 : 0) | (cv->deferred ? 0 : 2);
+            s.bitmap = cv->bitmap;
+            int64_t cost = static_cast<int64_t>(s.TH) * s.W * (s.cmd_count + 1);
+            for (int y = 0; y < s.H; y += s.TH) work.push_back({cost, make_int2(static_cast<int>(ci), y)});
+        }
+        std::stable_sort(work.begin(), work.end(),
+                         [](const std::pair<int64_t, int2> &a, const std::pair<int64_t, int2> &b) {
+                             return a.first > b.first;
+                         });
+        items_host.resize(work.size());
+        for (size_t k = 0; k < work.size(); ++k) items_host[k] = work[k].second;
+        n_items = static_cast<int>(items_host.size());
+        if (!scv_dev.ensure(scv.size() * sizeof(strip_canvas)) ||
+            !items_dev.ensure(std::max<size_t>(items_host.size(), 1) * sizeof(int2)) ||
+            !ext_dev.ensure(std::max<size_t>(ext.size(), 1) * sizeof(strip_cmd)) || !counter.ensure(4))
+            return fail(CY_ENOMEM);
+        if (!ok(cudaMemcpyAsync(scv_dev.p, scv.data(), scv.size() * sizeof(strip_canvas), cudaMemcpyHostToDevice,
+                                stream)))
+            return status;
+        if (n_items > 0 && !ok(cudaMemcpyAsync(items_dev.p, items_host.data(), items_host.size() * sizeof(int2),
+                                               cudaMemcpyHostToDevice, stream)))
+            return status;
+        if (!ext.empty() && !ok(cudaMemcpyAsync(ext_dev.p, ext.data(), ext.size() * sizeof(strip_cmd),
+                                                cudaMemcpyHostToDevice, stream)))
+            return status;
+        if (!ok(cudaFuncSetAttribute(k_strips, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))))
+            return status;
+    }
+    if (n_items == 0) return CY_OK;
+    if (!ok(cudaMemsetAsync(counter.p, 0, 4, stream))) return status;
+    strip_params P;
+    P.canvases = scv_dev.as<strip_canvas>();
+    P.items = items_dev.as<int2>();
+    P.n_items = n_items;
+    P.counter = counter.as<int>();
+    P.cmds = d_cmds;
+    P.ext = ext_dev.as<strip_cmd>();
+    P.rv = rv;
+    P.src = src;
+    P.rects = rects.as<shadow_rect>();
+    P.shadow_imgs = sh_img.as<float>();
+    P.put_px = d_put;
+    P.lut = lut;
+    P.get_buf = get_dev.as<uint8_t>();
+    P.strip_pixels = strip_pixels;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_strips, g_strip_threads, smem);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    int grid = std::max(1, std::min(n_items, sms * std::max(per_sm, 1)));
+    k_strips<<<grid, g_strip_threads, smem, stream>>>(P);
+    return ok(cudaGetLastError()) ? CY_OK : status;
+}
+
+int frame::finish() {
+    if (status) return status;
+    if (get_total > 0 && !ok(cudaMemcpyAsync(get_host.p, get_dev.p, static_cast<size_t>(get_total),
+                                             cudaMemcpyDeviceToHost, stream)))
+        return status;
+    if (!ok(cudaStreamSynchronize(stream))) return status;
+    // Deliver reads: to the caller's buffer, or keep them for deferred readers.
+    size_t g = 0;
+    for (size_t i = 0; i < all.cmds.size(); ++i) {
+        const command &c = all.cmds[i];
+        if (c.kind != CMD_GET) continue;
+        const uint8_t *src = static_cast<const uint8_t *>(get_host.p) + c.get_out;
+        unsigned char *dst = all.get_dst[g];
+        int stride = all.get_stride[g];
+        ++g;
+        cy_ctx *cv = cvs[cmd_cv[i]];
+        if (dst) {
+            for (int row = 0; row < c.get_h; ++row)
+                std::memcpy(dst + static_cast<ptrdiff_t>(row) * stride, src + static_cast<size_t>(row) * c.get_w * 4,
+                            static_cast<size_t>(c.get_w) * 4);
+        } else {
+            cv->deferred_out.insert(cv->deferred_out.end(), src, src + static_cast<size_t>(c.get_w) * c.get_h * 4);
+        }
+    }
+    for (cy_ctx *cv : cvs) {
+        queue &q = cv->q;
+        for (size_t i = 0; i < q.cmds.size(); ++i) {
+            int in = q.mask_ids[2 * i], out = q.mask_ids[2 * i + 1];
+            if (in > 0) cy_mask_release(cv, in);
+            if (out > 0) cy_mask_release(cv, out);
+            if (q.cmds[i].kind == CMD_FILL || q.cmds[i].kind == CMD_PUT) cv->has_content = true;
+        }
+        q.clear();
+    }
+    return CY_OK;
+}
 
 // ------------------------------------------------------------ host helpers
 namespace {
@@ -166,7 +827,7 @@ void bounds_of(const float *xy, size_t n, command &c) {
     c.gy1 = bad ? 1000000000 : clampi(y1) + 1;
 }
 
-int fill_paint(cy_ctx *ctx, const cy_paint *p, command &c) {
+int fill_paint(queue &q, const cy_paint *p, command &c) {
     c.paint = p->kind;
     c.clamp = p->clamp_edges;
     for (int i = 0; i < 6; ++i) c.inv[i] = p->inverse[i];
@@ -178,25 +839,25 @@ int fill_paint(cy_ctx *ctx, const cy_paint *p, command &c) {
     if (p->kind == CY_PAINT_LINEAR || p->kind == CY_PAINT_RADIAL) {
         if (p->n_stops <= 0) { c.paint = CY_PAINT_NONE; return CY_OK; }
         if (!p->stop_offsets || !p->stop_colors) return CY_EINVAL;
-        c.stop_first = static_cast<int32_t>(ctx->stop_off.size());
+        c.stop_first = static_cast<int32_t>(q.stop_off.size());
         c.stop_count = p->n_stops;
         for (int i = 0; i < p->n_stops; ++i) {
-            ctx->stop_off.push_back(p->stop_offsets[i]);
-            ctx->stop_col.push_back(make_float4(p->stop_colors[4 * i], p->stop_colors[4 * i + 1],
-                                                p->stop_colors[4 * i + 2], p->stop_colors[4 * i + 3]));
+            q.stop_off.push_back(p->stop_offsets[i]);
+            q.stop_col.push_back(make_float4(p->stop_colors[4 * i], p->stop_colors[4 * i + 1],
+                                             p->stop_colors[4 * i + 2], p->stop_colors[4 * i + 3]));
         }
-        ctx->queued_bytes += static_cast<size_t>(p->n_stops) * 20;
+        q.bytes += static_cast<size_t>(p->n_stops) * 20;
     } else if (p->kind == CY_PAINT_PATTERN) {
         if (!p->pattern || p->pattern_width <= 0 || p->pattern_height <= 0) return CY_EINVAL;
         size_t n = static_cast<size_t>(p->pattern_width) * static_cast<size_t>(p->pattern_height);
-        if (ctx->texels.size() + n > static_cast<size_t>(INT32_MAX)) return CY_EINVAL;
-        c.pat_first = static_cast<int32_t>(ctx->texels.size());
+        if (q.texels.size() + n > static_cast<size_t>(INT32_MAX)) return CY_EINVAL;
+        c.pat_first = static_cast<int32_t>(q.texels.size());
         c.pat_w = p->pattern_width;
         c.pat_h = p->pattern_height;
         c.pat_rep = p->repetition;
         const uchar4 *src = reinterpret_cast<const uchar4 *>(p->pattern);
-        ctx->texels.insert(ctx->texels.end(), src, src + n);
-        ctx->queued_bytes += n * 4;
+        q.texels.insert(q.texels.end(), src, src + n);
+        q.bytes += n * 4;
     } else if (p->kind != CY_PAINT_NONE && p->kind != CY_PAINT_SOLID) {
         return CY_EINVAL;
     }
@@ -238,12 +899,120 @@ bool valid_counts(const int *counts, int n, size_t &total) {
     return total < (static_cast<size_t>(1) << 30);
 }
 
+int queue_geometry(queue &q, const float *points, const int *counts, int n_sub, bool bezier, command &cmd) {
+    size_t total = 0;
+    if (n_sub < 0 || (n_sub > 0 && (!counts || !points)) || !valid_counts(counts, n_sub, total))
+        return CY_EINVAL;
+    bounds_of(points, total, cmd);
+    const float2 *p = reinterpret_cast<const float2 *>(points);
+    if (!bezier) {
+        cmd.geom = 0;
+        cmd.first = static_cast<int32_t>(q.host_pts.size());
+        cmd.count = static_cast<int32_t>(total);
+        size_t at = 0;
+        for (int s = 0; s < n_sub; ++s) {
+            int32_t base = static_cast<int32_t>(q.host_pts.size());
+            int n = counts[s];
+            for (int k = 0; k < n; ++k) {
+                q.host_pts.push_back(p[at + k]);
+                q.host_prev.push_back(k == 0 ? base + n - 1 : base + k - 1);
+            }
+            at += n;
+        }
+        q.bytes += total * 12;
+        return CY_OK;
+    }
+    // Bezier path: one flattening item per subpath start and per cubic.
+    for (int s = 0; s < n_sub; ++s)
+        if (counts[s] != 0 && (counts[s] - 1) % 3 != 0) return CY_EINVAL;
+    cmd.geom = 1;
+    cmd.first = static_cast<int32_t>(q.items.size());
+    int32_t pbase = static_cast<int32_t>(q.bez_pts.size());
+    q.bez_pts.insert(q.bez_pts.end(), p, p + total);
+    size_t at = 0;
+    for (int s = 0; s < n_sub; ++s) {
+        int n = counts[s];
+        if (n == 0) continue;
+        int32_t start = static_cast<int32_t>(q.items.size());
+        flat_item head = {pbase + static_cast<int32_t>(at), 0};
+        q.items.push_back(head);
+        for (int k = 1; k < n; k += 3) {
+            flat_item cub = {pbase + static_cast<int32_t>(at + k - 1), -1};
+            q.items.push_back(cub);
+        }
+        q.items[start].sub_end = static_cast<int32_t>(q.items.size());
+        at += n;
+    }
+    cmd.count = static_cast<int32_t>(q.items.size()) - cmd.first;
+    q.bytes += total * 8 + static_cast<size_t>(cmd.count) * 8;
+    return CY_OK;
+}
+
+int flush_ctx(cy_ctx *c) {
+    if (c->status) return c->status;
+    if (c->q.empty()) return CY_OK;
+    if (!c->cached_frame) c->cached_frame = new (std::nothrow) frame();
+    frame *f = static_cast<frame *>(c->cached_frame);
+    if (!f) return c->fail(CY_ENOMEM);
+    f->reset();
+    f->stream = c->stream;
+    f->engine = c->engine;
+    f->cvs.push_back(c);
+    int rc = f->prepare();
+    if (rc == CY_OK) rc = f->finish();
+    f->cvs.clear();
+    return rc;
+}
+
+int maybe_flush(cy_ctx *c) {
+    queue &q = c->q;
+    if (q.bytes > (static_cast<size_t>(256) << 20) || q.cmds.size() >= 65536 ||
+        q.rows > (static_cast<int64_t>(16) << 20))
+        return c->deferred ? CY_OK : flush_ctx(c);
+    return CY_OK;
+}
+
+int queue_draw(cy_ctx *c, const float *points, const int *counts, int n_sub, bool bezier, const cy_paint *paint,
+               const cy_draw_state *state) {
+    if (!c) return CY_EINVAL;
+    if (c->status) return c->status;
+    if (!paint || !state) return CY_EINVAL;
+    if (state->mask < 0 || state->mask >= static_cast<int>(c->masks.size()) ||
+        (state->mask > 0 && c->masks[state->mask].refs <= 0))
+        return CY_EINVAL;
+    queue &q = c->q;
+    command cmd;
+    std::memset(&cmd, 0, sizeof(cmd));
+    cmd.kind = CMD_FILL;
+    size_t stops = q.stop_off.size(), tex = q.texels.size();
+    int rc = fill_paint(q, paint, cmd);
+    if (rc == CY_OK) rc = queue_geometry(q, points, counts, n_sub, bezier, cmd);
+    if (rc != CY_OK) {
+        q.stop_off.resize(stops);
+        q.stop_col.resize(stops);
+        q.texels.resize(tex);
+        return rc;
+    }
+    fill_state(state, cmd);
+    q.rows += c->H + (cmd.shadow ? c->H + 2 * cmd.sh_border : 0);
+    q.cmds.push_back(cmd);
+    q.mask_ids.push_back(state->mask);
+    q.mask_ids.push_back(0);
+    if (state->mask > 0) c->masks[state->mask].refs++;   // held until the frame finishes
+    return maybe_flush(c);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------- public ABI
 extern "C" {
 
 void cy_set_engine(int engine) { g_engine = engine; }
+void cy_set_deferred(int deferred) { g_deferred = deferred; }
+void cy_set_strip_config(int pixels, int threads) {
+    if (pixels >= 256 && pixels <= 12288) g_strip_pixels = pixels;
+    if (threads == 128 || threads == 256 || threads == 512) g_strip_threads = threads;
+}
 
 // Internal: first engine failure raised in this thread since the last call.
 int cy_take_thread_status(void) {
@@ -265,16 +1034,23 @@ int cy_ctx_create(int width, int height, cy_ctx **out) {
     if (!c) return CY_ENOMEM;
     c->W = width;
     c->H = height;
+    c->engine = g_engine;
+    c->deferred = g_deferred != 0;
+    // Canvases wider than a strip use the per-draw engine.
+    if (width > g_strip_pixels) c->engine = 1;
     c->masks.resize(1);
     size_t npx = static_cast<size_t>(width) * static_cast<size_t>(height);
-    bool ok = c->ok(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) &&
-              c->ok(cudaMalloc(&c->bitmap, npx * sizeof(float4))) &&
-              c->ok(cudaMalloc(&c->lut, 256 * sizeof(float))) &&
-              c->ok(cudaMemsetAsync(c->bitmap, 0, npx * sizeof(float4), c->stream)) &&
-              c->ok(cudaMemcpyAsync(c->lut, linear_lut_host(), 256 * sizeof(float), cudaMemcpyHostToDevice,
-                                    c->stream)) &&
-              c->ok(cudaStreamSynchronize(c->stream));
-    if (!ok) {
+    auto okc = [&](cudaError_t e) {
+        if (e == cudaSuccess) return true;
+        cudaGetLastError();
+        c->fail(e == cudaErrorMemoryAllocation ? CY_ENOMEM : CY_ECUDA);
+        return false;
+    };
+    bool good = okc(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) &&
+                okc(cudaMalloc(&c->bitmap, npx * sizeof(float4))) &&
+                okc(cudaMemsetAsync(c->bitmap, 0, npx * sizeof(float4), c->stream)) &&
+                okc(cudaStreamSynchronize(c->stream));
+    if (!good) {
         int rc = c->status;
         cy_ctx_destroy(c);
         return rc ? rc : CY_ECUDA;
@@ -286,104 +1062,15 @@ int cy_ctx_create(int width, int height, cy_ctx **out) {
 void cy_ctx_destroy(cy_ctx *c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    delete static_cast<frame *>(c->cached_frame);
     for (auto &m : c->masks) m.free_all();
     for (auto &m : c->dead) m.free_all();
     if (c->bitmap) cudaFree(c->bitmap);
-    if (c->lut) cudaFree(c->lut);
-    dbuf *bufs[] = {&c->arena, &c->flat_pts, &c->flat_prev, &c->item_cnt, &c->item_off, &c->boxes,
-                    &c->pat_f4, &c->jobs_dev, &c->row_cnt, &c->row_off, &c->row_cur, &c->row_len,
-                    &c->runs, &c->sums, &c->sh_a, &c->sh_b, &c->sh_rect, &c->get_dev};
-    for (dbuf *b : bufs) b->release();
-    c->staging.release();
-    c->get_host.release();
-    c->offs_host.release();
-    c->rowoff_host.release();
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
 
 int cy_ctx_status(const cy_ctx *c) { return c ? c->status : CY_EINVAL; }
-
-static int queue_geometry(cy_ctx *c, const float *points, const int *counts, int n_sub, bool bezier,
-                          command &cmd) {
-    size_t total = 0;
-    if (n_sub < 0 || (n_sub > 0 && (!counts || !points)) || !valid_counts(counts, n_sub, total))
-        return CY_EINVAL;
-    bounds_of(points, total, cmd);
-    const float2 *p = reinterpret_cast<const float2 *>(points);
-    if (!bezier) {
-        cmd.geom = 0;
-        cmd.first = static_cast<int32_t>(c->host_pts.size());
-        cmd.count = static_cast<int32_t>(total);
-        size_t at = 0;
-        for (int s = 0; s < n_sub; ++s) {
-            int32_t base = static_cast<int32_t>(c->host_pts.size());
-            int n = counts[s];
-            for (int k = 0; k < n; ++k) {
-                c->host_pts.push_back(p[at + k]);
-                c->host_prev.push_back(k == 0 ? base + n - 1 : base + k - 1);
-            }
-            at += n;
-        }
-        c->queued_bytes += total * 12;
-        return CY_OK;
-    }
-    // Bezier path: one flattening item per subpath start and per cubic.
-    cmd.geom = 1;
-    cmd.first = static_cast<int32_t>(c->items.size());
-    int32_t pbase = static_cast<int32_t>(c->bez_pts.size());
-    c->bez_pts.insert(c->bez_pts.end(), p, p + total);
-    size_t at = 0;
-    for (int s = 0; s < n_sub; ++s) {
-        int n = counts[s];
-        if (n == 0) continue;
-        if ((n - 1) % 3 != 0) return CY_EINVAL;
-        int32_t start = static_cast<int32_t>(c->items.size());
-        flat_item head = {pbase + static_cast<int32_t>(at), 0};
-        c->items.push_back(head);
-        for (int k = 1; k < n; k += 3) {
-            flat_item cub = {pbase + static_cast<int32_t>(at + k - 1), -1};
-            c->items.push_back(cub);
-        }
-        c->items[start].sub_end = static_cast<int32_t>(c->items.size());
-        at += n;
-    }
-    cmd.count = static_cast<int32_t>(c->items.size()) - cmd.first;
-    c->queued_bytes += total * 8 + static_cast<size_t>(cmd.count) * 8;
-    return CY_OK;
-}
-
-static int queue_draw(cy_ctx *c, const float *points, const int *counts, int n_sub, bool bezier,
-                      const cy_paint *paint, const cy_draw_state *state) {
-    if (!c) return CY_EINVAL;
-    if (c->status) return c->status;
-    if (!paint || !state) return CY_EINVAL;
-    if (state->mask < 0 || state->mask >= static_cast<int>(c->masks.size()) ||
-        (state->mask > 0 && c->masks[state->mask].refs <= 0))
-        return CY_EINVAL;
-    command cmd;
-    std::memset(&cmd, 0, sizeof(cmd));
-    cmd.kind = CMD_FILL;
-    size_t stops = c->stop_off.size(), tex = c->texels.size();
-    int rc = fill_paint(c, paint, cmd);
-    if (rc == CY_OK) rc = queue_geometry(c, points, counts, n_sub, bezier, cmd);
-    if (rc != CY_OK) {
-        c->stop_off.resize(stops);
-        c->stop_col.resize(stops);
-        c->texels.resize(tex);
-        return rc;
-    }
-    fill_state(state, cmd);
-    c->queued_rows += c->H + (cmd.shadow ? c->H + 2 * cmd.sh_border : 0);
-    c->cmds.push_back(cmd);
-    c->mask_ids.push_back(state->mask);
-    c->mask_ids.push_back(0);
-    if (state->mask > 0) c->masks[state->mask].refs++;   // held until the flush
-    if (c->queued_bytes > (static_cast<size_t>(256) << 20) || c->cmds.size() >= 65536 ||
-        c->queued_rows > (static_cast<int64_t>(16) << 20))
-        return c->flush();
-    return CY_OK;
-}
 
 int cy_fill_path(cy_ctx *c, const float *points, const int *counts, int n_sub, const cy_paint *paint,
                  const cy_draw_state *state) {
@@ -418,10 +1105,11 @@ int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, i
     if (mask_in < 0 || mask_in >= static_cast<int>(c->masks.size()) ||
         (mask_in > 0 && c->masks[mask_in].refs <= 0))
         return CY_EINVAL;
+    queue &q = c->q;
     command cmd;
     std::memset(&cmd, 0, sizeof(cmd));
     cmd.kind = CMD_CLIP;
-    int rc = queue_geometry(c, points, counts, n_sub, true, cmd);
+    int rc = queue_geometry(q, points, counts, n_sub, true, cmd);
     if (rc != CY_OK) return rc;
     int id = 0;
     for (int i = 1; i < static_cast<int>(c->masks.size()); ++i)
@@ -432,396 +1120,155 @@ int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, i
     }
     mask_slot &m = c->masks[id];
     size_t H1 = static_cast<size_t>(c->H) + 1;
-    if (!c->ok(cudaMalloc(&m.vis, static_cast<size_t>(c->W) * c->H * sizeof(float))) ||
-        !c->ok(cudaMalloc(&m.off, H1 * 4)) || !c->ok(cudaMalloc(&m.len, H1 * 4)) ||
-        !c->ok(cudaMalloc(&m.last_row, 4)))
+    auto okc = [&](cudaError_t e) {
+        if (e == cudaSuccess) return true;
+        cudaGetLastError();
+        c->fail(CY_ENOMEM);
+        return false;
+    };
+    if (!okc(cudaMalloc(&m.vis, static_cast<size_t>(c->W) * c->H * sizeof(float))) ||
+        !okc(cudaMalloc(&m.off, H1 * 4)) || !okc(cudaMalloc(&m.len, H1 * 4)) || !okc(cudaMalloc(&m.last_row, 4)))
         return c->status;
     m.refs = 2;   // the caller's reference plus the queued command's
-    c->queued_rows += c->H;
-    c->cmds.push_back(cmd);
-    c->mask_ids.push_back(mask_in);
-    c->mask_ids.push_back(id);
+    q.rows += c->H;
+    q.cmds.push_back(cmd);
+    q.mask_ids.push_back(mask_in);
+    q.mask_ids.push_back(id);
     if (mask_in > 0) c->masks[mask_in].refs++;
     *mask_out = id;
-    return CY_OK;
+    return maybe_flush(c);
 }
 
 int cy_put_image(cy_ctx *c, const unsigned char *image, int w, int h, int stride, int x, int y) {
     if (!c) return CY_EINVAL;
     if (c->status) return c->status;
     if (!image || w <= 0 || h <= 0) return CY_OK;
+    queue &q = c->q;
     command cmd;
     std::memset(&cmd, 0, sizeof(cmd));
     cmd.kind = CMD_PUT;
     cmd.put_x = x; cmd.put_y = y; cmd.put_w = w; cmd.put_h = h;
-    cmd.put_first = static_cast<int64_t>(c->put_px.size());
+    cmd.put_first = static_cast<int64_t>(q.put_px.size());
     for (int row = 0; row < h; ++row) {
         const unsigned char *src = image + static_cast<ptrdiff_t>(row) * stride;
-        c->put_px.insert(c->put_px.end(), src, src + static_cast<size_t>(w) * 4);
+        q.put_px.insert(q.put_px.end(), src, src + static_cast<size_t>(w) * 4);
     }
-    c->cmds.push_back(cmd);
-    c->mask_ids.push_back(0);
-    c->mask_ids.push_back(0);
-    c->queued_bytes += static_cast<size_t>(w) * h * 4;
-    return CY_OK;
+    q.cmds.push_back(cmd);
+    q.mask_ids.push_back(0);
+    q.mask_ids.push_back(0);
+    q.bytes += static_cast<size_t>(w) * h * 4;
+    return maybe_flush(c);
 }
 
 int cy_flush(cy_ctx *c) {
     if (!c) return CY_EINVAL;
-    int rc = c->flush();
+    int rc = flush_ctx(c);
     if (rc) return rc;
-    return c->ok(cudaStreamSynchronize(c->stream)) ? CY_OK : c->status;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return c->fail(CY_ECUDA);
+    }
+    return CY_OK;
 }
 
 int cy_get_image(cy_ctx *c, unsigned char *image, int w, int h, int stride, int x, int y) {
     if (!c) return CY_EINVAL;
+    if (c->status) return c->status;
     if (!image || w <= 0 || h <= 0) return CY_OK;
-    int rc = c->flush();
-    if (rc) return rc;
-    size_t bytes = static_cast<size_t>(w) * h * 4;
-    if (!c->get_dev.ensure(bytes)) return c->fail(CY_ENOMEM);
-    if (!c->get_host.ensure(bytes)) return c->fail(CY_ENOMEM);
-    dim3 blk(32, 8), grd((w + 31) / 32, (h + 7) / 8);
-    k_get<<<grd, blk, 0, c->stream>>>(c->bitmap, c->W, c->H, c->get_dev.as<uchar4>(), w, h, x, y);
-    if (!c->ok(cudaGetLastError())) return c->status;
-    if (!c->ok(cudaMemcpyAsync(c->get_host.p, c->get_dev.p, bytes, cudaMemcpyDeviceToHost, c->stream)))
-        return c->status;
-    if (!c->ok(cudaStreamSynchronize(c->stream))) return c->status;
-    const unsigned char *src = static_cast<const unsigned char *>(c->get_host.p);
-    for (int row = 0; row < h; ++row)
-        std::memcpy(image + static_cast<ptrdiff_t>(row) * stride, src + static_cast<size_t>(row) * w * 4,
-                    static_cast<size_t>(w) * 4);
-    return CY_OK;
+    queue &q = c->q;
+    command cmd;
+    std::memset(&cmd, 0, sizeof(cmd));
+    cmd.kind = CMD_GET;
+    cmd.get_x = x; cmd.get_y = y; cmd.get_w = w; cmd.get_h = h;
+    cmd.get_out = q.get_bytes;
+    q.get_bytes += static_cast<int64_t>(w) * h * 4;
+    q.get_bytes = (q.get_bytes + 15) & ~static_cast<int64_t>(15);
+    q.cmds.push_back(cmd);
+    q.mask_ids.push_back(0);
+    q.mask_ids.push_back(0);
+    q.get_dst.push_back(c->deferred ? nullptr : image);
+    q.get_stride.push_back(stride);
+    if (c->deferred) return CY_OK;
+    return flush_ctx(c);
 }
 
 int cy_read_linear(cy_ctx *c, float *out) {
     if (!c || !out) return CY_EINVAL;
-    int rc = c->flush();
+    int rc = flush_ctx(c);
     if (rc) return rc;
     size_t bytes = static_cast<size_t>(c->W) * c->H * sizeof(float4);
-    if (!c->ok(cudaMemcpyAsync(out, c->bitmap, bytes, cudaMemcpyDeviceToHost, c->stream)) ||
-        !c->ok(cudaStreamSynchronize(c->stream)))
-        return c->status;
+    if (cudaMemcpyAsync(out, c->bitmap, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return c->fail(CY_ECUDA);
+    }
+    return CY_OK;
+}
+
+// ------------------------------------------------------------ batched API
+struct cy_frame {
+    std::unique_ptr<frame> f;
+    cudaStream_t stream = nullptr;
+};
+
+void cy_frame_destroy(cy_frame *fr) {
+    if (!fr) return;
+    if (fr->stream) cudaStreamSynchronize(fr->stream);
+    fr->f.reset();
+    if (fr->stream) cudaStreamDestroy(fr->stream);
+    delete fr;
+}
+
+int cy_frame_create(cy_ctx *const *ctxs, int n, int engine, cy_frame **out) {
+    if (!out || n < 0 || (n > 0 && !ctxs)) return CY_EINVAL;
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!ctxs[i]) return CY_EINVAL;
+        if (ctxs[i]->status) return ctxs[i]->status;
+        if (engine == 0 && ctxs[i]->W > g_strip_pixels) return CY_EINVAL;
+    }
+    cy_frame *fr = new (std::nothrow) cy_frame();
+    if (!fr) return CY_ENOMEM;
+    fr->f.reset(new frame());
+    if (cudaStreamCreateWithFlags(&fr->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete fr;
+        return CY_ECUDA;
+    }
+    fr->f->stream = fr->stream;
+    fr->f->engine = engine;
+    for (int i = 0; i < n; ++i) fr->f->cvs.push_back(ctxs[i]);
+    int rc = fr->f->prepare();
+    if (rc) {
+        cy_frame_destroy(fr);
+        return rc;
+    }
+    *out = fr;
+    return CY_OK;
+}
+
+int cy_frame_run(cy_frame *fr) { return fr ? fr->f->run() : CY_EINVAL; }
+
+int cy_frame_finish(cy_frame *fr) { return fr ? fr->f->finish() : CY_EINVAL; }
+
+int cy_frame_sync(cy_frame *fr) {
+    if (!fr) return CY_EINVAL;
+    if (cudaStreamSynchronize(fr->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return fr->f->fail(CY_ECUDA);
+    }
+    return fr->f->status;
+}
+
+void *cy_frame_stream(cy_frame *fr) { return fr ? static_cast<void *>(fr->stream) : nullptr; }
+
+int cy_ctx_take_reads(cy_ctx *c, unsigned char *out, size_t cap, size_t *len) {
+    if (!c) return CY_EINVAL;
+    if (len) *len = c->deferred_out.size();
+    if (c->deferred_out.size() > cap) return -2;
+    if (!c->deferred_out.empty()) std::memcpy(out, c->deferred_out.data(), c->deferred_out.size());
+    c->deferred_out.clear();
     return CY_OK;
 }
 
 }  // extern "C"
-
-// ------------------------------------------------------------------ flush
-int cy_ctx::scan(const int32_t *in, int32_t *out, int n) {
-    // Exclusive scan with recursion over tile sums.
-    int tiles = (n + 4095) / 4096;
-    if (tiles <= 0) return CY_OK;
-    if (tiles == 1) {
-        k_scan_tiles<<<1, 1024, 0, stream>>>(in, out, n, nullptr);
-        return ok(cudaGetLastError()) ? CY_OK : status;
-    }
-    dbuf sums, offs;
-    if (!sums.ensure(static_cast<size_t>(tiles) * 4) || !offs.ensure(static_cast<size_t>(tiles) * 4))
-        return fail(CY_ENOMEM);
-    k_scan_tiles<<<tiles, 1024, 0, stream>>>(in, out, n, sums.as<int32_t>());
-    int rc = scan(sums.as<int32_t>(), offs.as<int32_t>(), tiles);
-    if (rc == CY_OK) {
-        k_scan_add<<<(n + 255) / 256, 256, 0, stream>>>(out, n, offs.as<int32_t>());
-        if (!ok(cudaGetLastError())) rc = status;
-    }
-    cudaStreamSynchronize(stream);
-    sums.release();
-    offs.release();
-    return rc;
-}
-
-int cy_ctx::clip_mask(const command &c, int mask_in, int mask_out, const scan_job &job, int job_index,
-                      const int32_t *rowoff_h) {
-    (void)c;
-    mask_slot &nm = masks[mask_out];
-    const mask_slot *om = mask_in > 0 ? &masks[mask_in] : nullptr;
-    int64_t path_runs = rowoff_h[job.row_base + job.rows] - rowoff_h[job.row_base];
-    int64_t cap = path_runs + (om ? om->cap : 2 * static_cast<int64_t>(H));
-    if (cap > INT32_MAX) return fail(CY_ENOMEM);
-    if (!ok(cudaMalloc(&nm.runs, static_cast<size_t>(std::max<int64_t>(cap, 1)) * sizeof(run))) ||
-        !ok(cudaMalloc(&nm.sums, static_cast<size_t>(std::max<int64_t>(cap, 1)) * sizeof(float))))
-        return status;
-    nm.cap = cap;
-    // Row capacities: the path's raw runs plus the old mask's runs.
-    k_clip_caps<<<(H + 255) / 256, 256, 0, stream>>>(row_off.as<int32_t>() + job.row_base, om ? om->off : nullptr,
-                                                      H, nm.len);
-    if (!ok(cudaMemsetAsync(nm.len + H, 0, 4, stream))) return status;
-    int rc = scan(nm.len, nm.off, H + 1);
-    if (rc) return rc;
-    if (!ok(cudaMemsetAsync(nm.last_row, 0xff, 4, stream))) return status;
-    clip_args a;
-    a.p_off = row_off.as<int32_t>();
-    a.p_len = row_len.as<int32_t>();
-    a.p_runs = runs.as<run>();
-    a.p_base = job.row_base;
-    a.p_box = boxes.as<cover_box>() + job_index;
-    a.o_off = om ? om->off : nullptr;
-    a.o_len = om ? om->len : nullptr;
-    a.o_runs = om ? om->runs : nullptr;
-    a.o_last_row = om ? om->last_row : nullptr;
-    a.n_off = nm.off;
-    a.n_len = nm.len;
-    a.n_runs = nm.runs;
-    a.n_last_row = nm.last_row;
-    a.W = W;
-    a.H = H;
-    k_clip_rows<<<(H + 127) / 128, 128, 0, stream>>>(a);
-    k_mask_prefix<<<(H + 127) / 128, 128, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, H);
-    k_mask_fill<<<std::max(1, (H + 7) / 8), 256, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, W, H, nm.vis);
-    return ok(cudaGetLastError()) ? CY_OK : status;
-}
-
-int cy_ctx::flush() {
-    if (status) return status;
-    if (cmds.empty()) return CY_OK;
-    if (!ok(cudaStreamSynchronize(stream))) return status;
-    for (auto &m : dead) m.free_all();
-    dead.clear();
-    // Arena layout: everything queued goes up in one copy.
-    size_t o_cmd = 0;
-    size_t o_hpts = align256(o_cmd + cmds.size() * sizeof(command));
-    size_t o_hprev = align256(o_hpts + host_pts.size() * sizeof(float2));
-    size_t o_bez = align256(o_hprev + host_prev.size() * sizeof(int32_t));
-    size_t o_items = align256(o_bez + bez_pts.size() * sizeof(float2));
-    size_t o_soff = align256(o_items + items.size() * sizeof(flat_item));
-    size_t o_scol = align256(o_soff + stop_off.size() * sizeof(float));
-    size_t o_tex = align256(o_scol + stop_col.size() * sizeof(float4));
-    size_t o_put = align256(o_tex + texels.size() * sizeof(uchar4));
-    size_t total = align256(o_put + put_px.size());
-    if (!arena.ensure(total) || !staging.ensure(total)) return fail(CY_ENOMEM);
-    char *h = static_cast<char *>(staging.p);
-    auto put = [&](size_t off, const void *src, size_t n) { if (n) std::memcpy(h + off, src, n); };
-    put(o_hpts, host_pts.data(), host_pts.size() * sizeof(float2));
-    put(o_hprev, host_prev.data(), host_prev.size() * sizeof(int32_t));
-    put(o_bez, bez_pts.data(), bez_pts.size() * sizeof(float2));
-    put(o_items, items.data(), items.size() * sizeof(flat_item));
-    put(o_soff, stop_off.data(), stop_off.size() * sizeof(float));
-    put(o_scol, stop_col.data(), stop_col.size() * sizeof(float4));
-    put(o_tex, texels.data(), texels.size() * sizeof(uchar4));
-    put(o_put, put_px.data(), put_px.size());
-    char *d = static_cast<char *>(arena.p);
-    if (total > o_hpts &&
-        !ok(cudaMemcpyAsync(d + o_hpts, h + o_hpts, total - o_hpts, cudaMemcpyHostToDevice, stream)))
-        return status;
-    const float2 *d_hpts = reinterpret_cast<const float2 *>(d + o_hpts);
-    const int32_t *d_hprev = reinterpret_cast<const int32_t *>(d + o_hprev);
-    const float2 *d_bez = reinterpret_cast<const float2 *>(d + o_bez);
-    const flat_item *d_items = reinterpret_cast<const flat_item *>(d + o_items);
-    paint_src src;
-    src.stop_off = reinterpret_cast<const float *>(d + o_soff);
-    src.stop_col = reinterpret_cast<const float4 *>(d + o_scol);
-    src.texels = nullptr;
-    if (!texels.empty()) {
-        if (!pat_f4.ensure(texels.size() * sizeof(float4))) return fail(CY_ENOMEM);
-        int n = static_cast<int>(texels.size());
-        k_pattern_prep<<<(n + 255) / 256, 256, 0, stream>>>(reinterpret_cast<const uchar4 *>(d + o_tex),
-                                                            pat_f4.as<float4>(), n, lut);
-        src.texels = pat_f4.as<float4>();
-    }
-    // Flatten every Bezier path of the flush (path_to_lines, hpp:1495-1524).
-    int n_items = static_cast<int>(items.size());
-    const int32_t *offs_h = nullptr;
-    if (n_items > 0) {
-        if (!item_cnt.ensure(static_cast<size_t>(n_items + 1) * 4) ||
-            !item_off.ensure(static_cast<size_t>(n_items + 1) * 4) ||
-            !offs_host.ensure(static_cast<size_t>(n_items + 1) * 4))
-            return fail(CY_ENOMEM);
-        k_flat_count<<<(n_items + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items, item_cnt.as<int32_t>());
-        if (!ok(cudaMemsetAsync(item_cnt.as<int32_t>() + n_items, 0, 4, stream))) return status;
-        int rc = scan(item_cnt.as<int32_t>(), item_off.as<int32_t>(), n_items + 1);
-        if (rc) return rc;
-        if (!ok(cudaMemcpyAsync(offs_host.p, item_off.p, static_cast<size_t>(n_items + 1) * 4,
-                                cudaMemcpyDeviceToHost, stream)) ||
-            !ok(cudaStreamSynchronize(stream)))
-            return status;
-        offs_h = static_cast<const int32_t *>(offs_host.p);
-        int64_t nflat = offs_h[n_items];
-        if (nflat < 0 || nflat > (static_cast<int64_t>(1) << 30)) return fail(CY_ENOMEM);
-        if (!flat_pts.ensure(static_cast<size_t>(nflat + 1) * sizeof(float2)) ||
-            !flat_prev.ensure(static_cast<size_t>(nflat + 1) * 4))
-            return fail(CY_ENOMEM);
-        k_flat_emit<<<(n_items + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items, item_off.as<int32_t>(),
-                                                               flat_pts.as<float2>(), flat_prev.as<int32_t>(),
-                                                               nflat);
-        if (!ok(cudaGetLastError())) return status;
-    }
-    for (command &c : cmds) {
-        if (c.kind == CMD_PUT) continue;
-        if (c.geom == 0) {
-            c.line_first = c.first;
-            c.line_count = c.count;
-        } else if (c.count == 0 || !offs_h) {
-            c.line_first = 0;
-            c.line_count = 0;
-        } else {
-            c.line_first = offs_h[c.first];
-            c.line_count = offs_h[c.first + c.count] - c.line_first;
-        }
-    }
-    std::memcpy(h + o_cmd, cmds.data(), cmds.size() * sizeof(command));
-    if (!ok(cudaMemcpyAsync(d + o_cmd, h + o_cmd, cmds.size() * sizeof(command), cudaMemcpyHostToDevice, stream)))
-        return status;
-    const command *d_cmds = reinterpret_cast<const command *>(d + o_cmd);
-    // Scan-conversion jobs: the shadow pass (padded canvas) and the main pass
-    // of each draw, and the path of each clip.
-    std::vector<scan_job> jobs;
-    std::vector<int> main_job(cmds.size(), -1), shadow_job(cmds.size(), -1);
-    int64_t total_rows = 0, total_segs = 0;
-    auto add_job = [&](const command &c, int rows_n, int cols_n, float wd, float ht, float ox, float oy) {
-        scan_job j;
-        std::memset(&j, 0, sizeof(j));
-        j.geom = c.geom;
-        j.line_first = c.line_first;
-        j.seg_first = static_cast<int32_t>(total_segs);
-        j.seg_count = c.line_count;
-        j.row_base = static_cast<int32_t>(total_rows);
-        j.rows = rows_n;
-        j.cols = cols_n;
-        j.width = wd;
-        j.height = ht;
-        j.offx = ox;
-        j.offy = oy;
-        total_rows += rows_n;
-        total_segs += c.line_count;
-        jobs.push_back(j);
-        return static_cast<int>(jobs.size()) - 1;
-    };
-    for (size_t i = 0; i < cmds.size(); ++i) {
-        const command &c = cmds[i];
-        if (c.kind == CMD_PUT) continue;
-        if (c.kind == CMD_FILL && c.shadow) {
-            int b = c.sh_border;
-            int ew = W + 2 * b, eh = H + 2 * b;
-            shadow_job[i] = add_job(c, eh, ew + 2, static_cast<float>(ew), static_cast<float>(eh), c.sh_offx,
-                                    c.sh_offy);
-        }
-        main_job[i] = add_job(c, H, W + 2, static_cast<float>(W), static_cast<float>(H), 0.0f, 0.0f);
-    }
-    if (total_rows > INT32_MAX / 2 || total_segs > INT32_MAX / 2) return fail(CY_ENOMEM);
-    int n_jobs = static_cast<int>(jobs.size());
-    const int32_t *rowoff_h = nullptr;
-    job_tables t;
-    std::memset(&t, 0, sizeof(t));
-    if (n_jobs > 0) {
-        size_t nr = static_cast<size_t>(total_rows);
-        if (!jobs_dev.ensure(jobs.size() * sizeof(scan_job)) || !row_cnt.ensure((nr + 1) * 4) ||
-            !row_off.ensure((nr + 2) * 4) || !row_cur.ensure((nr + 1) * 4) || !row_len.ensure((nr + 1) * 4) ||
-            !boxes.ensure(jobs.size() * sizeof(cover_box)) || !rowoff_host.ensure((nr + 1) * 4))
-            return fail(CY_ENOMEM);
-        if (!ok(cudaMemcpyAsync(jobs_dev.p, jobs.data(), jobs.size() * sizeof(scan_job), cudaMemcpyHostToDevice,
-                                stream)) ||
-            !ok(cudaMemsetAsync(row_cnt.p, 0, (nr + 1) * 4, stream)) ||
-            !ok(cudaMemsetAsync(row_cur.p, 0, (nr + 1) * 4, stream)))
-            return status;
-        k_box_init<<<(n_jobs + 255) / 256, 256, 0, stream>>>(boxes.as<cover_box>(), n_jobs);
-        t.jobs = jobs_dev.as<scan_job>();
-        t.n_jobs = n_jobs;
-        t.pts[0] = d_hpts;
-        t.prev[0] = d_hprev;
-        t.pts[1] = flat_pts.p ? flat_pts.as<float2>() : d_hpts;
-        t.prev[1] = flat_prev.p ? flat_prev.as<int32_t>() : d_hprev;
-        t.boxes = boxes.as<cover_box>();
-        t.row_cnt = row_cnt.as<int32_t>();
-        t.row_cur = row_cur.as<int32_t>();
-        int segs = static_cast<int>(total_segs);
-        int grid = std::max(1, std::min((segs + 7) / 8, 152 * 32));
-        if (segs > 0) k_runs<false><<<grid, 256, 0, stream>>>(t, segs);
-        int rc = scan(row_cnt.as<int32_t>(), row_off.as<int32_t>(), static_cast<int>(nr) + 1);
-        if (rc) return rc;
-        if (!ok(cudaMemcpyAsync(rowoff_host.p, row_off.p, (nr + 1) * 4, cudaMemcpyDeviceToHost, stream)) ||
-            !ok(cudaStreamSynchronize(stream)))
-            return status;
-        rowoff_h = static_cast<const int32_t *>(rowoff_host.p);
-        int64_t nruns = rowoff_h[nr];
-        if (nruns < 0) return fail(CY_ENOMEM);
-        if (!runs.ensure(static_cast<size_t>(nruns + 1) * sizeof(run)) ||
-            !sums.ensure(static_cast<size_t>(nruns + 1) * sizeof(float)))
-            return fail(CY_ENOMEM);
-        t.row_off = row_off.as<int32_t>();
-        t.runs = runs.as<run>();
-        if (segs > 0) k_runs<true><<<grid, 256, 0, stream>>>(t, segs);
-        k_rows<<<static_cast<int>((nr + 127) / 128), 128, 0, stream>>>(
-            row_off.as<int32_t>(), row_cnt.as<int32_t>(), row_cur.as<int32_t>(), row_len.as<int32_t>(),
-            runs.as<run>(), sums.as<float>(), static_cast<int>(nr));
-        if (!ok(cudaGetLastError())) return status;
-    }
-    row_view rv;
-    rv.row_off = row_off.as<int32_t>();
-    rv.row_len = row_len.as<int32_t>();
-    rv.runs = runs.as<run>();
-    rv.sums = sums.as<float>();
-    const uint8_t *d_put = reinterpret_cast<const uint8_t *>(d + o_put);
-    for (size_t i = 0; i < cmds.size(); ++i) {
-        const command &c = cmds[i];
-        int in_id = mask_ids[2 * i], out_id = mask_ids[2 * i + 1];
-        if (c.kind == CMD_PUT) {
-            dim3 blk(32, 8), grd((c.put_w + 31) / 32, (c.put_h + 7) / 8);
-            k_put<<<grd, blk, 0, stream>>>(d_cmds + i, d_put, bitmap, W, H, lut);
-            if (!ok(cudaGetLastError())) return status;
-            continue;
-        }
-        if (c.kind == CMD_CLIP) {
-            int rc = clip_mask(c, in_id, out_id, jobs[main_job[i]], main_job[i], rowoff_h);
-            if (rc) return rc;
-            continue;
-        }
-        const float *vis = in_id > 0 ? masks[in_id].vis : nullptr;
-        if (c.shadow) {
-            const scan_job &sj = jobs[shadow_job[i]];
-            int b = c.sh_border;
-            int ew = W + 2 * b, eh = H + 2 * b;
-            size_t area = static_cast<size_t>(ew + 1) * eh;
-            if (!sh_a.ensure(area * 4) || !sh_b.ensure(area * 4) || !sh_rect.ensure(sizeof(shadow_rect)))
-                return fail(CY_ENOMEM);
-            shadow_rect *rect = sh_rect.as<shadow_rect>();
-            k_shadow_rect<<<1, 1, 0, stream>>>(boxes.as<cover_box>() + shadow_job[i], W, H, b, rect);
-            k_shadow_raster<<<std::max(1, (eh + 7) / 8), 256, 0, stream>>>(d_cmds + i, src, rv, sj.row_base, rect,
-                                                                           sh_a.as<float>());
-            k_blur_rows<<<(eh + 127) / 128, 128, 0, stream>>>(sh_a.as<float>(), sh_b.as<float>(), rect,
-                                                               c.sh_radius, c.sh_w1, c.sh_w2);
-            k_blur_cols<<<(ew + 1 + 127) / 128, 128, 0, stream>>>(sh_a.as<float>(), sh_b.as<float>(), rect,
-                                                                   c.sh_radius, c.sh_w1, c.sh_w2);
-            dim3 blk(32, 8), cgrd((W + 31) / 32, (H + 7) / 8);
-            k_shadow_composite<<<cgrd, blk, 0, stream>>>(d_cmds + i, bitmap, W, H, vis, rect, sh_a.as<float>());
-            if (!ok(cudaGetLastError())) return status;
-        }
-        bool clearing = !(c.op & 8);
-        int y0 = clearing ? 0 : std::max(0, std::min(H, c.gy0));
-        int y1 = clearing ? H : std::max(0, std::min(H, c.gy1 + 1));
-        if (y1 > y0) {
-            paint_args pa;
-            pa.cmd = d_cmds + i;
-            pa.bitmap = bitmap;
-            pa.W = W;
-            pa.H = H;
-            pa.rv = rv;
-            pa.row_base = jobs[main_job[i]].row_base;
-            pa.vis = vis;
-            pa.y_begin = y0;
-            pa.y_end = y1;
-            pa.src = src;
-            k_paint<<<std::max(1, (y1 - y0 + 7) / 8), 256, 0, stream>>>(pa);
-            if (!ok(cudaGetLastError())) return status;
-        }
-    }
-    // Release the references the queued commands held on clip masks.
-    for (size_t i = 0; i < cmds.size(); ++i) {
-        int in = mask_ids[2 * i], out = mask_ids[2 * i + 1];
-        if (in > 0) cy_mask_release(this, in);
-        if (out > 0) cy_mask_release(this, out);
-    }
-    cmds.clear();
-    host_pts.clear();
-    host_prev.clear();
-    bez_pts.clear();
-    items.clear();
-    stop_off.clear();
-    stop_col.clear();
-    texels.clear();
-    put_px.clear();
-    mask_ids.clear();
-    queued_bytes = 0;
-    queued_rows = 0;
-    return CY_OK;
-}

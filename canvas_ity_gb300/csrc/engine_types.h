@@ -6,7 +6,7 @@
 
 namespace cyg {
 
-enum { CMD_FILL = 1, CMD_CLIP = 2, CMD_PUT = 3 };
+enum { CMD_FILL = 1, CMD_CLIP = 2, CMD_PUT = 3, CMD_GET = 4 };
 
 // One flattening work item: the start point of a subpath (emits one point)
 // or one cubic of it (emits its adaptive polyline, hpp:1398-1487).
@@ -36,9 +36,9 @@ struct __align__(16) command {
     // put_image_data
     int32_t put_x, put_y, put_w, put_h;
     int64_t put_first;
-    // clip masks (device pointers resolved at flush)
-    const float *mask_in;
-    float *mask_out;
+    // get_image_data: compact RGBA8 rectangle at get_out in the frame's buffer
+    int32_t get_x, get_y, get_w, get_h;
+    int64_t get_out;
     // conservative bounds of the geometry, device pixels (host-computed)
     int32_t gx0, gy0, gx1, gy1;
 };

@@ -1,0 +1,291 @@
+// strips.cuh -- the batched ("strip") render path.
+//
+// After all scan conversions of a frame are done (row-sorted runs with
+// running sums, see kernels.cuh), one persistent kernel renders every canvas
+// of the frame.  A work item is a horizontal strip of one canvas, at most
+// `strip_pixels` pixels; its premultiplied linear float pixels live in shared
+// memory while the kernel applies, in call order, every command of the
+// canvas: shadow composite and paint of draws, put_image_data,
+// get_image_data.  Pixels are read from HBM at most once (when the canvas
+// already had content) and written once (RGBA8 for the reads, float state
+// for a canvas that persists).  Each pixel of a strip is always handled by
+// the same thread (fixed 32-pixel chunk to warp assignment), so no barrier
+// is needed between commands.
+#ifndef CY_STRIPS_CUH
+#define CY_STRIPS_CUH
+
+#include "kernels.cuh"
+
+namespace cyg {
+
+struct strip_canvas {
+    int32_t W, H, TH;         // size and strip height
+    int32_t cmd_first, cmd_count;
+    int32_t flags;            // 1: load float state from `bitmap`, 2: store it back
+    float4 *bitmap;
+};
+
+struct strip_cmd {            // per command extras resolved at the flush
+    int32_t main_row_base;    // rows of the command's main scan job
+    int32_t has_shadow;
+    int64_t shadow_img;       // float offset of the blurred shadow image
+    const float *vis;         // clip visibility (null: whole canvas)
+    int64_t get_out;          // GET: byte offset of the compact RGBA8 output
+    int32_t get_x, get_y, get_w, get_h;
+};
+
+struct strip_params {
+    const strip_canvas *canvases;
+    const int2 *items;        // (canvas, first row) in processing order
+    int n_items;
+    int *counter;             // work-queue cursor (reset per run)
+    const command *cmds;
+    const strip_cmd *ext;
+    row_view rv;
+    paint_src src;
+    const shadow_rect *rects; // per command (valid for shadows)
+    const float *shadow_imgs;
+    const uint8_t *put_px;
+    const float *lut;
+    uint8_t *get_buf;
+    int strip_pixels;
+};
+
+__global__ void __launch_bounds__(256) k_strips(strip_params P) {
+    extern __shared__ float4 px[];
+    __shared__ int item_slot;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) item_slot = atomicAdd(P.counter, 1);
+        __syncthreads();
+        int it = item_slot;
+        if (it >= P.n_items) break;
+        int2 item = P.items[it];
+        const strip_canvas cv = P.canvases[item.x];
+        const int W = cv.W, y0 = item.y;
+        const int rows = min(cv.TH, cv.H - y0);
+        const int cpr = (W + 31) >> 5;           // 32-pixel chunks per row
+        const int chunks = rows * cpr;
+        // Initial state.
+        for (int ch = warp; ch < chunks; ch += nwarps) {
+            int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
+            if (x >= W) continue;
+            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (cv.flags & 1) v = cv.bitmap[static_cast<size_t>(y0 + ly) * W + x];
+            px[ly * W + x] = v;
+        }
+        for (int ci = cv.cmd_first; ci < cv.cmd_first + cv.cmd_count; ++ci) {
+            const command &c = P.cmds[ci];
+            const strip_cmd &e = P.ext[ci];
+            if (c.kind == CMD_CLIP) continue;
+            if (c.kind == CMD_PUT) {
+                for (int ch = warp; ch < chunks; ch += nwarps) {
+                    int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
+                    int y = y0 + ly;
+                    int ix = x - c.put_x, iy = y - c.put_y;
+                    if (x >= W || ix < 0 || ix >= c.put_w || iy < 0 || iy >= c.put_h) continue;
+                    const uint8_t *p = P.put_px + c.put_first + (static_cast<size_t>(iy) * c.put_w + ix) * 4;
+                    float a = static_cast<float>(p[3]) / 255.0f;
+                    px[ly * W + x] = make_float4(P.lut[p[0]] * a, P.lut[p[1]] * a, P.lut[p[2]] * a, a);
+                }
+                continue;
+            }
+            if (c.kind == CMD_GET) {
+                for (int ch = warp; ch < chunks; ch += nwarps) {
+                    int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
+                    int y = y0 + ly;
+                    int ix = x - e.get_x, iy = y - e.get_y;
+                    if (x >= W || ix < 0 || ix >= e.get_w || iy < 0 || iy >= e.get_h) continue;
+                    uchar4 o = to_srgb8(px[ly * W + x], x, y);
+                    reinterpret_cast<uchar4 *>(P.get_buf + e.get_out)[static_cast<size_t>(iy) * e.get_w + ix] = o;
+                }
+                continue;
+            }
+            const int op = c.op;
+            const bool clearing = !(op & 8);
+            if (e.has_shadow) {
+                // render_shadow's composite (hpp:2504-2538)
+                const shadow_rect r = P.rects[ci];
+                const float *img = P.shadow_imgs + e.shadow_img;
+                int b = c.sh_border;
+                int sx0 = max(0, r.left - b), sx1 = min(W, r.right - b);
+                if (r.width > 0 && r.height > 0) {
+                    for (int ch = warp; ch < chunks; ch += nwarps) {
+                        int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
+                        int y = y0 + ly;
+                        if (x < sx0 || x >= sx1 || y + b < r.top || y + b >= r.bottom) continue;
+                        float vis = e.vis ? e.vis[static_cast<size_t>(y) * W + x] : 1.0f;
+                        if (vis < kVisible) continue;
+                        float s = img[static_cast<size_t>(y + b - r.top) * r.width + (x + b - r.left)];
+                        float k = c.alpha * s;
+                        float4 fore = make_float4(c.sh_color[0] * k, c.sh_color[1] * k, c.sh_color[2] * k,
+                                                  c.sh_color[3] * k);
+                        px[ly * W + x] = blend(px[ly * W + x], fore, op, vis);
+                    }
+                }
+            }
+            // render_main (hpp:2551-2605)
+            for (int ch = warp; ch < chunks; ch += nwarps) {
+                int ly = ch / cpr, x0 = (ch - ly * cpr) << 5;
+                int y = y0 + ly;
+                int row = e.main_row_base + y;
+                int n = P.rv.row_len[row];
+                const run *r = P.rv.runs + P.rv.row_off[row];
+                const float *sm = P.rv.sums + P.rv.row_off[row];
+                int xs, xe;
+                if (clearing) {
+                    xs = 0;
+                    xe = W - 1;
+                } else {
+                    if (n == 0) continue;
+                    xs = r[0].x;
+                    xe = min(r[n - 1].x, W - 1);
+                }
+                if (x0 + 31 < xs || x0 > xe) continue;
+                int x = x0 + lane;
+                if (x < xs || x > xe) continue;
+                float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+                float vis = e.vis ? e.vis[static_cast<size_t>(y) * W + x] : 1.0f;
+                if ((cov >= kVisible || clearing) && vis >= kVisible) {
+                    float4 p = paint_at(c, P.src, static_cast<float>(x) + 0.5f, static_cast<float>(y) + 0.5f);
+                    float k = cov * c.alpha;
+                    float4 fore = make_float4(p.x * k, p.y * k, p.z * k, p.w * k);
+                    px[ly * W + x] = blend(px[ly * W + x], fore, op, vis);
+                }
+            }
+        }
+        if (cv.flags & 2) {
+            for (int ch = warp; ch < chunks; ch += nwarps) {
+                int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
+                if (x >= W) continue;
+                cv.bitmap[static_cast<size_t>(y0 + ly) * W + x] = px[ly * W + x];
+            }
+        }
+    }
+}
+
+// ------------------------------------------------ frame-wide shadow passes
+// All shadows of a frame are prepared before the strip kernel: working
+// rectangle, alpha raster and blur of every shadowed draw, batched.
+struct shadow_job {
+    int32_t cmd;            // command index
+    int32_t job;            // scan job (padded canvas) index
+    int32_t row_base;       // its first row in the shared row arrays
+    int32_t W, H, border;   // canvas size and border
+    int64_t img;            // float offset of its image (and of its scratch)
+    int32_t radius;
+    float w1, w2;
+    int32_t pad;
+};
+
+__global__ void k_shadow_rects(const shadow_job *sj, int n, const cover_box *boxes, shadow_rect *rects) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const shadow_job &s = sj[i];
+    int ext_w = s.W + 2 * s.border, ext_h = s.H + 2 * s.border;
+    int left = ext_w, right = 0, top = ext_h, bottom = 0;
+    cover_box b = boxes[s.job];
+    if (b.x0 <= b.x1) {
+        left = min(left, b.x0); right = max(right, b.x1);
+        top = min(top, b.y0); bottom = max(bottom, b.y1);
+    }
+    if (b.first_key != 0x7fffffffffffffffll) {
+        int fx = static_cast<int>(b.first_key & 0xffffffffll), fy = static_cast<int>(b.first_key >> 32);
+        left = min(left, fx); right = max(right, fx);
+        top = min(top, fy); bottom = max(bottom, fy);
+    }
+    left = max(left - s.border, 0);
+    right = min(right + s.border, ext_w) + 1;
+    top = max(top - s.border, 0);
+    bottom = min(bottom + s.border, ext_h);
+    shadow_rect r;
+    r.left = left; r.right = right; r.top = top; r.bottom = bottom;
+    r.width = max(right - left, 0);
+    r.height = max(bottom - top, 0);
+    rects[s.cmd] = r;
+}
+
+// Raster: blockIdx.y selects the shadow, warps cover its working rows.
+__global__ void k_shadow_raster_all(const shadow_job *sj, const command *cmds, paint_src src, row_view rv,
+                                    const shadow_rect *rects, float *imgs) {
+    const shadow_job &s = sj[blockIdx.y];
+    const command &c = cmds[s.cmd];
+    const shadow_rect rc = rects[s.cmd];
+    int lane = threadIdx.x & 31;
+    int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    float *out = imgs + s.img;
+    for (int y = rc.top + wid; y < rc.bottom; y += nw) {
+        int row = s.row_base + y;
+        int n = rv.row_len[row];
+        const run *r = rv.runs + rv.row_off[row];
+        const float *sm = rv.sums + rv.row_off[row];
+        int first = n ? r[0].x : 0x7fffffff, last = n ? r[n - 1].x : -1;
+        for (int x = rc.left + lane; x < rc.right; x += 32) {
+            float val = 0.0f;
+            if (x >= first && x <= last) {
+                float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+                if (cov >= kVisible) {
+                    float pxx = (static_cast<float>(x) + 0.5f) - c.sh_offx;
+                    float pyy = (static_cast<float>(y) + 0.5f) - c.sh_offy;
+                    val = cov * paint_at(c, src, pxx, pyy).w;
+                }
+            }
+            out[static_cast<size_t>(y - rc.top) * rc.width + (x - rc.left)] = val;
+        }
+    }
+}
+
+// Exact running-sum blur (hpp:2453-2503), rows then columns, batched over
+// shadows through blockIdx.y.  `scratch` has one image-sized area per shadow.
+__global__ void k_blur_rows_all(const shadow_job *sj, const shadow_rect *rects, float *imgs, float *scratch) {
+    const shadow_job &s = sj[blockIdx.y];
+    const shadow_rect rc = rects[s.cmd];
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= rc.height) return;
+    size_t width = rc.width, r = s.radius;
+    float *row = imgs + s.img + static_cast<size_t>(y) * width;
+    float *t = scratch + s.img + static_cast<size_t>(y) * width;
+    float w1 = s.w1, w2 = s.w2;
+    for (int pass = 0; pass < 3; ++pass) {
+        for (size_t x = 0; x < width; ++x) t[x] = row[x];
+        float acc = r + 1 < width ? w1 * t[r + 1] : 0.0f;
+        for (size_t x = 0; x <= r && x < width; ++x) acc += (w1 + w2) * t[x];
+        row[0] = acc;
+        for (size_t x = 1; x < width; ++x) {
+            if (x >= r + 1) acc -= w2 * t[x - r - 1];
+            if (x >= r + 2) acc -= w1 * t[x - r - 2];
+            if (x + r < width) acc += w2 * t[x + r];
+            if (x + r + 1 < width) acc += w1 * t[x + r + 1];
+            row[x] = acc;
+        }
+    }
+}
+
+__global__ void k_blur_cols_all(const shadow_job *sj, const shadow_rect *rects, float *imgs, float *scratch) {
+    const shadow_job &s = sj[blockIdx.y];
+    const shadow_rect rc = rects[s.cmd];
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= rc.width) return;
+    size_t width = rc.width, height = rc.height, r = s.radius;
+    float *img = imgs + s.img;
+    float *tmp = scratch + s.img;
+    float w1 = s.w1, w2 = s.w2;
+    for (int pass = 0; pass < 3; ++pass) {
+        for (size_t y = 0; y < height; ++y) tmp[y * width + x] = img[y * width + x];
+        float acc = r + 1 < height ? w1 * tmp[(r + 1) * width + x] : 0.0f;
+        for (size_t y = 0; y <= r && y < height; ++y) acc += (w1 + w2) * tmp[y * width + x];
+        if (height > 0) img[x] = acc;
+        for (size_t y = 1; y < height; ++y) {
+            if (y >= r + 1) acc -= w2 * tmp[(y - r - 1) * width + x];
+            if (y >= r + 2) acc -= w1 * tmp[(y - r - 2) * width + x];
+            if (y + r < height) acc += w2 * tmp[(y + r) * width + x];
+            if (y + r + 1 < height) acc += w1 * tmp[(y + r + 1) * width + x];
+            img[y * width + x] = acc;
+        }
+    }
+}
+
+}  // namespace cyg
+
+#endif

@@ -78,3 +78,110 @@ def replay_linear(trace: bytes, width: int, height: int) -> np.ndarray:
     if rc != 0:
         raise RuntimeError(f"cy_replay_linear failed with status {rc}")
     return out
+
+
+# ------------------------------------------------------------ batched frames
+def _batch_lib() -> ctypes.CDLL:
+    lib = load()
+    if getattr(lib, "_batch_ready", False):
+        return lib
+    vp, c_int_p, c_size_p = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_size_t)
+    lib.cy_canvas_from_trace.restype = vp
+    lib.cy_canvas_from_trace.argtypes = [vp, ctypes.c_size_t, c_int_p]
+    lib.cy_canvas_ctx.restype = vp
+    lib.cy_canvas_ctx.argtypes = [vp]
+    lib.cy_canvas_delete.restype = None
+    lib.cy_canvas_delete.argtypes = [vp]
+    lib.cy_frame_create.restype = ctypes.c_int
+    lib.cy_frame_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+    for name in ("cy_frame_run", "cy_frame_sync", "cy_frame_finish"):
+        getattr(lib, name).restype = ctypes.c_int
+        getattr(lib, name).argtypes = [vp]
+    lib.cy_frame_destroy.restype = None
+    lib.cy_frame_destroy.argtypes = [vp]
+    lib.cy_frame_stream.restype = vp
+    lib.cy_frame_stream.argtypes = [vp]
+    lib.cy_ctx_take_reads.restype = ctypes.c_int
+    lib.cy_ctx_take_reads.argtypes = [vp, vp, ctypes.c_size_t, c_size_p]
+    lib.cy_set_strip_config.restype = None
+    lib.cy_set_strip_config.argtypes = [ctypes.c_int, ctypes.c_int]
+    lib._batch_ready = True
+    return lib
+
+
+def set_strip_config(strip_pixels: int, threads: int) -> None:
+    _batch_lib().cy_set_strip_config(int(strip_pixels), int(threads))
+
+
+class Frame:
+    """Many canvases rendered together: each call list is replayed on the
+    host into a canvas whose reads are deferred, then one frame renders all
+    of them (engine 0: persistent strip kernel; 1: per-draw launches)."""
+
+    def __init__(self, traces, engine: int = 0):
+        self.lib = _batch_lib()
+        self.canvases = []
+        self.frame = ctypes.c_void_p()
+        try:
+            for t in traces:
+                st = ctypes.c_int(0)
+                c = self.lib.cy_canvas_from_trace(t, len(t), ctypes.byref(st))
+                if not c:
+                    raise RuntimeError(f"replay into a deferred canvas failed with status {st.value}")
+                self.canvases.append(c)
+            ctxs = (ctypes.c_void_p * len(self.canvases))(*[self.lib.cy_canvas_ctx(c) for c in self.canvases])
+            rc = self.lib.cy_frame_create(ctxs, len(self.canvases), int(engine), ctypes.byref(self.frame))
+            if rc != 0:
+                raise RuntimeError(f"cy_frame_create failed with status {rc}")
+            self.ctxs = [ctxs[i] for i in range(len(self.canvases))]
+        except Exception:
+            self.close()
+            raise
+
+    def run(self) -> None:
+        rc = self.lib.cy_frame_run(self.frame)
+        if rc != 0:
+            raise RuntimeError(f"cy_frame_run failed with status {rc}")
+
+    def sync(self) -> None:
+        rc = self.lib.cy_frame_sync(self.frame)
+        if rc != 0:
+            raise RuntimeError(f"cy_frame_sync failed with status {rc}")
+
+    def stream(self) -> int:
+        return int(self.lib.cy_frame_stream(self.frame) or 0)
+
+    def finish(self) -> List[bytes]:
+        rc = self.lib.cy_frame_finish(self.frame)
+        if rc != 0:
+            raise RuntimeError(f"cy_frame_finish failed with status {rc}")
+        out = []
+        for ctx in self.ctxs:
+            n = ctypes.c_size_t(0)
+            self.lib.cy_ctx_take_reads(ctx, None, 0, ctypes.byref(n))
+            buf = ctypes.create_string_buffer(max(n.value, 1))
+            rc = self.lib.cy_ctx_take_reads(ctx, buf, n.value, ctypes.byref(n))
+            if rc != 0:
+                raise RuntimeError(f"cy_ctx_take_reads failed with status {rc}")
+            out.append(buf.raw[: n.value])
+        return out
+
+    def close(self) -> None:
+        if self.frame:
+            self.lib.cy_frame_destroy(self.frame)
+            self.frame = ctypes.c_void_p()
+        for c in self.canvases:
+            self.lib.cy_canvas_delete(c)
+        self.canvases = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def render_batch(traces, engine: int = 0) -> List[bytes]:
+    """Render call lists together; returns each one's get_image_data bytes."""
+    with Frame(traces, engine) as f:
+        return f.finish()

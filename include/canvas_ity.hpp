@@ -147,6 +147,11 @@ public:
     // Returns 0 or a negative status.  Used to check coverage exactly.
     int read_linear( float *rgba );
 
+    // Extension, no reference counterpart: the GPU context (cy_ctx in
+    // cy_gpu.h) holding this canvas's queued work, for batched rendering of
+    // many canvases in one frame (cy_batch.h).
+    void *gpu_context() const;
+
 private:
     detail::canvas_state *self;
     void sync_public_state();

@@ -94,6 +94,12 @@ int cy_replay(const void *trace, size_t trace_len, void *images, size_t images_c
 int cy_replay_linear(const void *trace, size_t trace_len, float *out, size_t out_floats, int *width,
                      int *height);
 
+/* Batched rendering helpers (cy_batch.h): replay a call list into a new
+ * canvas whose reads are deferred (nothing runs on the GPU yet), and get
+ * its engine context to put into a frame. */
+cy_canvas *cy_canvas_from_trace(const void *trace, size_t trace_len, int *status);
+void *cy_canvas_ctx(cy_canvas *c);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,61 @@
+/*
+ * cy_batch.h -- batched many-canvas rendering and engine controls.
+ *
+ * No reference counterpart: the reference renders one canvas at a time on
+ * the calling thread.  A frame renders the queued work of many canvases in
+ * one set of launches; with the tile engine (0) all pixel work happens in
+ * one persistent kernel that keeps each strip of a canvas in shared memory
+ * across all of its draws.  Contexts made while deferred mode is on queue
+ * their get_image_data reads instead of flushing; the results are collected
+ * with cy_ctx_take_reads after the frame finishes.
+ */
+#ifndef CY_BATCH_H
+#define CY_BATCH_H
+
+#include <stddef.h>
+
+#include "cy_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cy_frame cy_frame;
+
+/* Contexts created afterwards in this thread queue their reads (1) or
+ * flush on every read as the reference API requires (0, default). */
+void cy_set_deferred(int deferred);
+
+/* Tile engine strip size in pixels (256..12288, shared memory is 16 B per
+ * pixel) and threads per block (128, 256 or 512). */
+void cy_set_strip_config(int strip_pixels, int threads);
+
+/* Build a frame over the queued work of n contexts, upload it and run it
+ * once.  engine: 0 tile, 1 plain.  The contexts' queues are consumed by
+ * cy_frame_finish. */
+int cy_frame_create(cy_ctx *const *ctxs, int n, int engine, cy_frame **out);
+
+/* Run the prepared frame again on the device (asynchronous, no host
+ * synchronisation); for timing. */
+int cy_frame_run(cy_frame *frame);
+
+/* Wait for the frame's stream. */
+int cy_frame_sync(cy_frame *frame);
+
+/* The frame's CUDA stream (cudaStream_t), for event timing. */
+void *cy_frame_stream(cy_frame *frame);
+
+/* Copy the reads out, release queued resources. */
+int cy_frame_finish(cy_frame *frame);
+
+void cy_frame_destroy(cy_frame *frame);
+
+/* Deferred reads of a context, concatenated in call order (compact RGBA8
+ * rectangles); -2 if cap is too small (*len holds the size). */
+int cy_ctx_take_reads(cy_ctx *ctx, unsigned char *out, size_t cap, size_t *len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CY_BATCH_H */

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 MAX_LSB = 1
 MIN_IDENTICAL = 0.995
 COVERAGE_TOL = 1e-5
-ENGINES = {"plain": 1}
+ENGINES = {"tile": 0, "plain": 1}
 MANIFEST = G.manifest()
 
 
@@ -138,3 +138,32 @@ def test_one_by_one_and_large_canvas(engine):
         got = G.split_images(tb, native.replay(tb)[0])[-1]
         want = G.split_images(tb, oracle.replay(tb)[0])[-1]
         assert_images_close(got, want, f"{w}x{h}")
+
+
+@pytest.mark.parametrize("engine_id", [0, 1], ids=["tile", "plain"])
+def test_batched_frame_matches_oracle(engine_id):
+    """Many canvases of mixed sizes rendered in one frame: each result equals
+    the oracle's, i.e. the same as when rendered alone."""
+    traces = [scenes.small_scene(cfg, s) for s in range(3)
+              for cfg in ("c0_small", "c1_small", "c2_small", "mixed_small")]
+    traces += [G.load_fixture(e) for e in MANIFEST[::7]]
+    outs = native.render_batch(traces, engine_id)
+    for tb, raw in zip(traces, outs):
+        got = G.split_images(tb, raw)
+        want = G.split_images(tb, oracle.replay(tb)[0])
+        for g, w in zip(got, want):
+            assert_images_close(g, w, "batched")
+
+
+@pytest.mark.parametrize("strip_pixels", [1024, 4096, 8192])
+def test_tile_engine_strip_sizes(strip_pixels):
+    native.set_strip_config(strip_pixels, 256)
+    try:
+        traces = [scenes.small_scene("mixed_small", s) for s in range(4)]
+        outs = native.render_batch(traces, 0)
+        for tb, raw in zip(traces, outs):
+            got = G.split_images(tb, raw)[-1]
+            want = G.split_images(tb, oracle.replay(tb)[0])[-1]
+            assert_images_close(got, want, f"strip {strip_pixels}")
+    finally:
+        native.set_strip_config(4096, 256)
