@@ -1,0 +1,403 @@
+"""Benchmark: batched many-canvas rendering on one GB300.
+
+Workload (default): 4096 independent canvases, each side log-uniform in
+[64, 1024] px, 8-128 paths per canvas from the c0/c1/c2 mixture (60/30/10),
+seeded synthetic call lists (canvas_ity_gb300.scenes.c3).  A step renders
+the whole batch.
+
+* value: Mpix/s of the batched tile engine with the batch already uploaded
+  (device time of K runs of the prepared frame, CUDA events on its stream);
+* e2e: the same through the public C ABI with host buffers: call lists on the
+  host are replayed into canvases (path building, stroke expansion), the
+  frame is uploaded, rendered and read back as RGBA8, every step;
+* plain: Mpix/s of the per-canvas plain engine (per-draw launches over each
+  canvas's float bitmap), over a sample of the same canvases;
+* cpu_baseline: the CPU oracle on the host cores on a sample of canvases;
+* roofline: the dominant kernel's algorithmic bytes / its measured time.
+
+`--impl reference` times the CPU implementation of the path (the reference
+build where it exists, else the CPU oracle) on all host cores.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "Mpix/s batched vs plain per-canvas on 1 GB300 at +/-1 LSB; serving p50/p99 ms"
+WORKLOAD = ("c3: 4096 canvases, sides log-uniform 64-1024 px, 8-128 paths each from the "
+            "c0/c1/c2 mixture 60/30/10 (fills, strokes, gradients, patterns, 11 ops, shadows, clips)")
+
+
+def _gen_chunk(args):
+    first, count, base = args
+    from canvas_ity_gb300 import scenes
+    return [scenes.c3_canvas(i, base) for i in range(first, first + count)]
+
+
+def generate(count, base_seed, workers):
+    """Seeded call lists, generated in a spawn pool (before any GPU use)."""
+    import multiprocessing as mp
+    chunk = max(1, count // (workers * 4))
+    jobs = [(i, min(chunk, count - i), base_seed) for i in range(0, count, chunk)]
+    if workers <= 1:
+        return [t for j in jobs for t in _gen_chunk(j)]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        parts = pool.map(_gen_chunk, jobs)
+    return [t for p in parts for t in p]
+
+
+def pixels_of(traces):
+    from canvas_ity_gb300 import trace as T
+    total = 0
+    for t in traces:
+        w, h = T.canvas_size(t)
+        total += w * h
+    return total
+
+
+def cpu_render(traces, threads):
+    """Render call lists with the CPU implementation on `threads` threads;
+    returns (seconds, kind)."""
+    import oracle
+    kind = "port"
+    fn = oracle.replay
+    if oracle.reference_available():
+        kind, fn = "reference", oracle.reference_replay
+    fn(traces[0])  # load the library outside the timed region
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(fn, traces))
+    return time.perf_counter() - t0, kind
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per unit of work of a kernel from the committed ncu summary."""
+    path = os.path.join(HERE, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(value, world, backend):
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if backend == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(value, world, backend):
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if backend == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reference_arm(args, world, rank):
+    """CPU implementation of the path on all host cores, same metric/config."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        if rank != 0:
+            dist.barrier()
+            dist.destroy_process_group()
+            return
+    cores = os.cpu_count() or 1
+    traces = generate(args.ref_sample, args.seed, min(cores, 16))
+    px = pixels_of(traces)
+    for _ in range(args.warmup):
+        cpu_render(traces[: max(1, len(traces) // 8)], cores)
+    t_total, kind = 0.0, "port"
+    for _ in range(args.steps):
+        t, kind = cpu_render(traces, cores)
+        t_total += t
+    value = px * args.steps / t_total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mpix/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(t_total / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_canvases": len(traces), "sample_pixels": px},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mpix/s", "cores": cores, "kind": kind,
+                         "sample": f"first {len(traces)} canvases of the c3 batch ({px} px) per step"},
+        "e2e": {"value": round(value, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def gpu_arm(args, world, rank, local):
+    import numpy as np
+
+    cores = os.cpu_count() or 1
+    base_seed = args.seed + 100003 * rank
+    t_gen = time.perf_counter()
+    traces = generate(args.canvases, base_seed, min(cores, 16))
+    gen_s = time.perf_counter() - t_gen
+    # CPU baseline on a bounded sample (rank 0 only), before the GPU is used.
+    cpu = None
+    if rank == 0 and args.cpu_sample > 0:
+        sample = traces[: args.cpu_sample]
+        t, kind = cpu_render(sample, cores)
+        spx = pixels_of(sample)
+        cpu = {"value": round(spx / t / 1e6, 3), "unit": "Mpix/s", "cores": cores, "kind": kind,
+               "sample": f"first {len(sample)} canvases of the batch ({spx} px), one render per thread, "
+                         f"{t:.1f} s"}
+    import torch
+    torch.cuda.set_device(local)
+    backend = "nccl"
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend, device_id=torch.device("cuda", local))
+    from canvas_ity_gb300 import native, build
+    build.build()
+    if args.strip_pixels:
+        native.set_strip_config(args.strip_pixels, args.strip_threads)
+    px = pixels_of(traces)
+    # Parity spot check: a few canvases against the CPU oracle.
+    import oracle
+    check = traces[:: max(1, len(traces) // args.parity_sample)][: args.parity_sample]
+    outs = native.render_batch(check, 0)
+    worst, diff_frac = 0, 0.0
+    for tb, raw in zip(check, outs):
+        a = np.frombuffer(raw, np.uint8)
+        b = np.frombuffer(oracle.replay(tb)[0], np.uint8)
+        d = np.abs(a.astype(np.int16) - b.astype(np.int16)).reshape(-1, 4)
+        worst = max(worst, int(d.max(initial=0)))
+        diff_frac = max(diff_frac, float(np.any(d != 0, axis=1).mean()))
+    # Prepared frame: device-resident inputs.
+    frame = native.Frame(traces, 0)
+    stats = frame.stats()
+    stream = torch.cuda.ExternalStream(frame.stream())
+    for _ in range(max(args.warmup, 3)):
+        frame.run()
+    frame.sync()
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            frame.run()
+        stop.record(stream)
+        stop.synchronize()
+        elapsed_ms = start.elapsed_time(stop)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_max = reduce_max(elapsed_ms / 1e3, world, backend)
+    px_all = reduce_sum(float(px), world, backend)
+    value = px_all * args.steps / t_max / 1e6
+    # Phase profile of one run (CUDA events on the frame's stream).
+    frame.set_profiling(True)
+    frame.run()
+    phases = frame.profile()
+    frame.set_profiling(False)
+    frame.finish()
+    frame.close()
+    # End to end through the public C ABI, host buffers, every step.
+    t_e2e = 0.0
+    h2d = d2h = 0
+    for i in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        f = native.Frame(traces, 0)
+        st = f.stats()
+        outs = f.finish()
+        f.close()
+        t_e2e += time.perf_counter() - t0
+        h2d, d2h = st["upload_bytes"], sum(len(o) for o in outs)
+    e2e_s = reduce_max(t_e2e / max(args.e2e_steps, 1), world, backend)
+    e2e = px_all / e2e_s / 1e6 if e2e_s > 0 else None
+    # Plain per-canvas path on a sample of the same canvases.
+    sample = traces[: args.plain_sample]
+    plain_ms = 0.0
+    for tb in sample:
+        f = native.Frame([tb], 1)
+        s0 = torch.cuda.ExternalStream(f.stream())
+        f.run()
+        f.sync()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s0)
+        f.run()
+        b.record(s0)
+        b.synchronize()
+        plain_ms += a.elapsed_time(b)
+        f.finish()
+        f.close()
+    plain = pixels_of(sample) / (plain_ms / 1e3) / 1e6 if plain_ms > 0 else None
+    # Roofline of the dominant kernel.
+    peak, peak_kind = measured_peaks()
+    per_run_ms = elapsed_ms / args.steps
+    strips_ms = phases.get("paint", 0.0)
+    scan_ms = phases.get("scan_convert", 0.0)
+    if strips_ms >= scan_ms:
+        kernel = "k_strips"
+        alg = 12 * stats["draw_runs"] + 8 * stats["draw_rows"] + 4 * stats["shadow_floats"] + stats["read_bytes"]
+        kms = strips_ms
+    else:
+        kernel = "k_runs+k_rows"
+        alg = 20 * stats["segments"] * 2 + 8 * stats["runs"] * 3 + 16 * stats["rows"]
+        kms = scan_ms
+    achieved = alg / (kms / 1e3) / 1e9 if kms > 0 else 0.0
+    traffic_per_px = ncu_traffic(kernel)
+    roofline = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": (round(traffic_per_px * stats["pixels"]) if traffic_per_px else None),
+                "algorithmic_bytes": alg, "kernel_ms": round(kms, 3)}
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(t_max * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "canvases": len(traces), "pixels": px, "engine": "tile",
+                   "strip_pixels": args.strip_pixels or 4096, "commands": stats["commands"],
+                   "segments": stats["segments"], "runs": stats["runs"], "shadows": stats["shadows"],
+                   "clips": stats["clips"], "l2": "inputs larger than L2 (runs and outputs are GBs)",
+                   "parallelism": f"replicas x{world}", "generate_s": round(gen_s, 1)},
+        "e2e": {"value": round(e2e, 2) if e2e else None, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "plain_per_canvas": {"value": round(plain, 2) if plain else None, "unit": "Mpix/s",
+                             "sample_canvases": len(sample)},
+        "batched_over_plain": round(value / plain, 2) if plain else None,
+        "phases_ms": {k: round(v, 3) for k, v in phases.items()},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "parity": {"canvases": len(check), "max_lsb": worst, "max_frac_pixels_differing": round(diff_frac, 6)},
+        "clocks": clocks.summary(),
+        "gpu_launches": stats["launches"] * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--canvases", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--cpu-sample", type=int, default=128)
+    ap.add_argument("--ref-sample", type=int, default=64)
+    ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--parity-sample", type=int, default=8)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--strip-pixels", type=int, default=0)
+    ap.add_argument("--strip-threads", type=int, default=256)
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        gpu_arm(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -169,12 +169,10 @@ __device__ __forceinline__ int crossings_before(const dda_piece &p, float e) {
     return c < 0 ? 0 : c;
 }
 
-// Emit the signed-area deltas of row k of the piece through `emit(x, y, d)`.
-template <class Emit>
-__device__ __forceinline__ void dda_row(const dda_piece &p, int k, Emit &emit) {
-    float2 entry = k == 0 ? f2(p.fx, p.fy) : dda_exit(p, k - 1);
-    float2 ex = dda_exit(p, k);
-    int ps, pe;
+// Cell range of row k: the reference's pixel.x at the start of the row (ps)
+// and at its end (pe); the row emits cells ps..pe+1.  `entry` is the row's
+// entry point (the previous row's exit), `ex` its exit point.
+__device__ __forceinline__ void dda_span(const dda_piece &p, int k, float2 entry, float2 ex, int &ps, int &pe) {
     if (!p.vert) {
         int before = k == 0 ? 0 : crossings_before(p, entry.x);
         int upto = crossings_before(p, ex.x);
@@ -186,7 +184,16 @@ __device__ __forceinline__ void dda_row(const dda_piece &p, int k, Emit &emit) {
         ps = static_cast<int>(p.px0) + (consumed_before ? 1 : 0);
         pe = ps + (consumed_now ? 1 : 0);
     }
-    int row = static_cast<int>(p.py0) + (p.up ? k : -k);
+}
+
+__device__ __forceinline__ int dda_row_index(const dda_piece &p, int k) {
+    return static_cast<int>(p.py0) + (p.up ? k : -k);
+}
+
+// Emit the signed-area deltas of row k (cells ps..pe+1, in order) through
+// `emit(x, d)`: the body of add_runs' row loop (hpp:2131-2169).
+template <class Emit>
+__device__ __forceinline__ void dda_cells(const dda_piece &p, float2 entry, float2 ex, int ps, int pe, Emit &emit) {
     float2 now = entry;
     float carry = 0.0f;
     for (int m = ps; m < pe; ++m) {
@@ -200,15 +207,27 @@ __device__ __forceinline__ void dda_row(const dda_piece &p, int k, Emit &emit) {
         float strip = lo(hi((X.y - now.y) * p.ystep, 0.0f), 1.0f);
         float mid = (X.x + now.x) * 0.5f;
         float area = (mid - static_cast<float>(m)) * strip;
-        emit(m, row, (carry + strip - area) * p.sign);
+        emit(m, (carry + strip - area) * p.sign);
         carry = area;
         now = X;
     }
     float strip = lo(hi((ex.y - now.y) * p.ystep, 0.0f), 1.0f);
     float mid = (ex.x + now.x) * 0.5f;
     float area = (mid - static_cast<float>(pe)) * strip;
-    emit(pe, row, (carry + strip - area) * p.sign);
-    emit(pe + 1, row, area * p.sign);
+    emit(pe, (carry + strip - area) * p.sign);
+    emit(pe + 1, area * p.sign);
+}
+
+// Emit row k of the piece through `emit(x, y, d)` (used by host-side checks).
+template <class Emit>
+__device__ __forceinline__ void dda_row(const dda_piece &p, int k, Emit &emit) {
+    float2 entry = k == 0 ? f2(p.fx, p.fy) : dda_exit(p, k - 1);
+    float2 ex = dda_exit(p, k);
+    int ps, pe;
+    dda_span(p, k, entry, ex, ps, pe);
+    int row = dda_row_index(p, k);
+    auto e2 = [&](int x, float d) { emit(x, row, d); };
+    dda_cells(p, entry, ex, ps, pe, e2);
 }
 
 // Clip one polyline segment to [0,width] x [0,height] the way the

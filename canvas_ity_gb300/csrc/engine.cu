@@ -191,6 +191,14 @@ struct frame {
     char *d = nullptr;
     size_t o_cmd = 0, o_hpts = 0, o_hprev = 0, o_bez = 0, o_items = 0, o_soff = 0, o_scol = 0, o_tex = 0, o_put = 0;
     bool sized = false;        // run store and masks sized by the first run
+    int64_t n_runs = 0, main_runs = 0, main_rows = 0, h2d_bytes = 0;
+    int launches = 0;          // kernel launches of the last run
+    bool profiling = false;
+    cudaEvent_t ev[8] = {};
+    int n_ev = 0;
+    void mark() {
+        if (profiling && n_ev < 8) cudaEventRecord(ev[n_ev++], stream);
+    }
     bool ext_built = false;
     bool strips_built = false;
 
@@ -214,9 +222,11 @@ struct frame {
         total_rows = total_segs = 0;
         n_items = 0;
         sized = ext_built = strips_built = false;
+        n_runs = main_runs = main_rows = h2d_bytes = 0;
     }
 
     ~frame() {
+        for (cudaEvent_t e : ev) if (e) cudaEventDestroy(e);
         dbuf *b[] = {&arena, &flat_pts, &flat_prev, &item_cnt, &item_off, &pat_f4, &jobs_dev, &boxes, &row_cnt,
                      &row_off, &row_cur, &row_len, &runs, &sums, &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev};
@@ -239,6 +249,7 @@ struct frame {
         return false;
     }
     int scan(const int32_t *in, int32_t *out, int n);
+    int scan64(const int32_t *in, int64_t *out, int n);
     void gather();
     int prepare();
     int run();
@@ -260,6 +271,35 @@ int frame::scan(const int32_t *in, int32_t *out, int n) {
     k_scan_tiles<<<tiles, 1024, 0, stream>>>(in, out, n, sums_p);
     int rc = scan(sums_p, offs_p, tiles);
     if (rc == CY_OK) k_scan_add<<<(n + 255) / 256, 256, 0, stream>>>(out, n, offs_p);
+    cudaFreeAsync(sums_p, stream);
+    cudaFreeAsync(offs_p, stream);
+    if (rc == CY_OK && !ok(cudaGetLastError())) rc = status;
+    return rc;
+}
+
+int frame::scan64(const int32_t *in, int64_t *out, int n) {
+    // Exclusive scan of int32 counts into int64 offsets.
+    int tiles = (n + 4095) / 4096;
+    if (tiles <= 0) return CY_OK;
+    if (tiles == 1) {
+        k_scan_tiles64<int32_t><<<1, 1024, 0, stream>>>(in, out, n, nullptr);
+        return ok(cudaGetLastError()) ? CY_OK : status;
+    }
+    int64_t *sums_p = nullptr, *offs_p = nullptr;
+    if (!ok(cudaMallocAsync(reinterpret_cast<void **>(&sums_p), static_cast<size_t>(tiles) * 8, stream)) ||
+        !ok(cudaMallocAsync(reinterpret_cast<void **>(&offs_p), static_cast<size_t>(tiles) * 8, stream)))
+        return status;
+    k_scan_tiles64<int32_t><<<tiles, 1024, 0, stream>>>(in, out, n, sums_p);
+    // Tile sums are int64: scan them with the same kernel on int64 input.
+    int rc = CY_OK;
+    int t2 = (tiles + 4095) / 4096;
+    if (t2 == 1) {
+        k_scan_tiles64<int64_t><<<1, 1024, 0, stream>>>(sums_p, offs_p, tiles, nullptr);
+    } else {
+        // Beyond 16.7M tiles (6.9e10 entries) is not supported.
+        rc = fail(CY_ENOMEM);
+    }
+    if (rc == CY_OK) k_scan_add64<<<(n + 255) / 256, 256, 0, stream>>>(out, n, offs_p);
     cudaFreeAsync(sums_p, stream);
     cudaFreeAsync(offs_p, stream);
     if (rc == CY_OK && !ok(cudaGetLastError())) rc = status;
@@ -342,6 +382,7 @@ int frame::prepare() {
     d = static_cast<char *>(arena.p);
     if (total > o_hpts && !ok(cudaMemcpyAsync(d + o_hpts, h + o_hpts, total - o_hpts, cudaMemcpyHostToDevice, stream)))
         return status;
+    h2d_bytes = static_cast<int64_t>(total);
     if (!lut_dev.ensure(256 * sizeof(float))) return fail(CY_ENOMEM);
     if (!ok(cudaMemcpyAsync(lut_dev.p, linear_lut_host(), 256 * sizeof(float), cudaMemcpyHostToDevice, stream)))
         return status;
@@ -422,6 +463,7 @@ int frame::prepare() {
             int ew = W + 2 * b, eh = H + 2 * b;
             shadow_job[i] = add_job(c, eh, ew + 2, static_cast<float>(ew), static_cast<float>(eh), c.sh_offx,
                                     c.sh_offy);
+            jobs[shadow_job[i]].need_box = 1;
             cyg::shadow_job s;
             std::memset(&s, 0, sizeof(s));
             s.cmd = static_cast<int32_t>(i);
@@ -439,6 +481,7 @@ int frame::prepare() {
         }
         if (c.kind == CMD_FILL || c.kind == CMD_CLIP)
             main_job[i] = add_job(c, H, W + 2, static_cast<float>(W), static_cast<float>(H), 0.0f, 0.0f);
+        if (c.kind == CMD_CLIP) jobs[main_job[i]].need_box = 1;
         if (c.kind == CMD_CLIP) {
             int lv = level_of_cv[cmd_cv[i]]++;
             clips.push_back(clip_op{static_cast<int>(i), cmd_cv[i], all.mask_ids[2 * i], all.mask_ids[2 * i + 1], lv});
@@ -449,8 +492,8 @@ int frame::prepare() {
     size_t nr = static_cast<size_t>(total_rows);
     if (!jobs.empty()) {
         if (!jobs_dev.ensure(jobs.size() * sizeof(scan_job)) || !row_cnt.ensure((nr + 1) * 4) ||
-            !row_off.ensure((nr + 2) * 4) || !row_cur.ensure((nr + 1) * 4) || !row_len.ensure((nr + 1) * 4) ||
-            !boxes.ensure(jobs.size() * sizeof(cover_box)) || !rowoff_host.ensure((nr + 1) * 4))
+            !row_off.ensure((nr + 2) * 8) || !row_cur.ensure((nr + 1) * 4) || !row_len.ensure((nr + 1) * 4) ||
+            !boxes.ensure(jobs.size() * sizeof(cover_box)) || !rowoff_host.ensure((nr + 1) * 8))
             return fail(CY_ENOMEM);
         if (!ok(cudaMemcpyAsync(jobs_dev.p, jobs.data(), jobs.size() * sizeof(scan_job), cudaMemcpyHostToDevice,
                                 stream)) ||
@@ -477,6 +520,9 @@ int frame::prepare() {
 
 int frame::run() {
     if (status) return status;
+    n_ev = 0;
+    launches = 0;
+    mark();   // 0: start
     std::vector<command> &cmds = all.cmds;
     const float2 *d_hpts = reinterpret_cast<const float2 *>(d + o_hpts);
     const int32_t *d_hprev = reinterpret_cast<const int32_t *>(d + o_hprev);
@@ -503,10 +549,13 @@ int frame::run() {
                                                                     item_off.as<int32_t>(), flat_pts.as<float2>(),
                                                                     flat_prev.as<int32_t>(), nflat);
     }
+    if (!all.texels.empty()) ++launches;
+    if (n_items_flat > 0) ++launches;
+    mark();   // 1: patterns and flattening done
     size_t nr = static_cast<size_t>(total_rows);
     int n_jobs = static_cast<int>(jobs.size());
     row_view rv;
-    rv.row_off = row_off.as<int32_t>();
+    rv.row_off = row_off.as<int64_t>();
     rv.row_len = row_len.as<int32_t>();
     rv.runs = runs.as<cyg::run>();
     rv.sums = sums.as<float>();
@@ -524,19 +573,26 @@ int frame::run() {
         t.row_cnt = row_cnt.as<int32_t>();
         t.row_cur = row_cur.as<int32_t>();
         int segs = static_cast<int>(total_segs);
-        int grid = std::max(1, std::min((segs + 7) / 8, 152 * 32));
-        if (segs > 0) k_runs<false><<<grid, 256, 0, stream>>>(t, segs);
-        int rc = scan(row_cnt.as<int32_t>(), row_off.as<int32_t>(), static_cast<int>(nr) + 1);
+        int grid = std::max(1, std::min((segs + 127) / 128, 152 * 64));
+        if (segs > 0) k_runs<false><<<grid, 128, 0, stream>>>(t, segs);
+        int rc = scan64(row_cnt.as<int32_t>(), row_off.as<int64_t>(), static_cast<int>(nr) + 1);
         if (rc) return rc;
         if (!sized) {
             sized = true;
             // First run: size the run store and the new clip masks from the counts.
-            if (!ok(cudaMemcpyAsync(rowoff_host.p, row_off.p, (nr + 1) * 4, cudaMemcpyDeviceToHost, stream)) ||
+            if (!ok(cudaMemcpyAsync(rowoff_host.p, row_off.p, (nr + 1) * 8, cudaMemcpyDeviceToHost, stream)) ||
                 !ok(cudaStreamSynchronize(stream)))
                 return status;
-            const int32_t *rowoff_h = static_cast<const int32_t *>(rowoff_host.p);
+            const int64_t *rowoff_h = static_cast<const int64_t *>(rowoff_host.p);
             int64_t nruns = rowoff_h[nr];
             if (nruns < 0) return fail(CY_ENOMEM);
+            n_runs = nruns;
+            for (size_t i = 0; i < cmds.size(); ++i) {
+                if (cmds[i].kind != CMD_FILL || main_job[i] < 0) continue;
+                const scan_job &mj = jobs[main_job[i]];
+                main_runs += rowoff_h[mj.row_base + mj.rows] - rowoff_h[mj.row_base];
+                main_rows += mj.rows;
+            }
             if (!runs.ensure(static_cast<size_t>(nruns + 1) * sizeof(cyg::run)) ||
                 !sums.ensure(static_cast<size_t>(nruns + 1) * sizeof(float)))
                 return fail(CY_ENOMEM);
@@ -555,14 +611,17 @@ int frame::run() {
                     return status;
             }
         }
-        t.row_off = row_off.as<int32_t>();
+        t.row_off = row_off.as<int64_t>();
         t.runs = runs.as<cyg::run>();
-        if (segs > 0) k_runs<true><<<grid, 256, 0, stream>>>(t, segs);
-        k_rows<<<static_cast<int>((nr + 127) / 128), 128, 0, stream>>>(
-            row_off.as<int32_t>(), row_cnt.as<int32_t>(), row_cur.as<int32_t>(), row_len.as<int32_t>(),
+        if (segs > 0) k_runs<true><<<grid, 128, 0, stream>>>(t, segs);
+        int rgrid = static_cast<int>(std::min<size_t>((nr + kRowsWarps - 1) / kRowsWarps, 152 * 64));
+        k_rows<<<std::max(rgrid, 1), kRowsWarps * 32, 0, stream>>>(
+            row_off.as<int64_t>(), row_cnt.as<int32_t>(), row_cur.as<int32_t>(), row_len.as<int32_t>(),
             runs.as<cyg::run>(), sums.as<float>(), static_cast<int>(nr));
         if (!ok(cudaGetLastError())) return status;
+        launches += (segs > 0 ? 2 : 0) + 2 + (nr + 1 > 4096 ? 3 : 1);
     }
+    mark();   // 2: scan conversion done
     // Clip masks, level by level (a clip depends on the previous mask).
     for (int lv = 0; lv <= max_level; ++lv) {
         for (const clip_op &op : clips) {
@@ -572,14 +631,14 @@ int frame::run() {
             mask_slot &nm = cv->masks[op.out_id];
             const mask_slot *om = op.in_id > 0 ? &cv->masks[op.in_id] : nullptr;
             const scan_job &j = jobs[main_job[op.cmd]];
-            k_clip_caps<<<(H + 255) / 256, 256, 0, stream>>>(row_off.as<int32_t>() + j.row_base,
+            k_clip_caps<<<(H + 255) / 256, 256, 0, stream>>>(row_off.as<int64_t>() + j.row_base,
                                                               om ? om->off : nullptr, H, nm.len);
             if (!ok(cudaMemsetAsync(nm.len + H, 0, 4, stream))) return status;
             int rc = scan(nm.len, nm.off, H + 1);
             if (rc) return rc;
             if (!ok(cudaMemsetAsync(nm.last_row, 0xff, 4, stream))) return status;
             clip_args a;
-            a.p_off = row_off.as<int32_t>();
+            a.p_off = row_off.as<int64_t>();
             a.p_len = row_len.as<int32_t>();
             a.p_runs = runs.as<cyg::run>();
             a.p_base = j.row_base;
@@ -599,6 +658,7 @@ int frame::run() {
             k_mask_fill<<<std::max(1, (H + 7) / 8), 256, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, W, H,
                                                                       nm.vis);
             if (!ok(cudaGetLastError())) return status;
+            launches += 5 + (H + 1 > 4096 ? 3 : 1);
         }
     }
     // Shadow images of every shadowed draw.
@@ -614,12 +674,19 @@ int frame::run() {
         dim3 rg(std::max(1, std::min((max_h + 7) / 8, 64)), ns);
         k_shadow_raster_all<<<rg, 256, 0, stream>>>(dsj, d_cmds, src, rv, rects.as<shadow_rect>(), sh_img.as<float>());
         dim3 bg((max_h + 127) / 128, ns), cg((max_w + 127) / 128, ns);
+        dim3 tg((max_w + 31) / 32, (max_h + 31) / 32, ns), tb(32, 8);
+        // raster (column-major) -> row blur in place -> transpose into the
+        // scratch image -> column blur in place there: the final image.
         k_blur_rows_all<<<bg, 128, 0, stream>>>(dsj, rects.as<shadow_rect>(), sh_img.as<float>(),
                                                  sh_scratch.as<float>());
-        k_blur_cols_all<<<cg, 128, 0, stream>>>(dsj, rects.as<shadow_rect>(), sh_img.as<float>(),
-                                                 sh_scratch.as<float>());
+        k_transpose_all<<<tg, tb, 0, stream>>>(dsj, rects.as<shadow_rect>(), sh_img.as<float>(),
+                                               sh_scratch.as<float>());
+        k_blur_cols_all<<<cg, 128, 0, stream>>>(dsj, rects.as<shadow_rect>(), sh_scratch.as<float>(),
+                                                 sh_img.as<float>());
         if (!ok(cudaGetLastError())) return status;
+        launches += 5;
     }
+    mark();   // 3: masks and shadows done
     if (get_total > 0 && !ok(cudaMemsetAsync(get_dev.p, 0, static_cast<size_t>(get_total), stream))) return status;
     const uint8_t *d_put = reinterpret_cast<const uint8_t *>(d + o_put);
     // Per-command extras.
@@ -656,6 +723,7 @@ int frame::run() {
             if (c.kind == CMD_PUT) {
                 dim3 blk(32, 8), grd((c.put_w + 31) / 32, (c.put_h + 7) / 8);
                 k_put<<<grd, blk, 0, stream>>>(d_cmds + i, d_put, cv->bitmap, W, H, lut);
+                ++launches;
                 continue;
             }
             if (c.kind == CMD_GET) {
@@ -663,13 +731,14 @@ int frame::run() {
                 k_get<<<grd, blk, 0, stream>>>(cv->bitmap, W, H,
                                                reinterpret_cast<uchar4 *>(get_dev.as<uint8_t>() + c.get_out),
                                                c.get_w, c.get_h, c.get_x, c.get_y);
+                ++launches;
                 continue;
             }
             if (e.has_shadow) {
                 dim3 blk(32, 8), cgrd((W + 31) / 32, (H + 7) / 8);
                 k_shadow_composite<<<cgrd, blk, 0, stream>>>(d_cmds + i, cv->bitmap, W, H, e.vis,
                                                              rects.as<shadow_rect>() + i,
-                                                             sh_img.as<float>() + e.shadow_img);
+                                                             sh_scratch.as<float>() + e.shadow_img);
             }
             bool clearing = !(c.op & 8);
             int y0 = clearing ? 0 : std::max(0, std::min(H, c.gy0));
@@ -687,8 +756,11 @@ int frame::run() {
                 pa.y_end = y1;
                 pa.src = src;
                 k_paint<<<std::max(1, (y1 - y0 + 7) / 8), 256, 0, stream>>>(pa);
+                ++launches;
             }
+            if (e.has_shadow) ++launches;
         }
+        mark();   // 4: paint done
         return ok(cudaGetLastError()) ? CY_OK : status;
     }
     // Tile engine: one persistent launch over (canvas, strip) work items.
@@ -750,7 +822,7 @@ int frame::run() {
     P.rv = rv;
     P.src = src;
     P.rects = rects.as<shadow_rect>();
-    P.shadow_imgs = sh_img.as<float>();
+    P.shadow_imgs = sh_scratch.as<float>();
     P.put_px = d_put;
     P.lut = lut;
     P.get_buf = get_dev.as<uint8_t>();
@@ -761,6 +833,8 @@ int frame::run() {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     int grid = std::max(1, std::min(n_items, sms * std::max(per_sm, 1)));
     k_strips<<<grid, g_strip_threads, smem, stream>>>(P);
+    ++launches;
+    mark();   // 4: paint done
     return ok(cudaGetLastError()) ? CY_OK : status;
 }
 
@@ -1261,6 +1335,39 @@ int cy_frame_sync(cy_frame *fr) {
 }
 
 void *cy_frame_stream(cy_frame *fr) { return fr ? static_cast<void *>(fr->stream) : nullptr; }
+
+int cy_frame_set_profiling(cy_frame *fr, int on) {
+    if (!fr) return CY_EINVAL;
+    frame &f = *fr->f;
+    if (on && !f.ev[0])
+        for (cudaEvent_t &e : f.ev)
+            if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); return CY_ECUDA; }
+    f.profiling = on != 0;
+    return CY_OK;
+}
+
+int cy_frame_profile(cy_frame *fr, float *phase_ms, int n) {
+    if (!fr || !phase_ms) return CY_EINVAL;
+    frame &f = *fr->f;
+    if (cudaStreamSynchronize(fr->stream) != cudaSuccess) { cudaGetLastError(); return CY_ECUDA; }
+    for (int i = 0; i < n; ++i) phase_ms[i] = 0.0f;
+    for (int i = 0; i + 1 < f.n_ev && i < n; ++i)
+        if (cudaEventElapsedTime(&phase_ms[i], f.ev[i], f.ev[i + 1]) != cudaSuccess) cudaGetLastError();
+    return f.n_ev > 0 ? f.n_ev - 1 : 0;
+}
+
+int cy_frame_stats(cy_frame *fr, long long *stats, int n) {
+    if (!fr || !stats) return CY_EINVAL;
+    frame &f = *fr->f;
+    long long pixels = 0;
+    for (cy_ctx *c : f.cvs) pixels += static_cast<long long>(c->W) * c->H;
+    long long v[] = {pixels, static_cast<long long>(f.all.cmds.size()), f.total_segs, f.n_runs, f.total_rows,
+                     f.main_runs, f.main_rows, f.shadow_floats, f.get_total, f.h2d_bytes, f.launches,
+                     static_cast<long long>(f.sjobs.size()), static_cast<long long>(f.clips.size())};
+    int m = static_cast<int>(sizeof(v) / sizeof(v[0]));
+    for (int i = 0; i < n && i < m; ++i) stats[i] = v[i];
+    return m;
+}
 
 int cy_ctx_take_reads(cy_ctx *c, unsigned char *out, size_t cap, size_t *len) {
     if (!c) return CY_EINVAL;

@@ -119,12 +119,60 @@ __global__ void k_scan_add(int32_t *__restrict__ out, int n, const int32_t *__re
     out[i] += tile_offs[i >> 12];
 }
 
+// Exclusive scan of int32 counts into int64 offsets, tiles of 4096.
+template <class In>
+__global__ void k_scan_tiles64(const In *__restrict__ in, int64_t *__restrict__ out, int n,
+                               int64_t *__restrict__ tile_sums) {
+    __shared__ long long warp_sums[32];
+    int base = blockIdx.x * 4096 + threadIdx.x * 4;
+    long long v[4];
+    long long local = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        v[j] = base + j < n ? static_cast<long long>(in[base + j]) : 0;
+        local += v[j];
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        long long t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_sums[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        long long s = warp_sums[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        warp_sums[lane] = s;
+    }
+    __syncthreads();
+    long long run = incl - local + (w > 0 ? warp_sums[w - 1] : 0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (base + j < n) out[base + j] = run;
+        run += v[j];
+    }
+    if (threadIdx.x == 1023 && tile_sums) tile_sums[blockIdx.x] = warp_sums[31];
+}
+
+__global__ void k_scan_add64(int64_t *__restrict__ out, int n, const int64_t *__restrict__ tile_offs) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] += tile_offs[i >> 12];
+}
+
 // ------------------------------------------------------- scan conversion
 // lines_to_runs (hpp:2193-2253), row-parallel.  Every queued scan
 // conversion (a draw, its shadow, a clip) is a "job".  Pass 1 counts the
-// nonzero signed-area changes per job row and the job's exact bounds; pass 2
-// writes them into per-row buckets; then every row of every job is sorted,
-// coalesced and prefix-summed independently.
+// cells each segment touches in each job row (one atomic per segment row);
+// pass 2 reserves that many slots in the row's bucket and writes the cells'
+// signed-area changes (zeros included, dropped later).  Then every row of
+// every job is sorted, coalesced and prefix-summed independently.
 struct scan_job {
     int32_t geom;          // 0: host polylines, 1: GPU-flattened polylines
     int32_t line_first;    // first polyline point
@@ -134,7 +182,8 @@ struct scan_job {
     int32_t rows, cols;    // rows and cells per row of the (padded) canvas
     float width, height;   // clip rectangle [0,width] x [0,height]
     float offx, offy;      // added to every point first (shadow offset)
-    int32_t pad[2];
+    int32_t need_box;      // 1: track the exact bounds of nonzero cells
+    int32_t pad;
 };
 
 struct job_tables {
@@ -143,38 +192,10 @@ struct job_tables {
     const float2 *pts[2];
     const int32_t *prev[2];
     cover_box *boxes;       // one per job
-    int32_t *row_cnt;       // count pass: nonzero runs per row (all jobs)
-    const int32_t *row_off; // emit pass: bucket offsets
+    int32_t *row_cnt;       // count pass: cells per row (all jobs)
+    const int64_t *row_off; // emit pass: bucket offsets
     int32_t *row_cur;       // emit pass: bucket cursors
     run *runs;
-};
-
-template <bool EMIT>
-struct run_emit {
-    const job_tables *t;
-    const scan_job *j;
-    int x0, x1, y0, y1;
-    long long first;
-    __device__ void operator()(int x, int y, float d) {
-        if (y < 0 || y >= j->rows || x < 0 || x >= j->cols) return;
-        if (!EMIT) {
-            long long key = (static_cast<long long>(y) << 32) | static_cast<long long>(x);
-            if (key < first) first = key;
-        }
-        if (d == 0.0f) return;
-        int row = j->row_base + y;
-        if (EMIT) {
-            int k = atomicAdd(t->row_cur + row, 1);
-            int n = t->row_off[row + 1] - t->row_off[row];
-            if (k < n) t->runs[t->row_off[row] + k] = run{x, d};
-        } else {
-            atomicAdd(t->row_cnt + row, 1);
-            x0 = x < x0 ? x : x0;
-            x1 = x > x1 ? x : x1;
-            y0 = y < y0 ? y : y0;
-            y1 = y > y1 ? y : y1;
-        }
-    }
 };
 
 __device__ __forceinline__ int job_of_segment(const job_tables &t, int s) {
@@ -186,11 +207,11 @@ __device__ __forceinline__ int job_of_segment(const job_tables &t, int s) {
     return lo_i;
 }
 
-// One warp per segment, one lane per pixel row of each clipped piece.
+// One thread per segment: every row of every clipped piece of it.
 template <bool EMIT>
 __global__ void k_runs(job_tables t, int total_segments) {
-    int lane = threadIdx.x & 31;
-    for (int s = warp_id_global(); s < total_segments; s += warps_total()) {
+    int stride = gridDim.x * blockDim.x;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < total_segments; s += stride) {
         int ji = job_of_segment(t, s);
         const scan_job &j = t.jobs[ji];
         int k = j.line_first + (s - j.seg_first);
@@ -199,39 +220,61 @@ __global__ void k_runs(job_tables t, int total_segments) {
         float2 a = t.pts[g][t.prev[g][k]];
         a = f2(j.offx + a.x, j.offy + a.y);
         b = f2(j.offx + b.x, j.offy + b.y);
-        run_emit<EMIT> e;
-        e.t = &t;
-        e.j = &j;
-        e.x0 = 0x7fffffff; e.x1 = -0x7fffffff; e.y0 = 0x7fffffff; e.y1 = -0x7fffffff;
-        e.first = 0x7fffffffffffffffll;
         float2 pa[3], pb[3];
         int np = clip_segment(a, b, j.width, j.height, pa, pb);
+        int x0 = 0x7fffffff, x1 = -0x7fffffff, y0 = 0x7fffffff, y1 = -0x7fffffff;
+        long long first = 0x7fffffffffffffffll;
         for (int q = 0; q < np; ++q) {
             dda_piece p;
             if (!dda_setup(pa[q], pb[q], p)) continue;
             int nrows = p.nrows < j.rows + 2 ? p.nrows : j.rows + 2;
-            for (int r = lane; r < nrows; r += 32) dda_row(p, r, e);
-        }
-        if (!EMIT) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                e.x0 = min(e.x0, __shfl_xor_sync(0xffffffffu, e.x0, o));
-                e.x1 = max(e.x1, __shfl_xor_sync(0xffffffffu, e.x1, o));
-                e.y0 = min(e.y0, __shfl_xor_sync(0xffffffffu, e.y0, o));
-                e.y1 = max(e.y1, __shfl_xor_sync(0xffffffffu, e.y1, o));
-                e.first = min(e.first, __shfl_xor_sync(0xffffffffu, e.first, o));
-            }
-            if (lane == 0) {
-                cover_box *box = t.boxes + ji;
-                if (e.x0 <= e.x1) {
-                    atomicMin(&box->x0, e.x0);
-                    atomicMax(&box->x1, e.x1);
-                    atomicMin(&box->y0, e.y0);
-                    atomicMax(&box->y1, e.y1);
+            float2 entry = f2(p.fx, p.fy);
+            for (int r = 0; r < nrows; ++r) {
+                float2 ex = dda_exit(p, r);
+                int ps, pe;
+                dda_span(p, r, entry, ex, ps, pe);
+                int row = dda_row_index(p, r);
+                if (row >= 0 && row < j.rows) {
+                    int n = pe - ps + 2;
+                    int grow = j.row_base + row;
+                    if (!EMIT) {
+                        atomicAdd(t.row_cnt + grow, n);
+                        long long key = (static_cast<long long>(row) << 32) | static_cast<long long>(ps < 0 ? 0 : ps);
+                        if (key < first) first = key;
+                    } else {
+                        int base = atomicAdd(t.row_cur + grow, n);
+                        int64_t cap = t.row_off[grow + 1] - t.row_off[grow];
+                        if (base + n <= cap) {
+                            run *out = t.runs + t.row_off[grow] + base;
+                            int i = 0;
+                            int cols = j.cols;
+                            auto emit = [&](int x, float d) {
+                                bool okx = x >= 0 && x < cols;
+                                out[i++] = run{okx ? x : 0, okx ? d : 0.0f};
+                                if (okx && d != 0.0f) {
+                                    x0 = x < x0 ? x : x0;
+                                    x1 = x > x1 ? x : x1;
+                                    y0 = row < y0 ? row : y0;
+                                    y1 = row > y1 ? row : y1;
+                                }
+                            };
+                            dda_cells(p, entry, ex, ps, pe, emit);
+                        }
+                    }
                 }
-                if (e.first != 0x7fffffffffffffffll)
-                    atomicMin(reinterpret_cast<long long *>(&box->first_key), e.first);
+                entry = ex;
             }
+        }
+        if (j.need_box) {
+            cover_box *box = t.boxes + ji;
+            if (EMIT && x0 <= x1) {
+                atomicMin(&box->x0, x0);
+                atomicMax(&box->x1, x1);
+                atomicMin(&box->y0, y0);
+                atomicMax(&box->y1, y1);
+            }
+            if (!EMIT && first != 0x7fffffffffffffffll)
+                atomicMin(reinterpret_cast<long long *>(&box->first_key), first);
         }
     }
 }
@@ -270,34 +313,103 @@ __device__ void sort_runs(run *r, int n) {
     }
 }
 
+static constexpr int kRowCap = 256;   // runs per row sorted in shared memory
+static constexpr int kRowsWarps = 4;  // warps per block in k_rows
+
 // Sort and coalesce one row's runs exactly as the reference does after its
 // std::sort (hpp:2243-2252), then store the running coverage sum after each
 // coalesced cell (the value render_main's walk holds from that cell on).
-// One thread per row over all rows of all jobs.
-__global__ void k_rows(const int32_t *__restrict__ row_off, int32_t *__restrict__ row_cnt,
-                       int32_t *__restrict__ row_cur, int32_t *__restrict__ row_len, run *__restrict__ runs,
-                       float *__restrict__ sums, int total_rows) {
-    int y = blockIdx.x * blockDim.x + threadIdx.x;
-    if (y >= total_rows) return;
-    int n = row_cnt[y];
-    int cap = row_off[y + 1] - row_off[y];
-    if (n > cap) n = cap;
-    run *r = runs + row_off[y];
-    float *sm = sums + row_off[y];
-    sort_runs(r, n);
-    int m = 0;
-    for (int i = 0; i < n; ++i) {
-        if (m > 0 && r[m - 1].x == r[i].x) r[m - 1].delta += r[i].delta;
-        else r[m++] = r[i];
+// One warp per row: the row's nonzero runs are ranked in shared memory by
+// all lanes, then one lane coalesces and sums them in x order (the float
+// additions must follow the reference's order).  Rows longer than the
+// shared buffer are sorted in place by one lane.
+__global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restrict__ row_off,
+                                                          int32_t *__restrict__ row_cnt,
+                                                          int32_t *__restrict__ row_cur, int32_t *__restrict__ row_len,
+                                                          run *__restrict__ runs, float *__restrict__ sums,
+                                                          int total_rows) {
+    __shared__ run buf[kRowsWarps][kRowCap];
+    __shared__ run srt[kRowsWarps][kRowCap];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kRowsWarps + w, nw = gridDim.x * kRowsWarps;
+    for (int y = gw; y < total_rows; y += nw) {
+        int cap = static_cast<int>(row_off[y + 1] - row_off[y]);
+        int n = row_cur[y];
+        if (n > cap) n = cap;
+        run *r = runs + row_off[y];
+        float *sm = sums + row_off[y];
+        // Compact the nonzero runs.
+        int m = 0;
+        bool fits = true;
+        for (int base = 0; base < n; base += 32) {
+            int i = base + lane;
+            run v = i < n ? r[i] : run{0, 0.0f};
+            bool keep = i < n && v.delta != 0.0f;
+            unsigned bal = __ballot_sync(0xffffffffu, keep);
+            int at = m + __popc(bal & ((1u << lane) - 1u));
+            if (keep) {
+                if (at < kRowCap) buf[w][at] = v;
+                else r[at] = v;   // in place: at <= i always
+            }
+            m += __popc(bal);
+            if (m > kRowCap) fits = false;
+        }
+        __syncwarp();
+        if (fits) {
+            for (int i = lane; i < m; i += 32) {
+                run v = buf[w][i];
+                int rank = 0;
+                for (int j = 0; j < m; ++j) {
+                    run u = buf[w][j];
+                    rank += run_less(u, v) || (!run_less(v, u) && j < i);
+                }
+                srt[w][rank] = v;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                int k = 0;
+                float sum = 0.0f;
+                for (int i = 0; i < m; ++i) {
+                    run v = srt[w][i];
+                    if (k > 0 && buf[w][k - 1].x == v.x) buf[w][k - 1].delta += v.delta;
+                    else buf[w][k++] = v;
+                }
+                for (int i = 0; i < k; ++i) {
+                    sum += buf[w][i].delta;
+                    srt[w][i].delta = sum;
+                }
+                m = k;
+            }
+            m = __shfl_sync(0xffffffffu, m, 0);
+            __syncwarp();
+            for (int i = lane; i < m; i += 32) {
+                r[i] = buf[w][i];
+                sm[i] = srt[w][i].delta;
+            }
+        } else if (lane == 0) {
+            // Long row: the first kRowCap compacted runs are in shared memory.
+            for (int i = 0; i < kRowCap; ++i) r[i] = buf[w][i];
+            sort_runs(r, m);
+            int k = 0;
+            for (int i = 0; i < m; ++i) {
+                if (k > 0 && r[k - 1].x == r[i].x) r[k - 1].delta += r[i].delta;
+                else r[k++] = r[i];
+            }
+            float sum = 0.0f;
+            for (int i = 0; i < k; ++i) {
+                sum += r[i].delta;
+                sm[i] = sum;
+            }
+            m = k;
+        }
+        m = __shfl_sync(0xffffffffu, m, 0);
+        if (lane == 0) {
+            row_len[y] = m;
+            row_cnt[y] = 0;
+            row_cur[y] = 0;
+        }
+        __syncwarp();
     }
-    float sum = 0.0f;
-    for (int k = 0; k < m; ++k) {
-        sum += r[k].delta;
-        sm[k] = sum;
-    }
-    row_len[y] = m;
-    row_cnt[y] = 0;
-    row_cur[y] = 0;
 }
 
 // Running sum in force at pixel x: the sum after the last coalesced run at or
@@ -312,7 +424,7 @@ __device__ __forceinline__ float sum_at(const run *r, const float *sm, int n, in
 }
 
 struct row_view {
-    const int32_t *row_off;
+    const int64_t *row_off;
     const int32_t *row_len;
     const run *runs;
     const float *sums;
@@ -364,7 +476,8 @@ __global__ void k_paint(paint_args a) {
 // ------------------------------------------------------------------ clip
 struct clip_args {
     // path runs (sorted, coalesced) of this clip, rows from p_base
-    const int32_t *p_off, *p_len;
+    const int64_t *p_off;
+    const int32_t *p_len;
     const run *p_runs;
     int p_base;
     // old mask (null runs = the whole canvas: per row {0,+1}, {W,-1})
@@ -428,10 +541,10 @@ __global__ void k_clip_rows(clip_args a) {
 
 // Run capacity of each row of a new clip mask: the path's raw runs plus the
 // old mask's runs (2 per row for the whole canvas).
-__global__ void k_clip_caps(const int32_t *path_off, const int32_t *old_off, int H, int32_t *caps) {
+__global__ void k_clip_caps(const int64_t *path_off, const int32_t *old_off, int H, int32_t *caps) {
     int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= H) return;
-    int p = path_off[y + 1] - path_off[y];
+    int p = static_cast<int>(path_off[y + 1] - path_off[y]);
     int o = old_off ? old_off[y + 1] - old_off[y] : 2;
     caps[y] = p + o;
 }

@@ -67,8 +67,11 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
         const int rows = min(cv.TH, cv.H - y0);
         const int cpr = (W + 31) >> 5;           // 32-pixel chunks per row
         const int chunks = rows * cpr;
-        // Initial state.
-        for (int ch = warp; ch < chunks; ch += nwarps) {
+        // Each warp owns a contiguous range of chunks (row-major) for the
+        // whole item, so every pixel is always touched by the same thread.
+        const int per = (chunks + nwarps - 1) / nwarps;
+        const int cb = min(chunks, warp * per), ce = min(chunks, cb + per);
+        for (int ch = cb; ch < ce; ++ch) {
             int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
             if (x >= W) continue;
             float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -80,7 +83,7 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
             const strip_cmd &e = P.ext[ci];
             if (c.kind == CMD_CLIP) continue;
             if (c.kind == CMD_PUT) {
-                for (int ch = warp; ch < chunks; ch += nwarps) {
+                for (int ch = cb; ch < ce; ++ch) {
                     int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
                     int y = y0 + ly;
                     int ix = x - c.put_x, iy = y - c.put_y;
@@ -92,7 +95,7 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
                 continue;
             }
             if (c.kind == CMD_GET) {
-                for (int ch = warp; ch < chunks; ch += nwarps) {
+                for (int ch = cb; ch < ce; ++ch) {
                     int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
                     int y = y0 + ly;
                     int ix = x - e.get_x, iy = y - e.get_y;
@@ -111,7 +114,7 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
                 int b = c.sh_border;
                 int sx0 = max(0, r.left - b), sx1 = min(W, r.right - b);
                 if (r.width > 0 && r.height > 0) {
-                    for (int ch = warp; ch < chunks; ch += nwarps) {
+                    for (int ch = cb; ch < ce; ++ch) {
                         int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
                         int y = y0 + ly;
                         if (x < sx0 || x >= sx1 || y + b < r.top || y + b >= r.bottom) continue;
@@ -125,38 +128,79 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
                     }
                 }
             }
-            // render_main (hpp:2551-2605)
-            for (int ch = warp; ch < chunks; ch += nwarps) {
+            // render_main (hpp:2551-2605).  Walk each row's sorted runs with a
+            // warp-wide cursor: the coverage sum in force at a pixel is the
+            // running sum after the last run at or left of it.
+            int cur = -1, n = 0, j = 0, first_x = 0, last_x = -1;
+            const run *r = nullptr;
+            const float *sm = nullptr;
+            float carry = 0.0f;
+            for (int ch = cb; ch < ce; ++ch) {
                 int ly = ch / cpr, x0 = (ch - ly * cpr) << 5;
-                int y = y0 + ly;
-                int row = e.main_row_base + y;
-                int n = P.rv.row_len[row];
-                const run *r = P.rv.runs + P.rv.row_off[row];
-                const float *sm = P.rv.sums + P.rv.row_off[row];
-                int xs, xe;
-                if (clearing) {
-                    xs = 0;
-                    xe = W - 1;
-                } else {
-                    if (n == 0) continue;
-                    xs = r[0].x;
-                    xe = min(r[n - 1].x, W - 1);
+                if (ly != cur) {
+                    cur = ly;
+                    int row = e.main_row_base + y0 + ly;
+                    n = P.rv.row_len[row];
+                    r = P.rv.runs + P.rv.row_off[row];
+                    sm = P.rv.sums + P.rv.row_off[row];
+                    j = 0;
+                    carry = 0.0f;
+                    first_x = n ? r[0].x : 0x7fffffff;
+                    last_x = n ? r[n - 1].x : -1;
                 }
+                int xs = clearing ? 0 : first_x;
+                int xe = clearing ? W - 1 : min(last_x, W - 1);
                 if (x0 + 31 < xs || x0 > xe) continue;
+                // Consume the runs left of this chunk (they only set the carry).
+                int rx = 0x7fffffff;
+                float rs = 0.0f;
+                for (;;) {
+                    int idx = j + lane;
+                    rx = idx < n ? r[idx].x : 0x7fffffff;
+                    rs = idx < n ? sm[idx] : 0.0f;
+                    unsigned below = __ballot_sync(0xffffffffu, rx < x0);
+                    int nb = __popc(below);
+                    if (nb > 0) carry = __shfl_sync(0xffffffffu, rs, nb - 1);
+                    j += nb;
+                    if (nb < 32) {
+                        if (nb > 0) {   // realign the window at the new cursor
+                            rx = __shfl_down_sync(0xffffffffu, rx, nb);
+                            rs = __shfl_down_sync(0xffffffffu, rs, nb);
+                            if (lane + nb >= 32) {
+                                int k2 = j + lane;
+                                rx = k2 < n ? r[k2].x : 0x7fffffff;
+                                rs = k2 < n ? sm[k2] : 0.0f;
+                            }
+                        }
+                        break;
+                    }
+                }
+                // Runs inside the chunk: at most 32, one per distinct x.
+                bool in_chunk = rx < x0 + 32;
+                unsigned pos_mask = __reduce_or_sync(0xffffffffu, in_chunk ? (1u << (rx - x0)) : 0u);
+                int k = __popc(__ballot_sync(0xffffffffu, in_chunk));
+                unsigned upto = pos_mask & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u));
+                float v = carry;
+                int src = upto ? __popc(upto) - 1 : 0;
+                float from_run = __shfl_sync(0xffffffffu, rs, src);
+                if (upto) v = from_run;
+                if (k > 0) carry = __shfl_sync(0xffffffffu, rs, k - 1);
+                j += k;
                 int x = x0 + lane;
                 if (x < xs || x > xe) continue;
-                float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+                int y = y0 + ly;
+                float cov = lo(fabsf(v), 1.0f);
                 float vis = e.vis ? e.vis[static_cast<size_t>(y) * W + x] : 1.0f;
                 if ((cov >= kVisible || clearing) && vis >= kVisible) {
                     float4 p = paint_at(c, P.src, static_cast<float>(x) + 0.5f, static_cast<float>(y) + 0.5f);
-                    float k = cov * c.alpha;
-                    float4 fore = make_float4(p.x * k, p.y * k, p.z * k, p.w * k);
+                    float kk = cov * c.alpha;
+                    float4 fore = make_float4(p.x * kk, p.y * kk, p.z * kk, p.w * kk);
                     px[ly * W + x] = blend(px[ly * W + x], fore, op, vis);
                 }
             }
         }
         if (cv.flags & 2) {
-            for (int ch = warp; ch < chunks; ch += nwarps) {
+            for (int ch = cb; ch < ce; ++ch) {
                 int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
                 if (x >= W) continue;
                 cv.bitmap[static_cast<size_t>(y0 + ly) * W + x] = px[ly * W + x];
@@ -231,34 +275,59 @@ __global__ void k_shadow_raster_all(const shadow_job *sj, const command *cmds, p
                     val = cov * paint_at(c, src, pxx, pyy).w;
                 }
             }
-            out[static_cast<size_t>(y - rc.top) * rc.width + (x - rc.left)] = val;
+            // Column-major, so the row blur below reads with unit stride across threads.
+            out[static_cast<size_t>(x - rc.left) * rc.height + (y - rc.top)] = val;
         }
     }
 }
 
 // Exact running-sum blur (hpp:2453-2503), rows then columns, batched over
-// shadows through blockIdx.y.  `scratch` has one image-sized area per shadow.
+// shadows through blockIdx.y, one thread per row (then per column) running
+// the reference's sequential sums.  The row pass works on the column-major
+// raster, the image is then transposed, and the column pass works row-major,
+// so neighbouring threads always touch neighbouring addresses.
 __global__ void k_blur_rows_all(const shadow_job *sj, const shadow_rect *rects, float *imgs, float *scratch) {
     const shadow_job &s = sj[blockIdx.y];
     const shadow_rect rc = rects[s.cmd];
     int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= rc.height) return;
-    size_t width = rc.width, r = s.radius;
-    float *row = imgs + s.img + static_cast<size_t>(y) * width;
-    float *t = scratch + s.img + static_cast<size_t>(y) * width;
+    size_t width = rc.width, h = rc.height, r = s.radius;
+    float *row = imgs + s.img + y;
+    float *t = scratch + s.img + y;
     float w1 = s.w1, w2 = s.w2;
     for (int pass = 0; pass < 3; ++pass) {
-        for (size_t x = 0; x < width; ++x) t[x] = row[x];
-        float acc = r + 1 < width ? w1 * t[r + 1] : 0.0f;
-        for (size_t x = 0; x <= r && x < width; ++x) acc += (w1 + w2) * t[x];
+        for (size_t x = 0; x < width; ++x) t[x * h] = row[x * h];
+        float acc = r + 1 < width ? w1 * t[(r + 1) * h] : 0.0f;
+        for (size_t x = 0; x <= r && x < width; ++x) acc += (w1 + w2) * t[x * h];
         row[0] = acc;
         for (size_t x = 1; x < width; ++x) {
-            if (x >= r + 1) acc -= w2 * t[x - r - 1];
-            if (x >= r + 2) acc -= w1 * t[x - r - 2];
-            if (x + r < width) acc += w2 * t[x + r];
-            if (x + r + 1 < width) acc += w1 * t[x + r + 1];
-            row[x] = acc;
+            if (x >= r + 1) acc -= w2 * t[(x - r - 1) * h];
+            if (x >= r + 2) acc -= w1 * t[(x - r - 2) * h];
+            if (x + r < width) acc += w2 * t[(x + r) * h];
+            if (x + r + 1 < width) acc += w1 * t[(x + r + 1) * h];
+            row[x * h] = acc;
         }
+    }
+}
+
+// Column-major -> row-major, 32x32 tiles (blockIdx.z selects the shadow).
+__global__ void k_transpose_all(const shadow_job *sj, const shadow_rect *rects, const float *in, float *out) {
+    __shared__ float tile[32][33];
+    const shadow_job &s = sj[blockIdx.z];
+    const shadow_rect rc = rects[s.cmd];
+    int h = rc.height, w = rc.width;
+    int tx = blockIdx.x * 32, ty = blockIdx.y * 32;
+    if (tx >= w || ty >= h) return;
+    const float *src = in + s.img;
+    float *dst = out + s.img;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        int x = tx + i, y = ty + threadIdx.x;
+        if (x < w && y < h) tile[i][threadIdx.x] = src[static_cast<size_t>(x) * h + y];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        int y = ty + i, x = tx + threadIdx.x;
+        if (x < w && y < h) dst[static_cast<size_t>(y) * w + x] = tile[threadIdx.x][i];
     }
 }
 

@@ -105,6 +105,12 @@ def _batch_lib() -> ctypes.CDLL:
     lib.cy_ctx_take_reads.argtypes = [vp, vp, ctypes.c_size_t, c_size_p]
     lib.cy_set_strip_config.restype = None
     lib.cy_set_strip_config.argtypes = [ctypes.c_int, ctypes.c_int]
+    lib.cy_frame_set_profiling.restype = ctypes.c_int
+    lib.cy_frame_set_profiling.argtypes = [vp, ctypes.c_int]
+    lib.cy_frame_profile.restype = ctypes.c_int
+    lib.cy_frame_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+    lib.cy_frame_stats.restype = ctypes.c_int
+    lib.cy_frame_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]
     lib._batch_ready = True
     return lib
 
@@ -150,6 +156,24 @@ class Frame:
 
     def stream(self) -> int:
         return int(self.lib.cy_frame_stream(self.frame) or 0)
+
+    STAT_NAMES = ("pixels", "commands", "segments", "runs", "rows", "draw_runs", "draw_rows",
+                  "shadow_floats", "read_bytes", "upload_bytes", "launches", "shadows", "clips")
+
+    def stats(self) -> dict:
+        arr = (ctypes.c_longlong * len(self.STAT_NAMES))()
+        n = self.lib.cy_frame_stats(self.frame, arr, len(self.STAT_NAMES))
+        return {k: int(arr[i]) for i, k in enumerate(self.STAT_NAMES[:n])}
+
+    PHASES = ("flatten", "scan_convert", "masks_shadows", "paint")
+
+    def set_profiling(self, on: bool) -> None:
+        self.lib.cy_frame_set_profiling(self.frame, 1 if on else 0)
+
+    def profile(self) -> dict:
+        arr = (ctypes.c_float * 8)()
+        n = self.lib.cy_frame_profile(self.frame, arr, 8)
+        return {self.PHASES[i]: float(arr[i]) for i in range(min(n, len(self.PHASES)))}
 
     def finish(self) -> List[bytes]:
         rc = self.lib.cy_frame_finish(self.frame)

@@ -50,6 +50,20 @@ int cy_frame_finish(cy_frame *frame);
 
 void cy_frame_destroy(cy_frame *frame);
 
+/* Profiling: when on, each run records CUDA events on the frame's stream at
+ * its phase boundaries.  cy_frame_profile waits for the stream and writes
+ * the phase durations in ms: [0] patterns + flattening, [1] scan conversion
+ * (run counting, bucketing, row sort/prefix), [2] clip masks + shadow
+ * images, [3] paint (the strip kernel, or all per-draw launches).  Returns
+ * the number of phases written. */
+int cy_frame_set_profiling(cy_frame *frame, int on);
+int cy_frame_profile(cy_frame *frame, float *phase_ms, int n);
+
+/* Frame statistics (first n of): pixels, commands, segments, runs, rows,
+ * runs of draws, rows of draws, shadow image floats, read-back bytes,
+ * uploaded bytes, kernel launches per run, shadows, clips. */
+int cy_frame_stats(cy_frame *frame, long long *stats, int n);
+
 /* Deferred reads of a context, concatenated in call order (compact RGBA8
  * rectangles); -2 if cap is too small (*len holds the size). */
 int cy_ctx_take_reads(cy_ctx *ctx, unsigned char *out, size_t cap, size_t *len);
