@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -153,8 +154,11 @@ struct cy_ctx {
     queue q;
     std::vector<uint8_t> deferred_out;   // results of deferred reads
     void *cached_frame = nullptr;        // frame reused by this context's flushes
-    int fail(int rc) {
-        if (status == 0) status = rc;
+    int fail(int rc, int line = 0) {
+        if (status == 0) {
+            status = rc;
+            if (std::getenv("CY_DEBUG")) std::fprintf(stderr, "canvas_ity_gb300: frame failed with %d (engine.cu:%d)\n", rc, line);
+        }
         note_thread_status(rc);
         return rc;
     }
@@ -181,11 +185,17 @@ struct frame {
     std::vector<clip_op> clips;
     int max_level = -1;
     int64_t total_rows = 0, total_segs = 0;
+    // Jobs scanned straight from their polylines (tab_nc) and jobs that go
+    // through the clip passes first (tab_cl): (first point, job index).
+    std::vector<int2> tab_nc, tab_cl;
+    int64_t nc_segs = 0, cl_points = 0;
+    int64_t pass_n[5] = {};    // clip pass sizes (input of pass 0 .. output of pass 3)
     int n_items = 0;
     int strip_pixels = 4096;
     // device
     dbuf arena, flat_pts, flat_prev, item_cnt, item_off, pat_f4, jobs_dev, boxes;
-    dbuf row_cnt, row_off, row_cur, row_len, runs, sums;
+    dbuf row_cnt, row_off, row_cur, row_len, long_rows, n_long, runs, sums;
+    dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
     hbuf staging, offs_host, rowoff_host, get_host;
     char *d = nullptr;
@@ -220,6 +230,10 @@ struct frame {
         clips.clear();
         max_level = -1;
         total_rows = total_segs = 0;
+        tab_nc.clear();
+        tab_cl.clear();
+        nc_segs = cl_points = 0;
+        for (int64_t &v : pass_n) v = 0;
         n_items = 0;
         sized = ext_built = strips_built = false;
         n_runs = main_runs = main_rows = h2d_bytes = 0;
@@ -228,7 +242,8 @@ struct frame {
     ~frame() {
         for (cudaEvent_t e : ev) if (e) cudaEventDestroy(e);
         dbuf *b[] = {&arena, &flat_pts, &flat_prev, &item_cnt, &item_off, &pat_f4, &jobs_dev, &boxes, &row_cnt,
-                     &row_off, &row_cur, &row_len, &runs, &sums, &sj_dev, &sh_img, &sh_scratch, &rects,
+                     &row_off, &row_cur, &row_len, &long_rows, &n_long, &runs, &sums, &tabs_dev, &cp_cnt, &cp_off,
+                     &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev};
         for (dbuf *x : b) x->release();
         staging.release();
@@ -236,8 +251,11 @@ struct frame {
         rowoff_host.release();
         get_host.release();
     }
-    int fail(int rc) {
-        if (status == 0) status = rc;
+    int fail(int rc, int line = 0) {
+        if (status == 0) {
+            status = rc;
+            if (std::getenv("CY_DEBUG")) std::fprintf(stderr, "canvas_ity_gb300: frame failed with %d (engine.cu:%d)\n", rc, line);
+        }
         for (cy_ctx *c : cvs) c->fail(rc);
         note_thread_status(rc);
         return rc;
@@ -245,11 +263,13 @@ struct frame {
     bool ok(cudaError_t e) {
         if (e == cudaSuccess) return true;
         cudaGetLastError();
+        if (std::getenv("CY_DEBUG")) std::fprintf(stderr, "canvas_ity_gb300: CUDA error %s\n", cudaGetErrorString(e));
         fail(e == cudaErrorMemoryAllocation ? CY_ENOMEM : CY_ECUDA);
         return false;
     }
     int scan(const int32_t *in, int32_t *out, int n);
-    int scan64(const int32_t *in, int64_t *out, int n);
+    template <class In> int scan64(const In *in, int64_t *out, int n);
+    int clip_passes(job_tables &t);
     void gather();
     int prepare();
     int run();
@@ -277,28 +297,105 @@ int frame::scan(const int32_t *in, int32_t *out, int n) {
     return rc;
 }
 
-int frame::scan64(const int32_t *in, int64_t *out, int n) {
-    // Exclusive scan of int32 counts into int64 offsets.
+// Kernels one tiled scan of n entries launches (4096 entries per tile).
+static int scan_launch_count(int64_t n) {
+    int c = 1;
+    while (n > 4096) {
+        n = (n + 4095) / 4096;
+        c += 2;
+    }
+    return c;
+}
+
+// The reference's Sutherland-Hodgman clip of the jobs that need it
+// (hpp:2204-2235): four passes over the polygons of all such jobs, each a
+// count, a scan and an emit.  The first run reads every pass's size back to
+// size the buffers; later runs of the same frame reuse them.
+int frame::clip_passes(job_tables &t) {
+    if (pass_n[0] <= 0) {
+        pass_n[4] = 0;
+        return CY_OK;
+    }
+    clip_pass P;
+    std::memset(&P, 0, sizeof(P));
+    P.jobs = jobs_dev.as<scan_job>();
+    P.tab = tabs_dev.as<int2>() + tab_nc.size();
+    P.n_tab = static_cast<int>(tab_cl.size());
+    P.src_pts[0] = t.pts[0];
+    P.src_pts[1] = t.pts[1];
+    P.src_prev[0] = t.prev[0];
+    P.src_prev[1] = t.prev[1];
+    for (int e = 0; e < 4; ++e) {
+        int64_t n = pass_n[e];
+        if (n > INT32_MAX / 2) return fail(CY_ENOMEM, __LINE__);
+        P.n = static_cast<int>(n);
+        P.edge = e;
+        if (!sized && (!cp_cnt.ensure(static_cast<size_t>(n + 1) * 4) || !cp_off.ensure(static_cast<size_t>(n + 1) * 4)))
+            return fail(CY_ENOMEM, __LINE__);
+        P.cnt = cp_cnt.as<int32_t>();
+        P.off = cp_off.as<int32_t>();
+        if (e > 0) {
+            int in = (e - 1) & 1;
+            P.in_pts = cp_pts[in].as<float2>();
+            P.in_prev = cp_prev[in].as<int32_t>();
+            P.in_job = cp_job[in].as<int32_t>();
+        }
+        int grid = std::max(1, static_cast<int>(std::min<int64_t>((n + 1 + 255) / 256, 152 * 32)));
+        if (n > 0) {
+            if (e == 0) k_clip_count<true><<<grid, 256, 0, stream>>>(P);
+            else k_clip_count<false><<<grid, 256, 0, stream>>>(P);
+            int rc = scan(P.cnt, cp_off.as<int32_t>(), static_cast<int>(n) + 1);
+            if (rc) return rc;
+            launches += 1 + scan_launch_count(n + 1);
+        }
+        if (!sized) {
+            int32_t total = 0;
+            if (n > 0 && (!ok(cudaMemcpyAsync(&total, cp_off.as<int32_t>() + n, 4, cudaMemcpyDeviceToHost, stream)) ||
+                          !ok(cudaStreamSynchronize(stream))))
+                return status;
+            if (total < 0 || total > INT32_MAX / 2) return fail(CY_ENOMEM, __LINE__);
+            pass_n[e + 1] = total;
+            int out = e & 1;
+            size_t m = static_cast<size_t>(total) + 1;
+            if (!cp_pts[out].ensure(m * sizeof(float2)) || !cp_prev[out].ensure(m * 4) || !cp_job[out].ensure(m * 4))
+                return fail(CY_ENOMEM, __LINE__);
+        }
+        int out = e & 1;
+        P.out_pts = cp_pts[out].as<float2>();
+        P.out_prev = cp_prev[out].as<int32_t>();
+        P.out_job = cp_job[out].as<int32_t>();
+        if (n > 0) {
+            if (e == 0) {
+                k_clip_emit<true><<<grid, 256, 0, stream>>>(P);
+                k_clip_link<true><<<grid, 256, 0, stream>>>(P);
+            } else {
+                k_clip_emit<false><<<grid, 256, 0, stream>>>(P);
+                k_clip_link<false><<<grid, 256, 0, stream>>>(P);
+            }
+            launches += 2;
+        }
+    }
+    t.cl_pts = cp_pts[1].as<float2>();
+    t.cl_prev = cp_prev[1].as<int32_t>();
+    t.cl_job = cp_job[1].as<int32_t>();
+    return ok(cudaGetLastError()) ? CY_OK : status;
+}
+
+template <class In>
+int frame::scan64(const In *in, int64_t *out, int n) {
+    // Exclusive scan of counts into int64 offsets, recursing over tile sums.
     int tiles = (n + 4095) / 4096;
     if (tiles <= 0) return CY_OK;
     if (tiles == 1) {
-        k_scan_tiles64<int32_t><<<1, 1024, 0, stream>>>(in, out, n, nullptr);
+        k_scan_tiles64<In><<<1, 1024, 0, stream>>>(in, out, n, nullptr);
         return ok(cudaGetLastError()) ? CY_OK : status;
     }
     int64_t *sums_p = nullptr, *offs_p = nullptr;
     if (!ok(cudaMallocAsync(reinterpret_cast<void **>(&sums_p), static_cast<size_t>(tiles) * 8, stream)) ||
         !ok(cudaMallocAsync(reinterpret_cast<void **>(&offs_p), static_cast<size_t>(tiles) * 8, stream)))
         return status;
-    k_scan_tiles64<int32_t><<<tiles, 1024, 0, stream>>>(in, out, n, sums_p);
-    // Tile sums are int64: scan them with the same kernel on int64 input.
-    int rc = CY_OK;
-    int t2 = (tiles + 4095) / 4096;
-    if (t2 == 1) {
-        k_scan_tiles64<int64_t><<<1, 1024, 0, stream>>>(sums_p, offs_p, tiles, nullptr);
-    } else {
-        // Beyond 16.7M tiles (6.9e10 entries) is not supported.
-        rc = fail(CY_ENOMEM);
-    }
+    k_scan_tiles64<In><<<tiles, 1024, 0, stream>>>(in, out, n, sums_p);
+    int rc = scan64<int64_t>(sums_p, offs_p, tiles);
     if (rc == CY_OK) k_scan_add64<<<(n + 255) / 256, 256, 0, stream>>>(out, n, offs_p);
     cudaFreeAsync(sums_p, stream);
     cudaFreeAsync(offs_p, stream);
@@ -350,6 +447,17 @@ void frame::gather() {
     }
 }
 
+// Whether a job's points (command bounds moved by the job's offset) can fall
+// outside [0, wd] x [0, ht].  Inside, the reference's Sutherland-Hodgman
+// pass returns the polygon unchanged, so the clip passes are skipped; the one
+// pixel margin covers the rounding of flattening and of adding the offset.
+static bool needs_clip(const command &c, float wd, float ht, float ox, float oy) {
+    if (c.gx0 <= -1000000000 || c.gy0 <= -1000000000 || c.gx1 >= 1000000000 || c.gy1 >= 1000000000) return true;
+    double x0 = static_cast<double>(c.gx0) + ox, x1 = static_cast<double>(c.gx1) + ox;
+    double y0 = static_cast<double>(c.gy0) + oy, y1 = static_cast<double>(c.gy1) + oy;
+    return !(x0 >= 1.0 && y0 >= 1.0 && x1 <= static_cast<double>(wd) - 1.0 && y1 <= static_cast<double>(ht) - 1.0);
+}
+
 int frame::prepare() {
     gather();
     std::vector<command> &cmds = all.cmds;
@@ -368,7 +476,7 @@ int frame::prepare() {
     o_tex = align256(o_scol + all.stop_col.size() * sizeof(float4));
     o_put = align256(o_tex + all.texels.size() * sizeof(uchar4));
     size_t total = align256(o_put + all.put_px.size());
-    if (!arena.ensure(total) || !staging.ensure(total)) return fail(CY_ENOMEM);
+    if (!arena.ensure(total) || !staging.ensure(total)) return fail(CY_ENOMEM, __LINE__);
     char *h = static_cast<char *>(staging.p);
     auto put = [&](size_t off, const void *src, size_t n) { if (n) std::memcpy(h + off, src, n); };
     put(o_hpts, all.host_pts.data(), all.host_pts.size() * sizeof(float2));
@@ -383,7 +491,7 @@ int frame::prepare() {
     if (total > o_hpts && !ok(cudaMemcpyAsync(d + o_hpts, h + o_hpts, total - o_hpts, cudaMemcpyHostToDevice, stream)))
         return status;
     h2d_bytes = static_cast<int64_t>(total);
-    if (!lut_dev.ensure(256 * sizeof(float))) return fail(CY_ENOMEM);
+    if (!lut_dev.ensure(256 * sizeof(float))) return fail(CY_ENOMEM, __LINE__);
     if (!ok(cudaMemcpyAsync(lut_dev.p, linear_lut_host(), 256 * sizeof(float), cudaMemcpyHostToDevice, stream)))
         return status;
     // Flattening counts size the polyline store (one read-back).
@@ -393,7 +501,7 @@ int frame::prepare() {
         if (!item_cnt.ensure(static_cast<size_t>(n_items + 1) * 4) ||
             !item_off.ensure(static_cast<size_t>(n_items + 1) * 4) ||
             !offs_host.ensure(static_cast<size_t>(n_items + 1) * 4))
-            return fail(CY_ENOMEM);
+            return fail(CY_ENOMEM, __LINE__);
         const float2 *d_bez = reinterpret_cast<const float2 *>(d + o_bez);
         const flat_item *d_items = reinterpret_cast<const flat_item *>(d + o_items);
         k_flat_count<<<(n_items + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items, item_cnt.as<int32_t>());
@@ -406,10 +514,10 @@ int frame::prepare() {
             return status;
         offs_h = static_cast<const int32_t *>(offs_host.p);
         int64_t nflat = offs_h[n_items];
-        if (nflat < 0 || nflat > (static_cast<int64_t>(1) << 30)) return fail(CY_ENOMEM);
+        if (nflat < 0 || nflat > (static_cast<int64_t>(1) << 30)) return fail(CY_ENOMEM, __LINE__);
         if (!flat_pts.ensure(static_cast<size_t>(nflat + 1) * sizeof(float2)) ||
             !flat_prev.ensure(static_cast<size_t>(nflat + 1) * 4))
-            return fail(CY_ENOMEM);
+            return fail(CY_ENOMEM, __LINE__);
     }
     for (command &c : cmds) {
         if (c.kind != CMD_FILL && c.kind != CMD_CLIP) continue;
@@ -437,8 +545,8 @@ int frame::prepare() {
         std::memset(&j, 0, sizeof(j));
         j.geom = c.geom;
         j.line_first = c.line_first;
-        j.seg_first = static_cast<int32_t>(total_segs);
         j.seg_count = c.line_count;
+        j.clip = needs_clip(c, wd, ht, ox, oy) ? 1 : 0;
         j.row_base = static_cast<int32_t>(total_rows);
         j.rows = rows_n;
         j.cols = cols_n;
@@ -488,13 +596,35 @@ int frame::prepare() {
             max_level = std::max(max_level, lv);
         }
     }
-    if (total_rows > INT32_MAX / 2 || total_segs > INT32_MAX / 2) return fail(CY_ENOMEM);
+    if (total_rows > INT32_MAX / 2 || total_segs > INT32_MAX / 2) return fail(CY_ENOMEM, __LINE__);
+    for (size_t ji = 0; ji < jobs.size(); ++ji) {
+        const scan_job &j = jobs[ji];
+        if (j.seg_count <= 0) continue;
+        if (j.clip) {
+            tab_cl.push_back(make_int2(static_cast<int>(cl_points), static_cast<int>(ji)));
+            cl_points += j.seg_count;
+        } else {
+            tab_nc.push_back(make_int2(static_cast<int>(nc_segs), static_cast<int>(ji)));
+            nc_segs += j.seg_count;
+        }
+    }
+    pass_n[0] = cl_points;
+    if (!tab_nc.empty() || !tab_cl.empty()) {
+        size_t nt = tab_nc.size() + tab_cl.size();
+        if (!tabs_dev.ensure(nt * sizeof(int2))) return fail(CY_ENOMEM, __LINE__);
+        std::vector<int2> both(tab_nc);
+        both.insert(both.end(), tab_cl.begin(), tab_cl.end());
+        if (!ok(cudaMemcpyAsync(tabs_dev.p, both.data(), nt * sizeof(int2), cudaMemcpyHostToDevice, stream)) ||
+            !ok(cudaStreamSynchronize(stream)))
+            return status;
+    }
     size_t nr = static_cast<size_t>(total_rows);
     if (!jobs.empty()) {
         if (!jobs_dev.ensure(jobs.size() * sizeof(scan_job)) || !row_cnt.ensure((nr + 1) * 4) ||
             !row_off.ensure((nr + 2) * 8) || !row_cur.ensure((nr + 1) * 4) || !row_len.ensure((nr + 1) * 4) ||
-            !boxes.ensure(jobs.size() * sizeof(cover_box)) || !rowoff_host.ensure((nr + 1) * 8))
-            return fail(CY_ENOMEM);
+            !boxes.ensure(jobs.size() * sizeof(cover_box)) || !rowoff_host.ensure((nr + 1) * 8) ||
+            !long_rows.ensure((nr + 1) * 4) || !n_long.ensure(4))
+            return fail(CY_ENOMEM, __LINE__);
         if (!ok(cudaMemcpyAsync(jobs_dev.p, jobs.data(), jobs.size() * sizeof(scan_job), cudaMemcpyHostToDevice,
                                 stream)) ||
             !ok(cudaMemsetAsync(row_cnt.p, 0, (nr + 1) * 4, stream)) ||
@@ -505,15 +635,16 @@ int frame::prepare() {
         if (!sj_dev.ensure(sjobs.size() * sizeof(cyg::shadow_job)) ||
             !sh_img.ensure(static_cast<size_t>(shadow_floats) * 4) ||
             !sh_scratch.ensure(static_cast<size_t>(shadow_floats) * 4))
-            return fail(CY_ENOMEM);
+            return fail(CY_ENOMEM, __LINE__);
         if (!ok(cudaMemcpyAsync(sj_dev.p, sjobs.data(), sjobs.size() * sizeof(cyg::shadow_job),
                                 cudaMemcpyHostToDevice, stream)))
             return status;
     }
-    if (!rects.ensure(std::max<size_t>(cmds.size(), 1) * sizeof(shadow_rect))) return fail(CY_ENOMEM);
+    if (!rects.ensure(std::max<size_t>(cmds.size(), 1) * sizeof(shadow_rect))) return fail(CY_ENOMEM, __LINE__);
     if (!get_dev.ensure(static_cast<size_t>(std::max<int64_t>(get_total, 16))) ||
         !get_host.ensure(static_cast<size_t>(std::max<int64_t>(get_total, 16))))
-        return fail(CY_ENOMEM);
+        return fail(CY_ENOMEM, __LINE__);
+    if (!ok(cudaFuncSetAttribute(k_rows_long, cudaFuncAttributeMaxDynamicSharedMemorySize, kLongSmem))) return status;
     // The first run also sizes the run store and the clip masks.
     return run();
 }
@@ -535,7 +666,7 @@ int frame::run() {
     src.stop_col = reinterpret_cast<const float4 *>(d + o_scol);
     src.texels = nullptr;
     if (!all.texels.empty()) {
-        if (!pat_f4.ensure(all.texels.size() * sizeof(float4))) return fail(CY_ENOMEM);
+        if (!pat_f4.ensure(all.texels.size() * sizeof(float4))) return fail(CY_ENOMEM, __LINE__);
         int n = static_cast<int>(all.texels.size());
         k_pattern_prep<<<(n + 255) / 256, 256, 0, stream>>>(reinterpret_cast<const uchar4 *>(d + o_tex),
                                                             pat_f4.as<float4>(), n, lut);
@@ -564,7 +695,8 @@ int frame::run() {
         std::memset(&t, 0, sizeof(t));
         k_box_init<<<(n_jobs + 255) / 256, 256, 0, stream>>>(boxes.as<cover_box>(), n_jobs);
         t.jobs = jobs_dev.as<scan_job>();
-        t.n_jobs = n_jobs;
+        t.tab = tabs_dev.as<int2>();
+        t.n_tab = static_cast<int>(tab_nc.size());
         t.pts[0] = d_hpts;
         t.prev[0] = d_hprev;
         t.pts[1] = flat_pts.p ? flat_pts.as<float2>() : d_hpts;
@@ -572,10 +704,14 @@ int frame::run() {
         t.boxes = boxes.as<cover_box>();
         t.row_cnt = row_cnt.as<int32_t>();
         t.row_cur = row_cur.as<int32_t>();
-        int segs = static_cast<int>(total_segs);
-        int grid = std::max(1, std::min((segs + 127) / 128, 152 * 64));
-        if (segs > 0) k_runs<false><<<grid, 128, 0, stream>>>(t, segs);
-        int rc = scan64(row_cnt.as<int32_t>(), row_off.as<int64_t>(), static_cast<int>(nr) + 1);
+        int rc = clip_passes(t);
+        if (rc) return rc;
+        int segs_nc = static_cast<int>(nc_segs), segs_cl = static_cast<int>(pass_n[4]);
+        int grid_nc = std::max(1, std::min((segs_nc + 127) / 128, 152 * 64));
+        int grid_cl = std::max(1, std::min((segs_cl + 127) / 128, 152 * 64));
+        if (segs_nc > 0) k_runs<false, false><<<grid_nc, 128, 0, stream>>>(t, segs_nc);
+        if (segs_cl > 0) k_runs<false, true><<<grid_cl, 128, 0, stream>>>(t, segs_cl);
+        rc = scan64(row_cnt.as<int32_t>(), row_off.as<int64_t>(), static_cast<int>(nr) + 1);
         if (rc) return rc;
         if (!sized) {
             sized = true;
@@ -585,7 +721,7 @@ int frame::run() {
                 return status;
             const int64_t *rowoff_h = static_cast<const int64_t *>(rowoff_host.p);
             int64_t nruns = rowoff_h[nr];
-            if (nruns < 0) return fail(CY_ENOMEM);
+            if (nruns < 0) return fail(CY_ENOMEM, __LINE__);
             n_runs = nruns;
             for (size_t i = 0; i < cmds.size(); ++i) {
                 if (cmds[i].kind != CMD_FILL || main_job[i] < 0) continue;
@@ -595,7 +731,7 @@ int frame::run() {
             }
             if (!runs.ensure(static_cast<size_t>(nruns + 1) * sizeof(cyg::run)) ||
                 !sums.ensure(static_cast<size_t>(nruns + 1) * sizeof(float)))
-                return fail(CY_ENOMEM);
+                return fail(CY_ENOMEM, __LINE__);
             rv.runs = runs.as<cyg::run>();
             rv.sums = sums.as<float>();
             for (const clip_op &op : clips) {
@@ -605,7 +741,7 @@ int frame::run() {
                 int64_t path_runs = rowoff_h[j.row_base + j.rows] - rowoff_h[j.row_base];
                 int64_t old_cap = op.in_id > 0 ? cv->masks[op.in_id].cap : 2 * static_cast<int64_t>(cv->H);
                 nm.cap = std::max<int64_t>(path_runs + old_cap, 1);
-                if (nm.cap > INT32_MAX) return fail(CY_ENOMEM);
+                if (nm.cap > INT32_MAX) return fail(CY_ENOMEM, __LINE__);
                 if (!ok(cudaMalloc(&nm.runs, static_cast<size_t>(nm.cap) * sizeof(cyg::run))) ||
                     !ok(cudaMalloc(&nm.sums, static_cast<size_t>(nm.cap) * sizeof(float))))
                     return status;
@@ -613,13 +749,19 @@ int frame::run() {
         }
         t.row_off = row_off.as<int64_t>();
         t.runs = runs.as<cyg::run>();
-        if (segs > 0) k_runs<true><<<grid, 128, 0, stream>>>(t, segs);
-        int rgrid = static_cast<int>(std::min<size_t>((nr + kRowsWarps - 1) / kRowsWarps, 152 * 64));
+        if (segs_nc > 0) k_runs<true, false><<<grid_nc, 128, 0, stream>>>(t, segs_nc);
+        if (segs_cl > 0) k_runs<true, true><<<grid_cl, 128, 0, stream>>>(t, segs_cl);
+        int rgrid = static_cast<int>(std::min<size_t>((nr + kRowsWarps - 1) / kRowsWarps, 152 * 32));
+        if (!ok(cudaMemsetAsync(n_long.p, 0, 4, stream))) return status;
         k_rows<<<std::max(rgrid, 1), kRowsWarps * 32, 0, stream>>>(
             row_off.as<int64_t>(), row_cnt.as<int32_t>(), row_cur.as<int32_t>(), row_len.as<int32_t>(),
-            runs.as<cyg::run>(), sums.as<float>(), static_cast<int>(nr));
+            runs.as<cyg::run>(), sums.as<float>(), static_cast<int>(nr), long_rows.as<int32_t>(),
+            n_long.as<int32_t>());
+        k_rows_long<<<152 * 2, kLongThreads, kLongSmem, stream>>>(
+            row_off.as<int64_t>(), row_cnt.as<int32_t>(), row_cur.as<int32_t>(), row_len.as<int32_t>(),
+            runs.as<cyg::run>(), sums.as<float>(), long_rows.as<int32_t>(), n_long.as<int32_t>());
         if (!ok(cudaGetLastError())) return status;
-        launches += (segs > 0 ? 2 : 0) + 2 + (nr + 1 > 4096 ? 3 : 1);
+        launches += (segs_nc > 0 ? 2 : 0) + (segs_cl > 0 ? 2 : 0) + 2 + scan_launch_count(static_cast<int64_t>(nr) + 1);
     }
     mark();   // 2: scan conversion done
     // Clip masks, level by level (a clip depends on the previous mask).
@@ -658,7 +800,7 @@ int frame::run() {
             k_mask_fill<<<std::max(1, (H + 7) / 8), 256, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, W, H,
                                                                       nm.vis);
             if (!ok(cudaGetLastError())) return status;
-            launches += 5 + (H + 1 > 4096 ? 3 : 1);
+            launches += 5 + scan_launch_count(H + 1);
         }
     }
     // Shadow images of every shadowed draw.
@@ -797,7 +939,7 @@ int frame::run() {
         if (!scv_dev.ensure(scv.size() * sizeof(strip_canvas)) ||
             !items_dev.ensure(std::max<size_t>(items_host.size(), 1) * sizeof(int2)) ||
             !ext_dev.ensure(std::max<size_t>(ext.size(), 1) * sizeof(strip_cmd)) || !counter.ensure(4))
-            return fail(CY_ENOMEM);
+            return fail(CY_ENOMEM, __LINE__);
         if (!ok(cudaMemcpyAsync(scv_dev.p, scv.data(), scv.size() * sizeof(strip_canvas), cudaMemcpyHostToDevice,
                                 stream)))
             return status;
@@ -1027,7 +1169,7 @@ int flush_ctx(cy_ctx *c) {
     if (c->q.empty()) return CY_OK;
     if (!c->cached_frame) c->cached_frame = new (std::nothrow) frame();
     frame *f = static_cast<frame *>(c->cached_frame);
-    if (!f) return c->fail(CY_ENOMEM);
+    if (!f) return c->fail(CY_ENOMEM, __LINE__);
     f->reset();
     f->stream = c->stream;
     f->engine = c->engine;
@@ -1197,7 +1339,7 @@ int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, i
     auto okc = [&](cudaError_t e) {
         if (e == cudaSuccess) return true;
         cudaGetLastError();
-        c->fail(CY_ENOMEM);
+        c->fail(CY_ENOMEM, __LINE__);
         return false;
     };
     if (!okc(cudaMalloc(&m.vis, static_cast<size_t>(c->W) * c->H * sizeof(float))) ||
@@ -1361,7 +1503,7 @@ int cy_frame_stats(cy_frame *fr, long long *stats, int n) {
     frame &f = *fr->f;
     long long pixels = 0;
     for (cy_ctx *c : f.cvs) pixels += static_cast<long long>(c->W) * c->H;
-    long long v[] = {pixels, static_cast<long long>(f.all.cmds.size()), f.total_segs, f.n_runs, f.total_rows,
+    long long v[] = {pixels, static_cast<long long>(f.all.cmds.size()), f.nc_segs + f.pass_n[4], f.n_runs, f.total_rows,
                      f.main_runs, f.main_rows, f.shadow_floats, f.get_total, f.h2d_bytes, f.launches,
                      static_cast<long long>(f.sjobs.size()), static_cast<long long>(f.clips.size())};
     int m = static_cast<int>(sizeof(v) / sizeof(v[0]));

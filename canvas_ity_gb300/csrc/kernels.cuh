@@ -168,7 +168,11 @@ __global__ void k_scan_add64(int64_t *__restrict__ out, int n, const int64_t *__
 
 // ------------------------------------------------------- scan conversion
 // lines_to_runs (hpp:2193-2253), row-parallel.  Every queued scan
-// conversion (a draw, its shadow, a clip) is a "job".  Pass 1 counts the
+// conversion (a draw, its shadow, a clip) is a "job".  A job whose points can
+// leave its rectangle first goes through the reference's Sutherland-Hodgman
+// clip (four passes, each a count, a scan and an emit over all points of all
+// such jobs); jobs that stay inside are scanned straight from their
+// polylines, which the clip would return unchanged.  Then pass 1 counts the
 // cells each segment touches in each job row (one atomic per segment row);
 // pass 2 reserves that many slots in the row's bucket and writes the cells'
 // signed-area changes (zeros included, dropped later).  Then every row of
@@ -176,8 +180,8 @@ __global__ void k_scan_add64(int64_t *__restrict__ out, int n, const int64_t *__
 struct scan_job {
     int32_t geom;          // 0: host polylines, 1: GPU-flattened polylines
     int32_t line_first;    // first polyline point
-    int32_t seg_first;     // prefix of segment counts over jobs
-    int32_t seg_count;
+    int32_t seg_count;     // polyline points (= segments, each closing on its predecessor)
+    int32_t clip;          // 1: points may leave [0,width] x [0,height]
     int32_t row_base;      // first row of this job in the shared row arrays
     int32_t rows, cols;    // rows and cells per row of the (padded) canvas
     float width, height;   // clip rectangle [0,width] x [0,height]
@@ -186,11 +190,156 @@ struct scan_job {
     int32_t pad;
 };
 
+// Segment ranges of a list of jobs: entry i = (first segment, job index),
+// sorted by first segment.
+__device__ __forceinline__ int table_find(const int2 *tab, int n, int s) {
+    int lo_i = 0, hi_i = n;   // last entry with first <= s
+    while (hi_i - lo_i > 1) {
+        int mid = (lo_i + hi_i) >> 1;
+        if (tab[mid].x <= s) lo_i = mid; else hi_i = mid;
+    }
+    return lo_i;
+}
+
+// One polygon point of a clip pass: the segment ending at it, its job, and
+// whether it starts its polygon (then `last` is the polygon's last point).
+struct poly_point {
+    float2 from, to;
+    int job;
+    bool start;
+    int last;
+};
+
+struct clip_pass {
+    // pass 0 reads the polylines of the clipped jobs
+    const scan_job *jobs;
+    const int2 *tab;           // clipped jobs: (first input point, job)
+    int n_tab;
+    const float2 *src_pts[2];
+    const int32_t *src_prev[2];
+    // passes 1-3 read the previous pass's polygons
+    const float2 *in_pts;
+    const int32_t *in_prev, *in_job;
+    int n;                     // input points
+    int edge;                  // 0: x >= 0, 1: y >= 0, 2: x <= width, 3: y <= height
+    int32_t *cnt;              // per input point: points emitted (n + 1 entries)
+    const int32_t *off;        // exclusive scan of cnt
+    float2 *out_pts;
+    int32_t *out_prev, *out_job;
+};
+
+template <bool FIRST>
+__device__ __forceinline__ poly_point clip_point(const clip_pass &P, int k) {
+    poly_point q;
+    if (FIRST) {
+        int c = table_find(P.tab, P.n_tab, k);
+        const scan_job &j = P.jobs[P.tab[c].y];
+        int g = j.geom ? 1 : 0;
+        int i = j.line_first + (k - P.tab[c].x);
+        int pi = P.src_prev[g][i];
+        float2 a = P.src_pts[g][pi], b = P.src_pts[g][i];
+        q.from = f2(j.offx + a.x, j.offy + a.y);   // scan's add(offset, point) (hpp:2205)
+        q.to = f2(j.offx + b.x, j.offy + b.y);
+        q.job = P.tab[c].y;
+        q.start = pi >= i;
+        q.last = k + (pi - i);
+    } else {
+        int pk = P.in_prev[k];
+        q.from = P.in_pts[pk];
+        q.to = P.in_pts[k];
+        q.job = P.in_job[k];
+        q.start = pk >= k;
+        q.last = pk;
+    }
+    if (q.last >= P.n) q.last = P.n - 1;
+    return q;
+}
+
+// Signed distances of the segment's ends from clip edge `edge` of the job,
+// as the reference computes them: dot(point, normal) + place (hpp:2209-2218).
+__device__ __forceinline__ void edge_sides(const clip_pass &P, const poly_point &q, float &fs, float &ts) {
+    const scan_job &j = P.jobs[q.job];
+    float nx = P.edge == 0 ? 1.0f : P.edge == 2 ? -1.0f : 0.0f;
+    float ny = P.edge == 1 ? 1.0f : P.edge == 3 ? -1.0f : 0.0f;
+    float place = P.edge == 2 ? j.width : P.edge == 3 ? j.height : 0.0f;
+    fs = (q.from.x * nx + q.from.y * ny) + place;
+    ts = (q.to.x * nx + q.to.y * ny) + place;
+}
+
+template <bool FIRST>
+__global__ void k_clip_count(clip_pass P) {
+    int stride = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= P.n; k += stride) {
+        if (k == P.n) { P.cnt[k] = 0; continue; }
+        poly_point q = clip_point<FIRST>(P, k);
+        float fs, ts;
+        edge_sides(P, q, fs, ts);
+        P.cnt[k] = (fs * ts < 0.0f ? 1 : 0) + (ts >= 0.0f ? 1 : 0);
+    }
+}
+
+// Emit a pass's polygon points: the crossing with the edge, then the end
+// point if it is inside (hpp:2213-2216).  Each point links to the one before
+// it; k_clip_link then closes every polygon.
+template <bool FIRST>
+__global__ void k_clip_emit(clip_pass P) {
+    int stride = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += stride) {
+        poly_point q = clip_point<FIRST>(P, k);
+        float fs, ts;
+        edge_sides(P, q, fs, ts);
+        int o = P.off[k];
+        if (fs * ts < 0.0f) {
+            P.out_pts[o] = mix2(q.from, q.to, fs / (fs - ts));
+            P.out_prev[o] = o - 1;
+            P.out_job[o] = q.job;
+            ++o;
+        }
+        if (ts >= 0.0f) {
+            P.out_pts[o] = q.to;
+            P.out_prev[o] = o - 1;
+            P.out_job[o] = q.job;
+        }
+    }
+}
+
+// The first emitted point of each polygon closes on its last one.
+template <bool FIRST>
+__global__ void k_clip_link(clip_pass P) {
+    int stride = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P.n; k += stride) {
+        bool start;
+        int last;
+        if (FIRST) {
+            int c = table_find(P.tab, P.n_tab, k);
+            const scan_job &j = P.jobs[P.tab[c].y];
+            int g = j.geom ? 1 : 0;
+            int i = j.line_first + (k - P.tab[c].x);
+            int pi = P.src_prev[g][i];
+            start = pi >= i;
+            last = k + (pi - i);
+        } else {
+            int pk = P.in_prev[k];
+            start = pk >= k;
+            last = pk;
+        }
+        if (!start) continue;
+        if (last >= P.n) last = P.n - 1;
+        int first_out = P.off[k], end_out = P.off[last + 1];
+        if (end_out > first_out) P.out_prev[first_out] = end_out - 1;
+    }
+}
+
 struct job_tables {
     const scan_job *jobs;
-    int n_jobs;
+    // unclipped jobs: segments straight from the polylines
+    const int2 *tab;          // (first segment, job)
+    int n_tab;
     const float2 *pts[2];
     const int32_t *prev[2];
+    // clipped jobs: the last clip pass's polygons (offset already applied)
+    const float2 *cl_pts;
+    const int32_t *cl_prev, *cl_job;
     cover_box *boxes;       // one per job
     int32_t *row_cnt;       // count pass: cells per row (all jobs)
     const int64_t *row_off; // emit pass: bucket offsets
@@ -198,35 +347,36 @@ struct job_tables {
     run *runs;
 };
 
-__device__ __forceinline__ int job_of_segment(const job_tables &t, int s) {
-    int lo_i = 0, hi_i = t.n_jobs;   // last job with seg_first <= s
-    while (hi_i - lo_i > 1) {
-        int mid = (lo_i + hi_i) >> 1;
-        if (t.jobs[mid].seg_first <= s) lo_i = mid; else hi_i = mid;
-    }
-    return lo_i;
-}
-
-// One thread per segment: every row of every clipped piece of it.
-template <bool EMIT>
+// One thread per segment: every row of it, clamped to the job's rectangle
+// as scan does before add_runs (hpp:2236-2238).
+template <bool EMIT, bool CLIPPED>
 __global__ void k_runs(job_tables t, int total_segments) {
     int stride = gridDim.x * blockDim.x;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < total_segments; s += stride) {
-        int ji = job_of_segment(t, s);
+        int ji;
+        float2 a, b;
+        if (CLIPPED) {
+            ji = t.cl_job[s];
+            a = t.cl_pts[t.cl_prev[s]];
+            b = t.cl_pts[s];
+        } else {
+            int c = table_find(t.tab, t.n_tab, s);
+            ji = t.tab[c].y;
+            const scan_job &jj = t.jobs[ji];
+            int k = jj.line_first + (s - t.tab[c].x);
+            int g = jj.geom ? 1 : 0;
+            float2 pb = t.pts[g][k];
+            float2 pa = t.pts[g][t.prev[g][k]];
+            a = f2(jj.offx + pa.x, jj.offy + pa.y);
+            b = f2(jj.offx + pb.x, jj.offy + pb.y);
+        }
         const scan_job &j = t.jobs[ji];
-        int k = j.line_first + (s - j.seg_first);
-        int g = j.geom ? 1 : 0;
-        float2 b = t.pts[g][k];
-        float2 a = t.pts[g][t.prev[g][k]];
-        a = f2(j.offx + a.x, j.offy + a.y);
-        b = f2(j.offx + b.x, j.offy + b.y);
-        float2 pa[3], pb[3];
-        int np = clip_segment(a, b, j.width, j.height, pa, pb);
+        a = f2(lo(hi(a.x, 0.0f), j.width), lo(hi(a.y, 0.0f), j.height));
+        b = f2(lo(hi(b.x, 0.0f), j.width), lo(hi(b.y, 0.0f), j.height));
         int x0 = 0x7fffffff, x1 = -0x7fffffff, y0 = 0x7fffffff, y1 = -0x7fffffff;
         long long first = 0x7fffffffffffffffll;
-        for (int q = 0; q < np; ++q) {
-            dda_piece p;
-            if (!dda_setup(pa[q], pb[q], p)) continue;
+        dda_piece p;
+        if (dda_setup(a, b, p)) {
             int nrows = p.nrows < j.rows + 2 ? p.nrows : j.rows + 2;
             float2 entry = f2(p.fx, p.fy);
             for (int r = 0; r < nrows; ++r) {
@@ -313,25 +463,88 @@ __device__ void sort_runs(run *r, int n) {
     }
 }
 
-static constexpr int kRowCap = 256;   // runs per row sorted in shared memory
-static constexpr int kRowsWarps = 4;  // warps per block in k_rows
+static constexpr int kRowCap = 256;     // runs per row sorted by one warp in shared memory
+static constexpr int kRowsWarps = 8;    // warps per block in k_rows
+static constexpr int kLongCap = 8192;   // runs per row sorted by one block in k_rows_long
+static constexpr int kLongThreads = 512;
+static constexpr int kLongSmem = kLongCap * (sizeof(run) + sizeof(float));
+
+__device__ __forceinline__ run run_pad() { return run{0x7fffffff, 0.0f}; }
+
+// Coalesce a sorted row and store the running sum after each cell, in the
+// reference's float order (hpp:2243-2252 then the walk of hpp:2551-2605):
+// equal-x deltas are added in sorted order, then the cells are summed left
+// to right.  In place: the k-th coalesced cell is written after element k
+// has been read.  Returns the number of cells.
+__device__ __forceinline__ int coalesce_sum(run *v, float *acc, int m) {
+    if (m == 0) return 0;
+    run cur = v[0];
+    float sum = 0.0f;
+    int k = 0;
+    for (int i = 1; i < m; ++i) {
+        run u = v[i];
+        if (u.x == cur.x) {
+            cur.delta += u.delta;
+        } else {
+            sum += cur.delta;
+            v[k] = cur;
+            acc[k] = sum;
+            ++k;
+            cur = u;
+        }
+    }
+    sum += cur.delta;
+    v[k] = cur;
+    acc[k] = sum;
+    return k + 1;
+}
+
+// Bitonic sort of v[0, n2) (n2 a power of two) by run_less, `lanes` threads
+// with ids `id` cooperating; `sync` orders the steps.
+struct warp_sync {
+    __device__ void operator()() const { __syncwarp(); }
+};
+struct block_sync {
+    __device__ void operator()() const { __syncthreads(); }
+};
+
+template <class Sync>
+__device__ __forceinline__ void bitonic_sort(run *v, int n2, int id, int lanes, Sync sync) {
+    for (int k = 2; k <= n2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = id; i < (n2 >> 1); i += lanes) {
+                int lo_i = ((i & ~(j - 1)) << 1) | (i & (j - 1));
+                int hi_i = lo_i + j;
+                bool up = (lo_i & k) == 0;
+                run a = v[lo_i], b = v[hi_i];
+                if (run_less(b, a) == up) {
+                    v[lo_i] = b;
+                    v[hi_i] = a;
+                }
+            }
+            sync();
+        }
+    }
+}
 
 // Sort and coalesce one row's runs exactly as the reference does after its
 // std::sort (hpp:2243-2252), then store the running coverage sum after each
 // coalesced cell (the value render_main's walk holds from that cell on).
-// One warp per row: the row's nonzero runs are ranked in shared memory by
-// all lanes, then one lane coalesces and sums them in x order (the float
-// additions must follow the reference's order).  Rows longer than the
-// shared buffer are sorted in place by one lane.
+// One warp per row: the row's nonzero runs are compacted into shared memory
+// and bitonic-sorted by the warp, then one lane coalesces and sums them in x
+// order (the float additions must follow the reference's order).  Rows with
+// more than kRowCap nonzero runs are listed for k_rows_long.
 __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restrict__ row_off,
                                                           int32_t *__restrict__ row_cnt,
                                                           int32_t *__restrict__ row_cur, int32_t *__restrict__ row_len,
                                                           run *__restrict__ runs, float *__restrict__ sums,
-                                                          int total_rows) {
+                                                          int total_rows, int32_t *__restrict__ long_rows,
+                                                          int32_t *__restrict__ n_long) {
     __shared__ run buf[kRowsWarps][kRowCap];
-    __shared__ run srt[kRowsWarps][kRowCap];
+    __shared__ float acc[kRowsWarps][kRowCap];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int gw = blockIdx.x * kRowsWarps + w, nw = gridDim.x * kRowsWarps;
+    run *v = buf[w];
     for (int y = gw; y < total_rows; y += nw) {
         int cap = static_cast<int>(row_off[y + 1] - row_off[y]);
         int n = row_cur[y];
@@ -340,75 +553,131 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restr
         float *sm = sums + row_off[y];
         // Compact the nonzero runs.
         int m = 0;
-        bool fits = true;
         for (int base = 0; base < n; base += 32) {
             int i = base + lane;
-            run v = i < n ? r[i] : run{0, 0.0f};
-            bool keep = i < n && v.delta != 0.0f;
+            run u = i < n ? r[i] : run{0, 0.0f};
+            bool keep = i < n && u.delta != 0.0f;
             unsigned bal = __ballot_sync(0xffffffffu, keep);
             int at = m + __popc(bal & ((1u << lane) - 1u));
-            if (keep) {
-                if (at < kRowCap) buf[w][at] = v;
-                else r[at] = v;   // in place: at <= i always
-            }
+            if (keep && at < kRowCap) v[at] = u;
             m += __popc(bal);
-            if (m > kRowCap) fits = false;
         }
+        if (m > kRowCap) {
+            if (lane == 0) long_rows[atomicAdd(n_long, 1)] = y;
+            continue;
+        }
+        int n2 = 1;
+        while (n2 < m) n2 <<= 1;
+        for (int i = m + lane; i < n2; i += 32) v[i] = run_pad();
         __syncwarp();
-        if (fits) {
-            for (int i = lane; i < m; i += 32) {
-                run v = buf[w][i];
-                int rank = 0;
-                for (int j = 0; j < m; ++j) {
-                    run u = buf[w][j];
-                    rank += run_less(u, v) || (!run_less(v, u) && j < i);
-                }
-                srt[w][rank] = v;
-            }
-            __syncwarp();
-            if (lane == 0) {
-                int k = 0;
-                float sum = 0.0f;
-                for (int i = 0; i < m; ++i) {
-                    run v = srt[w][i];
-                    if (k > 0 && buf[w][k - 1].x == v.x) buf[w][k - 1].delta += v.delta;
-                    else buf[w][k++] = v;
-                }
-                for (int i = 0; i < k; ++i) {
-                    sum += buf[w][i].delta;
-                    srt[w][i].delta = sum;
-                }
-                m = k;
-            }
-            m = __shfl_sync(0xffffffffu, m, 0);
-            __syncwarp();
-            for (int i = lane; i < m; i += 32) {
-                r[i] = buf[w][i];
-                sm[i] = srt[w][i].delta;
-            }
-        } else if (lane == 0) {
-            // Long row: the first kRowCap compacted runs are in shared memory.
-            for (int i = 0; i < kRowCap; ++i) r[i] = buf[w][i];
-            sort_runs(r, m);
-            int k = 0;
-            for (int i = 0; i < m; ++i) {
-                if (k > 0 && r[k - 1].x == r[i].x) r[k - 1].delta += r[i].delta;
-                else r[k++] = r[i];
-            }
-            float sum = 0.0f;
-            for (int i = 0; i < k; ++i) {
-                sum += r[i].delta;
-                sm[i] = sum;
-            }
-            m = k;
-        }
+        if (n2 > 1) bitonic_sort(v, n2, lane, 32, warp_sync());
+        if (lane == 0) m = coalesce_sum(v, acc[w], m);
         m = __shfl_sync(0xffffffffu, m, 0);
+        __syncwarp();
+        for (int i = lane; i < m; i += 32) {
+            r[i] = v[i];
+            sm[i] = acc[w][i];
+        }
         if (lane == 0) {
             row_len[y] = m;
             row_cnt[y] = 0;
             row_cur[y] = 0;
         }
         __syncwarp();
+    }
+}
+
+// The rows k_rows listed: one block per row, sorted in shared memory when
+// they hold at most kLongCap nonzero runs, else in place by one thread.
+__global__ void __launch_bounds__(kLongThreads) k_rows_long(const int64_t *__restrict__ row_off,
+                                                           int32_t *__restrict__ row_cnt,
+                                                           int32_t *__restrict__ row_cur,
+                                                           int32_t *__restrict__ row_len, run *__restrict__ runs,
+                                                           float *__restrict__ sums,
+                                                           const int32_t *__restrict__ long_rows,
+                                                           const int32_t *__restrict__ n_long) {
+    extern __shared__ run lbuf[];   // kLongCap runs, then kLongCap floats
+    float *lacc = reinterpret_cast<float *>(lbuf + kLongCap);
+    __shared__ int warp_cnt[kLongThreads / 32];
+    __shared__ int total;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int count = *n_long;
+    for (int li = blockIdx.x; li < count; li += gridDim.x) {
+        const int y = long_rows[li];
+        int cap = static_cast<int>(row_off[y + 1] - row_off[y]);
+        int n = row_cur[y];
+        if (n > cap) n = cap;
+        run *r = runs + row_off[y];
+        float *sm = sums + row_off[y];
+        // Count the nonzero runs, then compact them in order.
+        int mine = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) mine += r[i].delta != 0.0f;
+        for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+        if (lane == 0) warp_cnt[w] = mine;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int i = 0; i < kLongThreads / 32; ++i) t += warp_cnt[i];
+            total = t;
+        }
+        __syncthreads();
+        const int m = total;
+        int kept = m;
+        if (m <= kLongCap) {
+            int base = 0;
+            for (int b0 = 0; b0 < n; b0 += blockDim.x) {
+                int i = b0 + threadIdx.x;
+                run u = i < n ? r[i] : run{0, 0.0f};
+                bool keep = i < n && u.delta != 0.0f;
+                unsigned bal = __ballot_sync(0xffffffffu, keep);
+                if (lane == 0) warp_cnt[w] = __popc(bal);
+                __syncthreads();
+                int before = 0, all = 0;
+                for (int q = 0; q < kLongThreads / 32; ++q) {
+                    before += q < w ? warp_cnt[q] : 0;
+                    all += warp_cnt[q];
+                }
+                if (keep) lbuf[base + before + __popc(bal & ((1u << lane) - 1u))] = u;
+                base += all;
+                __syncthreads();
+            }
+            int n2 = 1;
+            while (n2 < m) n2 <<= 1;
+            for (int i = m + threadIdx.x; i < n2; i += blockDim.x) lbuf[i] = run_pad();
+            __syncthreads();
+            if (n2 > 1) bitonic_sort(lbuf, n2, threadIdx.x, blockDim.x, block_sync());
+            if (threadIdx.x == 0) total = coalesce_sum(lbuf, lacc, m);
+            __syncthreads();
+            kept = total;
+            for (int i = threadIdx.x; i < kept; i += blockDim.x) {
+                r[i] = lbuf[i];
+                sm[i] = lacc[i];
+            }
+        } else if (threadIdx.x == 0) {
+            int k = 0;
+            for (int i = 0; i < n; ++i)
+                if (r[i].delta != 0.0f) r[k++] = r[i];
+            sort_runs(r, k);
+            int c = 0;
+            float sum = 0.0f;
+            for (int i = 0; i < k; ++i) {
+                if (c > 0 && r[c - 1].x == r[i].x) {
+                    r[c - 1].delta += r[i].delta;
+                } else {
+                    if (c > 0) sm[c - 1] = (sum += r[c - 1].delta);
+                    r[c++] = r[i];
+                }
+            }
+            if (c > 0) sm[c - 1] = (sum += r[c - 1].delta);
+            total = c;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            row_len[y] = total;
+            row_cnt[y] = 0;
+            row_cur[y] = 0;
+        }
+        __syncthreads();
     }
 }
 
@@ -456,8 +725,13 @@ __global__ void k_paint(paint_args a) {
         if (!clearing && n == 0) continue;
         const run *r = a.rv.runs + a.rv.row_off[row];
         const float *sm = a.rv.sums + a.rv.row_off[row];
+        // The reference walks the path runs merged with the clip runs, so
+        // after the last path run it keeps painting with the row's final
+        // sum up to the clip's end (hpp:2572-2600): that matters when the
+        // float sum is left above the visibility threshold.
         int xs = clearing ? 0 : r[0].x;
-        int xe = clearing ? a.W - 1 : min(r[n - 1].x, a.W - 1);
+        bool tail = lo(fabsf(sm[n - 1]), 1.0f) >= kVisible;
+        int xe = clearing || tail ? a.W - 1 : min(r[n - 1].x, a.W - 1);
         for (int x = xs + lane; x <= xe; x += 32) {
             float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
             float vis = a.vis ? a.vis[static_cast<size_t>(y) * a.W + x] : 1.0f;

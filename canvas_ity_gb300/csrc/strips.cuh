@@ -146,7 +146,9 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
                     j = 0;
                     carry = 0.0f;
                     first_x = n ? r[0].x : 0x7fffffff;
-                    last_x = n ? r[n - 1].x : -1;
+                    // Past the last run the row's final sum still paints
+                    // up to the clip's end when it is visible (see k_paint).
+                    last_x = n ? (lo(fabsf(sm[n - 1]), 1.0f) >= kVisible ? W - 1 : r[n - 1].x) : -1;
                 }
                 int xs = clearing ? 0 : first_x;
                 int xe = clearing ? W - 1 : min(last_x, W - 1);

@@ -213,6 +213,7 @@ class Record:
     args: Tuple
     data: bytes = b""          # variable payload (pixels, font, text, dash)
     expected: Optional[bytes] = None  # recorded get_image_data output
+    span: Tuple[int, int] = (0, 0)    # byte range of the record in the raw call list
 
 
 @dataclass
@@ -255,6 +256,7 @@ def parse(buf: bytes) -> Trace:
         raise ValueError("not a canvas call list")
     trace: Optional[Trace] = None
     while True:
+        start = at
         (op,), at = _read(buf, at, "i")
         if op == END:
             break
@@ -303,9 +305,20 @@ def parse(buf: bytes) -> Trace:
             raise ValueError(f"unknown opcode {op}")
         if trace is None:
             raise ValueError("trace does not start with a canvas")
+        rec.span = (start, at)
         trace.records.append(rec)
     assert trace is not None
     return trace
+
+
+def prefix(buf: bytes, n_records: int) -> bytes:
+    """The call list cut after its first `n_records` records (the canvas
+    record counts as one), ended again."""
+    if buf[:2] in (b"\x78\x9c", b"\x78\xda", b"\x78\x01"):
+        buf = zlib.decompress(buf)
+    recs = parse(buf).records
+    end = recs[min(n_records, len(recs)) - 1].span[1] if n_records > 0 else 8
+    return buf[:end] + _i(END)
 
 
 def canvas_size(buf: bytes) -> Tuple[int, int]:

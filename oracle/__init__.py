@@ -18,6 +18,9 @@ from typing import List, Optional, Tuple
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 ORACLE_SO = os.path.join(BUILD_DIR, "libcy_oracle.so")
+# Same restatement with equal-magnitude, opposite-sign runs of a cell ordered
+# negative first (the GPU's order) instead of std::sort's own choice.
+ORACLE_SIGN_SO = os.path.join(BUILD_DIR, "libcy_oracle_sign.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libcy_ref.so")
 REFERENCE_ROOT = os.environ.get("CY_REFERENCE_ROOT", "/root/reference")
@@ -25,18 +28,22 @@ REFERENCE_ROOT = os.environ.get("CY_REFERENCE_ROOT", "/root/reference")
 _FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
 
 
-def build(force: bool = False) -> str:
-    """Compile the oracle restatement (fast: one translation unit)."""
+def build(force: bool = False, ties: str = "reference") -> str:
+    """Compile the oracle restatement (fast: one translation unit).
+
+    ties="sign" builds the variant whose sort orders equal-magnitude,
+    opposite-sign runs of one cell negative first."""
     src = os.path.join(HERE, "cy_oracle.cpp")
+    out, extra = (ORACLE_SIGN_SO, ["-DCYO_TIES_BY_SIGN"]) if ties == "sign" else (ORACLE_SO, [])
     hdrs = [os.path.join(HERE, "..", "include", h) for h in ("cy_trace.h", "cy_replay.hpp")]
     newest = max(os.path.getmtime(p) for p in [src] + hdrs)
-    if not force and os.path.exists(ORACLE_SO) and os.path.getmtime(ORACLE_SO) >= newest:
-        return ORACLE_SO
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return out
     os.makedirs(BUILD_DIR, exist_ok=True)
-    tmp = ORACLE_SO + ".tmp"
-    subprocess.check_call(["g++", *_FLAGS, "-o", tmp, src])
-    os.replace(tmp, ORACLE_SO)
-    return ORACLE_SO
+    tmp = out + ".tmp"
+    subprocess.check_call(["g++", *_FLAGS, *extra, "-o", tmp, src])
+    os.replace(tmp, out)
+    return out
 
 
 def build_reference(force: bool = False) -> Optional[str]:
@@ -72,25 +79,25 @@ class _Lib:
             return img.raw[: n_img.value], [res[i] for i in range(n_res.value)]
 
 
-_oracle: Optional[_Lib] = None
+_oracles: dict = {}
 _ref: Optional[_Lib] = None
 
 
-def replay(trace: bytes) -> Tuple[bytes, List[float]]:
+def _get(ties: str) -> _Lib:
+    if ties not in _oracles:
+        _oracles[ties] = _Lib(build(ties=ties), "cyo_replay")
+    return _oracles[ties]
+
+
+def replay(trace: bytes, ties: str = "reference") -> Tuple[bytes, List[float]]:
     """Replay through the oracle: (concatenated get_image_data bytes, results)."""
-    global _oracle
-    if _oracle is None:
-        _oracle = _Lib(build(), "cyo_replay")
-    return _oracle.replay(trace)
+    return _get(ties).replay(trace)
 
 
-def replay_linear(trace: bytes, width: int, height: int):
+def replay_linear(trace: bytes, width: int, height: int, ties: str = "reference"):
     """Replay through the oracle; return the final float canvas (H, W, 4)."""
     import numpy as np
-    global _oracle
-    if _oracle is None:
-        _oracle = _Lib(build(), "cyo_replay")
-    fn = _oracle.lib.cyo_replay_linear
+    fn = _get(ties).lib.cyo_replay_linear
     fn.restype = ctypes.c_int
     fn.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t,
                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]

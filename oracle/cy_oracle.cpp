@@ -110,10 +110,17 @@ struct subpath { size_t count; bool closed; };
 struct polyline { std::vector<vec2> pts; std::vector<subpath> subs; };
 struct run { unsigned short x, y; float delta; };
 
-// Sort order of runs (hpp:2172-2181).
+// Sort order of runs (hpp:2172-2181).  Runs of one cell with equal
+// magnitude and opposite sign are equivalent under it, so std::sort leaves
+// their order to its own partitioning.  Built with CYO_TIES_BY_SIGN the
+// oracle orders them negative first instead, which is the order the GPU
+// path uses; that build pins the GPU's float canvas bit for bit.
 static bool run_before(const run &l, const run &r) {
     if (l.y != r.y) return l.y < r.y;
     if (l.x != r.x) return l.x < r.x;
+#ifdef CYO_TIES_BY_SIGN
+    if (fabsf(l.delta) == fabsf(r.delta)) return l.delta < r.delta;
+#endif
     return fabsf(l.delta) < fabsf(r.delta);
 }
 

@@ -78,6 +78,35 @@ def test_c2_size_vs_oracle(engine):
     assert_images_close(got, want, "c2/60")
 
 
+def assert_float_canvas_exact(tb, what):
+    """The GPU's final premultiplied linear canvas equals, bit for bit, the
+    oracle built with the GPU's order for runs of one cell that the
+    reference's sort leaves unordered (equal magnitude, opposite sign)."""
+    w, h = T.canvas_size(tb)
+    got = native.replay_linear(tb, w, h)
+    want = oracle.replay_linear(tb, w, h, ties="sign")
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, f"{what}: {len(bad)} float values differ, first at (y, x, c) = {bad[0].tolist()}"
+
+
+@pytest.mark.parametrize("entry", MANIFEST, ids=[e["name"] for e in MANIFEST])
+def test_float_canvas_bit_exact_reference_suite(engine, entry):
+    assert_float_canvas_exact(G.load_fixture(entry), entry["name"])
+
+
+@pytest.mark.parametrize("config", ["c0_small", "c1_small", "c2_small", "mixed_small"])
+@pytest.mark.parametrize("seed", range(3))
+def test_float_canvas_bit_exact_seeded(engine, config, seed):
+    assert_float_canvas_exact(scenes.small_scene(config, seed), f"{config}/{seed}")
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_float_canvas_bit_exact_batched_workload(engine, seed):
+    """Canvases of the many-canvas workload (random size, 8-128 paths of the
+    c0/c1/c2 mixture, global transform)."""
+    assert_float_canvas_exact(scenes.c3_canvas(seed), f"c3 canvas {seed}")
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_float_coverage(engine, seed):
     """One opaque white nonzero fill on a blank canvas: the linear alpha is the
