@@ -1421,6 +1421,58 @@ int cy_read_linear(cy_ctx *c, float *out) {
     return CY_OK;
 }
 
+// ------------------------------------------- allocation-free image readback
+// cy_get_image_noalloc: the RGBA8 conversion of cy_get_image with its device
+// staging buffer replaced by one fixed array in this file, so the call makes
+// no allocation of any kind.  The array lives in every GPU that loads this
+// library, until the process exits.
+static __device__ __align__(256) uchar4 g_noalloc_rgba[CY_GET_IMAGE_NOALLOC_MAX_PIXELS];
+
+namespace {
+std::mutex g_noalloc_lock;             // serialises the calls of this process
+constexpr int kNoallocDevices = 64;
+uchar4 *g_noalloc_addr[kNoallocDevices] = {};   // device address of the array, per device
+}  // namespace
+
+extern "C" int cy_get_image_noalloc(cy_ctx *c, unsigned char *image, int w, int h, int stride, int x, int y) {
+    if (!c || !image || w <= 0 || h <= 0) return CY_EINVAL;
+    if (static_cast<int64_t>(w) * h > CY_GET_IMAGE_NOALLOC_MAX_PIXELS) return CY_EINVAL;
+    if (static_cast<int64_t>(stride) < static_cast<int64_t>(w) * 4) return CY_EINVAL;
+    if (c->status) return c->status;
+    // Queued draws would need a frame run, which allocates: flush them first.
+    if (!c->q.cmds.empty()) return CY_EINVAL;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocDevices) {
+        cudaGetLastError();
+        return CY_ENODEV;
+    }
+    std::lock_guard<std::mutex> hold(g_noalloc_lock);
+    if (!g_noalloc_addr[dev]) {
+        // Set-up, once per device, with that device current: host code must
+        // use the array's device address, not its host-side name.
+        void *addr = nullptr;
+        if (cudaGetSymbolAddress(&addr, g_noalloc_rgba) != cudaSuccess || !addr) {
+            cudaGetLastError();
+            return CY_ECUDA;
+        }
+        g_noalloc_addr[dev] = static_cast<uchar4 *>(addr);
+    }
+    uchar4 *staging = g_noalloc_addr[dev];
+    // k_get writes every pixel of the w x h rectangle (zero outside the
+    // canvas), so nothing in the array has to start at zero.
+    dim3 blk(32, 32), grd((w + 31) / 32, (h + 31) / 32);
+    k_get<<<grd, blk, 0, c->stream>>>(c->bitmap, c->W, c->H, staging, w, h, x, y);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpy2DAsync(image, static_cast<size_t>(stride), staging, static_cast<size_t>(w) * 4,
+                          static_cast<size_t>(w) * 4, static_cast<size_t>(h), cudaMemcpyDeviceToHost,
+                          c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return c->fail(CY_ECUDA);
+    }
+    return CY_OK;
+}
+
 // ------------------------------------------------------------ batched API
 struct cy_frame {
     std::unique_ptr<frame> f;

@@ -113,6 +113,32 @@ int cy_read_linear(cy_ctx *ctx, float *out);
 /* Run all queued work and wait for it. */
 int cy_flush(cy_ctx *ctx);
 
+/* Largest rectangle cy_get_image_noalloc reads: 1024 x 1024 pixels (a
+ * 4 MiB device array that every GPU loading this library keeps until exit). */
+#define CY_GET_IMAGE_NOALLOC_MAX_PIXELS (1024 * 1024)
+
+/* No counterpart in the reference.  get_image_data for callers that must
+ * not allocate: code running under a memory pool or budget it does not own
+ * (a serving loop admitting work against a fixed HBM budget, a host program
+ * whose GPU memory is reserved by another framework), or on a latency path
+ * where cudaMalloc/cudaFree would stall other streams while the device
+ * synchronises.  Converts the canvas as of its last flush exactly like
+ * cy_get_image, staging in one fixed device array instead of allocated
+ * memory, and calls no allocating routine.
+ *   - Call with the context's device current.  The first call on a device
+ *     looks up the array's device address (cudaGetSymbolAddress); make that
+ *     first call before any stream capture on the device.
+ *   - Fails with CY_EINVAL when width*height exceeds
+ *     CY_GET_IMAGE_NOALLOC_MAX_PIXELS, when stride < 4*width, or when the
+ *     context still holds queued commands (run cy_flush first: a flush may
+ *     allocate).  Returns when the pixels are in `image`.
+ *   - All calls share the array.  Each call writes every pixel it copies
+ *     back, so no part of the array has to start at zero.  Calls from the
+ *     threads of one process are serialised by a lock and each waits for
+ *     its copy; calls whose kernels and copies overlapped on the GPU would
+ *     race on the array. */
+int cy_get_image_noalloc(cy_ctx *ctx, unsigned char *image, int width, int height, int stride, int x, int y);
+
 /* First failure seen by the context (0 if none). */
 int cy_ctx_status(const cy_ctx *ctx);
 
