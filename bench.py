@@ -297,14 +297,18 @@ def gpu_arm(args, world, rank, local):
     # End to end through the public C ABI, host buffers, every step.
     t_e2e = 0.0
     h2d = d2h = 0
+    e2e_parts = {}
     for i in range(args.e2e_steps):
         t0 = time.perf_counter()
         f = native.Frame(traces, 0)
         st = f.stats()
         outs = f.finish()
+        t_close = time.perf_counter()
         f.close()
         t_e2e += time.perf_counter() - t0
         h2d, d2h = st["upload_bytes"], sum(len(o) for o in outs)
+        for k, v in list(f.timing.items()) + [("close_s", time.perf_counter() - t_close)]:
+            e2e_parts[k] = e2e_parts.get(k, 0.0) + v / args.e2e_steps
     e2e_s = reduce_max(t_e2e / max(args.e2e_steps, 1), world, backend)
     e2e = px_all / e2e_s / 1e6 if e2e_s > 0 else None
     # Plain per-canvas path on a sample of the same canvases.
@@ -359,7 +363,8 @@ def gpu_arm(args, world, rank, local):
                    "clips": stats["clips"], "l2": "inputs larger than L2 (runs and outputs are GBs)",
                    "parallelism": f"replicas x{world}", "generate_s": round(gen_s, 1)},
         "e2e": {"value": round(e2e, 2) if e2e else None, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h, "host_threads": cores,
+                "parts_s": {k: round(v, 4) for k, v in e2e_parts.items()}},
         "plain_per_canvas": {"value": round(plain, 2) if plain else None, "unit": "Mpix/s",
                              "sample_canvases": len(sample)},
         "batched_over_plain": round(value / plain, 2) if plain else None,

@@ -1,8 +1,11 @@
 // capi.cpp -- flat C binding of canvas_ity::canvas and the call-list replay
 // entry point (include/canvas_ity_c.h).
+#include <atomic>
 #include <cstring>
 #include <memory>
 #include <new>
+#include <thread>
+#include <vector>
 
 #include "../../include/canvas_ity.hpp"
 #include "../../include/canvas_ity_c.h"
@@ -179,5 +182,49 @@ cy_canvas *cy_canvas_from_trace(const void *trace, size_t trace_len, int *status
 }
 
 void *cy_canvas_ctx(cy_canvas *c) { return c ? c->get().gpu_context() : nullptr; }
+
+int cy_canvases_from_traces(const void *const *traces, const size_t *lens, int n, int engine, int threads,
+                            cy_canvas **out) {
+    if (n < 0 || (n > 0 && (!traces || !lens || !out))) return CY_EINVAL;
+    for (int i = 0; i < n; ++i) out[i] = nullptr;
+    if (n == 0) return CY_OK;
+    if (threads <= 0) threads = static_cast<int>(std::thread::hardware_concurrency());
+    if (threads < 1) threads = 1;
+    if (threads > n) threads = n;
+    if (threads > 256) threads = 256;
+    std::atomic<int> next(0), failure(0);
+    // Each canvas is an independent instance (as in the reference, separate
+    // canvases may be used from different threads), so the host halves of the
+    // replays run side by side; their device contexts only queue work.
+    auto work = [&]() {
+        cy_set_engine(engine);
+        for (;;) {
+            int i = next.fetch_add(1);
+            if (i >= n) break;
+            int st = 0;
+            out[i] = cy_canvas_from_trace(traces[i], lens[i], &st);
+            if (!out[i]) {
+                int none = 0;
+                failure.compare_exchange_strong(none, st ? st : CY_EINVAL);
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    try {
+        for (int t = 1; t < threads; ++t) pool.emplace_back(work);
+    } catch (...) {
+        // fewer threads than asked: the ones started and this one finish the work
+    }
+    work();
+    for (std::thread &t : pool) t.join();
+    int rc = failure.load();
+    if (rc) {
+        for (int i = 0; i < n; ++i) {
+            delete out[i];
+            out[i] = nullptr;
+        }
+    }
+    return rc;
+}
 
 }  // extern "C"

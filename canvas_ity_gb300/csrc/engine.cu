@@ -25,6 +25,8 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <thread>
+#include <atomic>
 #include <vector>
 
 #include "../../include/cy_gpu.h"
@@ -171,7 +173,10 @@ struct frame {
     int status = 0;
     std::vector<cy_ctx *> cvs;
     // combined host data
-    queue all;
+    queue all;                 // commands and reads of all contexts (geometry stays in their queues)
+    struct ctx_base { int32_t hpts, bez, items, stop, tex; int64_t put; };
+    std::vector<ctx_base> bases;   // where each context's geometry lands in the arena
+    int64_t n_hpts = 0, n_bez = 0, n_items_all = 0, n_stop = 0, n_tex = 0, n_put = 0;
     std::vector<int32_t> cmd_cv;
     int64_t get_total = 0;
     std::vector<scan_job> jobs;
@@ -217,6 +222,8 @@ struct frame {
         status = 0;
         cvs.clear();
         all.clear();
+        bases.clear();
+        n_hpts = n_bez = n_items_all = n_stop = n_tex = n_put = 0;
         cmd_cv.clear();
         get_total = 0;
         jobs.clear();
@@ -271,6 +278,7 @@ struct frame {
     template <class In> int scan64(const In *in, int64_t *out, int n);
     int clip_passes(job_tables &t);
     void gather();
+    void stage(char *h);
     int prepare();
     int run();
     int finish();
@@ -405,34 +413,30 @@ int frame::scan64(const In *in, int64_t *out, int n) {
 
 // Concatenate the queues of every canvas of the frame, rebasing indices.
 void frame::gather() {
+    bases.resize(cvs.size());
     for (size_t ci = 0; ci < cvs.size(); ++ci) {
         queue &q = cvs[ci]->q;
-        int32_t b_hpts = static_cast<int32_t>(all.host_pts.size());
-        int32_t b_bez = static_cast<int32_t>(all.bez_pts.size());
-        int32_t b_items = static_cast<int32_t>(all.items.size());
-        int32_t b_stop = static_cast<int32_t>(all.stop_off.size());
-        int32_t b_tex = static_cast<int32_t>(all.texels.size());
-        int64_t b_put = static_cast<int64_t>(all.put_px.size());
-        all.host_pts.insert(all.host_pts.end(), q.host_pts.begin(), q.host_pts.end());
-        for (int32_t v : q.host_prev) all.host_prev.push_back(v + b_hpts);
-        all.bez_pts.insert(all.bez_pts.end(), q.bez_pts.begin(), q.bez_pts.end());
-        for (flat_item it : q.items) {
-            it.pt += b_bez;
-            if (it.sub_end >= 0) it.sub_end += b_items;
-            all.items.push_back(it);
-        }
-        all.stop_off.insert(all.stop_off.end(), q.stop_off.begin(), q.stop_off.end());
-        all.stop_col.insert(all.stop_col.end(), q.stop_col.begin(), q.stop_col.end());
-        all.texels.insert(all.texels.end(), q.texels.begin(), q.texels.end());
-        all.put_px.insert(all.put_px.end(), q.put_px.begin(), q.put_px.end());
+        ctx_base &b = bases[ci];
+        b.hpts = static_cast<int32_t>(n_hpts);
+        b.bez = static_cast<int32_t>(n_bez);
+        b.items = static_cast<int32_t>(n_items_all);
+        b.stop = static_cast<int32_t>(n_stop);
+        b.tex = static_cast<int32_t>(n_tex);
+        b.put = n_put;
+        n_hpts += static_cast<int64_t>(q.host_pts.size());
+        n_bez += static_cast<int64_t>(q.bez_pts.size());
+        n_items_all += static_cast<int64_t>(q.items.size());
+        n_stop += static_cast<int64_t>(q.stop_off.size());
+        n_tex += static_cast<int64_t>(q.texels.size());
+        n_put += static_cast<int64_t>(q.put_px.size());
         for (size_t k = 0; k < q.cmds.size(); ++k) {
             command c = q.cmds[k];
             if (c.kind == CMD_FILL || c.kind == CMD_CLIP) {
-                c.first += c.geom == 0 ? b_hpts : b_items;
-                c.stop_first += b_stop;
-                c.pat_first += b_tex;
+                c.first += c.geom == 0 ? b.hpts : b.items;
+                c.stop_first += b.stop;
+                c.pat_first += b.tex;
             } else if (c.kind == CMD_PUT) {
-                c.put_first += b_put;
+                c.put_first += b.put;
             } else if (c.kind == CMD_GET) {
                 c.get_out += get_total;
             }
@@ -445,6 +449,58 @@ void frame::gather() {
         all.get_stride.insert(all.get_stride.end(), q.get_stride.begin(), q.get_stride.end());
         get_total += q.get_bytes;
     }
+}
+
+// Copy every context's geometry, stops, texels and put pixels into the
+// staging buffer at its place in the arena, contexts spread over host threads.
+void frame::stage(char *h) {
+    auto copy_ctx = [&](size_t ci) {
+        const queue &q = cvs[ci]->q;
+        const ctx_base &b = bases[ci];
+        if (!q.host_pts.empty())
+            std::memcpy(h + o_hpts + static_cast<size_t>(b.hpts) * sizeof(float2), q.host_pts.data(),
+                        q.host_pts.size() * sizeof(float2));
+        int32_t *prev = reinterpret_cast<int32_t *>(h + o_hprev) + b.hpts;
+        for (size_t k = 0; k < q.host_prev.size(); ++k) prev[k] = q.host_prev[k] + b.hpts;
+        if (!q.bez_pts.empty())
+            std::memcpy(h + o_bez + static_cast<size_t>(b.bez) * sizeof(float2), q.bez_pts.data(),
+                        q.bez_pts.size() * sizeof(float2));
+        flat_item *items = reinterpret_cast<flat_item *>(h + o_items) + b.items;
+        for (size_t k = 0; k < q.items.size(); ++k) {
+            flat_item it = q.items[k];
+            it.pt += b.bez;
+            if (it.sub_end >= 0) it.sub_end += b.items;
+            items[k] = it;
+        }
+        if (!q.stop_off.empty()) {
+            std::memcpy(h + o_soff + static_cast<size_t>(b.stop) * sizeof(float), q.stop_off.data(),
+                        q.stop_off.size() * sizeof(float));
+            std::memcpy(h + o_scol + static_cast<size_t>(b.stop) * sizeof(float4), q.stop_col.data(),
+                        q.stop_col.size() * sizeof(float4));
+        }
+        if (!q.texels.empty())
+            std::memcpy(h + o_tex + static_cast<size_t>(b.tex) * sizeof(uchar4), q.texels.data(),
+                        q.texels.size() * sizeof(uchar4));
+        if (!q.put_px.empty())
+            std::memcpy(h + o_put + static_cast<size_t>(b.put), q.put_px.data(), q.put_px.size());
+    };
+    size_t n = cvs.size();
+    int threads = static_cast<int>(std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 16));
+    if (n < 64 || threads <= 1) {
+        for (size_t ci = 0; ci < n; ++ci) copy_ctx(ci);
+        return;
+    }
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+        for (size_t ci = next.fetch_add(1); ci < n; ci = next.fetch_add(1)) copy_ctx(ci);
+    };
+    std::vector<std::thread> pool;
+    try {
+        for (int t = 1; t < threads; ++t) pool.emplace_back(work);
+    } catch (...) {
+    }
+    work();
+    for (std::thread &t : pool) t.join();
 }
 
 // Whether a job's points (command bounds moved by the job's offset) can fall
@@ -468,25 +524,20 @@ int frame::prepare() {
     // Arena: everything queued goes up in one copy.
     o_cmd = 0;
     o_hpts = align256(o_cmd + cmds.size() * sizeof(command));
-    o_hprev = align256(o_hpts + all.host_pts.size() * sizeof(float2));
-    o_bez = align256(o_hprev + all.host_prev.size() * sizeof(int32_t));
-    o_items = align256(o_bez + all.bez_pts.size() * sizeof(float2));
-    o_soff = align256(o_items + all.items.size() * sizeof(flat_item));
-    o_scol = align256(o_soff + all.stop_off.size() * sizeof(float));
-    o_tex = align256(o_scol + all.stop_col.size() * sizeof(float4));
-    o_put = align256(o_tex + all.texels.size() * sizeof(uchar4));
-    size_t total = align256(o_put + all.put_px.size());
+    o_hprev = align256(o_hpts + static_cast<size_t>(n_hpts) * sizeof(float2));
+    o_bez = align256(o_hprev + static_cast<size_t>(n_hpts) * sizeof(int32_t));
+    o_items = align256(o_bez + static_cast<size_t>(n_bez) * sizeof(float2));
+    o_soff = align256(o_items + static_cast<size_t>(n_items_all) * sizeof(flat_item));
+    o_scol = align256(o_soff + static_cast<size_t>(n_stop) * sizeof(float));
+    o_tex = align256(o_scol + static_cast<size_t>(n_stop) * sizeof(float4));
+    o_put = align256(o_tex + static_cast<size_t>(n_tex) * sizeof(uchar4));
+    size_t total = align256(o_put + static_cast<size_t>(n_put));
+    if (n_hpts > INT32_MAX / 2 || n_bez > INT32_MAX / 2 || n_items_all > INT32_MAX / 2 || n_stop > INT32_MAX / 2 ||
+        n_tex > INT32_MAX / 2)
+        return fail(CY_ENOMEM, __LINE__);
     if (!arena.ensure(total) || !staging.ensure(total)) return fail(CY_ENOMEM, __LINE__);
     char *h = static_cast<char *>(staging.p);
-    auto put = [&](size_t off, const void *src, size_t n) { if (n) std::memcpy(h + off, src, n); };
-    put(o_hpts, all.host_pts.data(), all.host_pts.size() * sizeof(float2));
-    put(o_hprev, all.host_prev.data(), all.host_prev.size() * sizeof(int32_t));
-    put(o_bez, all.bez_pts.data(), all.bez_pts.size() * sizeof(float2));
-    put(o_items, all.items.data(), all.items.size() * sizeof(flat_item));
-    put(o_soff, all.stop_off.data(), all.stop_off.size() * sizeof(float));
-    put(o_scol, all.stop_col.data(), all.stop_col.size() * sizeof(float4));
-    put(o_tex, all.texels.data(), all.texels.size() * sizeof(uchar4));
-    put(o_put, all.put_px.data(), all.put_px.size());
+    stage(h);
     d = static_cast<char *>(arena.p);
     if (total > o_hpts && !ok(cudaMemcpyAsync(d + o_hpts, h + o_hpts, total - o_hpts, cudaMemcpyHostToDevice, stream)))
         return status;
@@ -495,7 +546,7 @@ int frame::prepare() {
     if (!ok(cudaMemcpyAsync(lut_dev.p, linear_lut_host(), 256 * sizeof(float), cudaMemcpyHostToDevice, stream)))
         return status;
     // Flattening counts size the polyline store (one read-back).
-    int n_items = static_cast<int>(all.items.size());
+    int n_items = static_cast<int>(n_items_all);
     const int32_t *offs_h = nullptr;
     if (n_items > 0) {
         if (!item_cnt.ensure(static_cast<size_t>(n_items + 1) * 4) ||
@@ -665,14 +716,14 @@ int frame::run() {
     src.stop_off = reinterpret_cast<const float *>(d + o_soff);
     src.stop_col = reinterpret_cast<const float4 *>(d + o_scol);
     src.texels = nullptr;
-    if (!all.texels.empty()) {
-        if (!pat_f4.ensure(all.texels.size() * sizeof(float4))) return fail(CY_ENOMEM, __LINE__);
-        int n = static_cast<int>(all.texels.size());
+    if (n_tex > 0) {
+        if (!pat_f4.ensure(static_cast<size_t>(n_tex) * sizeof(float4))) return fail(CY_ENOMEM, __LINE__);
+        int n = static_cast<int>(n_tex);
         k_pattern_prep<<<(n + 255) / 256, 256, 0, stream>>>(reinterpret_cast<const uchar4 *>(d + o_tex),
                                                             pat_f4.as<float4>(), n, lut);
         src.texels = pat_f4.as<float4>();
     }
-    int n_items_flat = static_cast<int>(all.items.size());
+    int n_items_flat = static_cast<int>(n_items_all);
     if (n_items_flat > 0) {
         const int32_t *offs_h = static_cast<const int32_t *>(offs_host.p);
         int64_t nflat = offs_h[n_items_flat];
@@ -680,7 +731,7 @@ int frame::run() {
                                                                     item_off.as<int32_t>(), flat_pts.as<float2>(),
                                                                     flat_prev.as<int32_t>(), nflat);
     }
-    if (!all.texels.empty()) ++launches;
+    if (n_tex > 0) ++launches;
     if (n_items_flat > 0) ++launches;
     mark();   // 1: patterns and flattening done
     size_t nr = static_cast<size_t>(total_rows);
@@ -1115,7 +1166,44 @@ bool valid_counts(const int *counts, int n, size_t &total) {
     return total < (static_cast<size_t>(1) << 30);
 }
 
-int queue_geometry(queue &q, const float *points, const int *counts, int n_sub, bool bezier, command &cmd) {
+// The rectangles a command's geometry is scanned against: the canvas, and
+// for a shadow the padded canvas with the points moved by the shadow offset.
+struct cull_rects {
+    float w, h;
+    bool shadow;
+    float sw, sh, sx, sy;
+};
+
+// Whether the Sutherland-Hodgman clip (hpp:2204-2235) leaves nothing of a
+// polygon in every rectangle of the command.  The clip's passes run in the
+// order x >= 0, y >= 0, x <= w, y <= h: a polygon wholly beyond the edge of
+// a pass loses all its points there, provided every earlier pass returned it
+// unchanged (wholly inside its edge; a crossing would add points whose
+// rounding is not bounded by the polygon's).  The comparisons are the
+// clip's own; `margin` widens them for control polygons, whose flattened
+// points may stray from the hull by rounding.
+bool culled(const float2 *p, int n, const cull_rects &r, float margin) {
+    auto empty = [&](float ox, float oy, float w, float h) {
+        for (int e = 0; e < 4; ++e) {
+            bool out = true, in = true;
+            for (int k = 0; k < n && (out || in); ++k) {
+                float x = ox + p[k].x, y = oy + p[k].y;
+                float d = e == 0 ? x : e == 1 ? y : e == 2 ? w - x : h - y;
+                out = out && d < -margin;
+                in = in && d >= margin;
+            }
+            if (out) return true;
+            if (!in) return false;
+        }
+        return false;
+    };
+    if (n <= 0) return true;
+    if (!empty(0.0f, 0.0f, r.w, r.h)) return false;
+    return !r.shadow || empty(r.sx, r.sy, r.sw, r.sh);
+}
+
+int queue_geometry(queue &q, const float *points, const int *counts, int n_sub, bool bezier, command &cmd,
+                   const cull_rects &rects) {
     size_t total = 0;
     if (n_sub < 0 || (n_sub > 0 && (!counts || !points)) || !valid_counts(counts, n_sub, total))
         return CY_EINVAL;
@@ -1124,18 +1212,21 @@ int queue_geometry(queue &q, const float *points, const int *counts, int n_sub, 
     if (!bezier) {
         cmd.geom = 0;
         cmd.first = static_cast<int32_t>(q.host_pts.size());
-        cmd.count = static_cast<int32_t>(total);
-        size_t at = 0;
+        size_t at = 0, kept = 0;
         for (int s = 0; s < n_sub; ++s) {
             int32_t base = static_cast<int32_t>(q.host_pts.size());
             int n = counts[s];
-            for (int k = 0; k < n; ++k) {
-                q.host_pts.push_back(p[at + k]);
-                q.host_prev.push_back(k == 0 ? base + n - 1 : base + k - 1);
+            if (!culled(p + at, n, rects, 0.0f)) {
+                for (int k = 0; k < n; ++k) {
+                    q.host_pts.push_back(p[at + k]);
+                    q.host_prev.push_back(k == 0 ? base + n - 1 : base + k - 1);
+                }
+                kept += n;
             }
             at += n;
         }
-        q.bytes += total * 12;
+        cmd.count = static_cast<int32_t>(kept);
+        q.bytes += kept * 12;
         return CY_OK;
     }
     // Bezier path: one flattening item per subpath start and per cubic.
@@ -1149,6 +1240,12 @@ int queue_geometry(queue &q, const float *points, const int *counts, int n_sub, 
     for (int s = 0; s < n_sub; ++s) {
         int n = counts[s];
         if (n == 0) continue;
+        float big = 0.0f;
+        for (int k = 0; k < n; ++k) big = std::max(big, std::max(std::fabs(p[at + k].x), std::fabs(p[at + k].y)));
+        if (culled(p + at, n, rects, 1.0f + 1.0e-5f * big)) {
+            at += n;
+            continue;
+        }
         int32_t start = static_cast<int32_t>(q.items.size());
         flat_item head = {pbase + static_cast<int32_t>(at), 0};
         q.items.push_back(head);
@@ -1201,15 +1298,18 @@ int queue_draw(cy_ctx *c, const float *points, const int *counts, int n_sub, boo
     std::memset(&cmd, 0, sizeof(cmd));
     cmd.kind = CMD_FILL;
     size_t stops = q.stop_off.size(), tex = q.texels.size();
+    fill_state(state, cmd);
+    cull_rects rects = {static_cast<float>(c->W), static_cast<float>(c->H), cmd.shadow != 0,
+                        static_cast<float>(c->W + 2 * cmd.sh_border), static_cast<float>(c->H + 2 * cmd.sh_border),
+                        cmd.sh_offx, cmd.sh_offy};
     int rc = fill_paint(q, paint, cmd);
-    if (rc == CY_OK) rc = queue_geometry(q, points, counts, n_sub, bezier, cmd);
+    if (rc == CY_OK) rc = queue_geometry(q, points, counts, n_sub, bezier, cmd, rects);
     if (rc != CY_OK) {
         q.stop_off.resize(stops);
         q.stop_col.resize(stops);
         q.texels.resize(tex);
         return rc;
     }
-    fill_state(state, cmd);
     q.rows += c->H + (cmd.shadow ? c->H + 2 * cmd.sh_border : 0);
     q.cmds.push_back(cmd);
     q.mask_ids.push_back(state->mask);
@@ -1325,7 +1425,8 @@ int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, i
     command cmd;
     std::memset(&cmd, 0, sizeof(cmd));
     cmd.kind = CMD_CLIP;
-    int rc = queue_geometry(q, points, counts, n_sub, true, cmd);
+    cull_rects rects = {static_cast<float>(c->W), static_cast<float>(c->H), false, 0.0f, 0.0f, 0.0f, 0.0f};
+    int rc = queue_geometry(q, points, counts, n_sub, true, cmd, rects);
     if (rc != CY_OK) return rc;
     int id = 0;
     for (int i = 1; i < static_cast<int>(c->masks.size()); ++i)
@@ -1479,12 +1580,63 @@ struct cy_frame {
     cudaStream_t stream = nullptr;
 };
 
+// Device workspaces of finished frames, at most one per device: the next
+// frame reuses its buffers instead of allocating them again.
+namespace {
+std::mutex g_ws_lock;
+std::vector<std::pair<int, std::unique_ptr<frame>>> g_ws;
+
+std::unique_ptr<frame> take_workspace() {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    std::lock_guard<std::mutex> hold(g_ws_lock);
+    for (auto &w : g_ws)
+        if (w.first == dev && w.second) return std::move(w.second);
+    return nullptr;
+}
+
+void give_workspace(std::unique_ptr<frame> f) {
+    int dev = -1;
+    if (!f || f->status || cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return; }
+    f->reset();
+    std::unique_ptr<frame> spare;
+    {
+        std::lock_guard<std::mutex> hold(g_ws_lock);
+        for (auto &w : g_ws)
+            if (w.first == dev) {
+                if (!w.second) { w.second = std::move(f); return; }
+                spare = std::move(f);   // one is kept already: free this one
+                break;
+            }
+        if (f) g_ws.emplace_back(dev, std::move(f));
+    }
+}
+}  // namespace
+
 void cy_frame_destroy(cy_frame *fr) {
     if (!fr) return;
     if (fr->stream) cudaStreamSynchronize(fr->stream);
+    give_workspace(std::move(fr->f));
     fr->f.reset();
     if (fr->stream) cudaStreamDestroy(fr->stream);
     delete fr;
+}
+
+void cy_frame_workspace_release(void) {
+    std::vector<std::pair<int, std::unique_ptr<frame>>> all;
+    {
+        std::lock_guard<std::mutex> hold(g_ws_lock);
+        all.swap(g_ws);
+    }
+    int dev = -1;
+    cudaGetDevice(&dev);
+    for (auto &w : all)
+        if (w.second) {
+            cudaSetDevice(w.first);
+            w.second.reset();
+        }
+    if (dev >= 0) cudaSetDevice(dev);
+    cudaGetLastError();
 }
 
 int cy_frame_create(cy_ctx *const *ctxs, int n, int engine, cy_frame **out) {
@@ -1497,7 +1649,8 @@ int cy_frame_create(cy_ctx *const *ctxs, int n, int engine, cy_frame **out) {
     }
     cy_frame *fr = new (std::nothrow) cy_frame();
     if (!fr) return CY_ENOMEM;
-    fr->f.reset(new frame());
+    fr->f = take_workspace();
+    if (!fr->f) fr->f.reset(new frame());
     if (cudaStreamCreateWithFlags(&fr->stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete fr;

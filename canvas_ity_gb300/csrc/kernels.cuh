@@ -730,7 +730,7 @@ __global__ void k_paint(paint_args a) {
         // sum up to the clip's end (hpp:2572-2600): that matters when the
         // float sum is left above the visibility threshold.
         int xs = clearing ? 0 : r[0].x;
-        bool tail = lo(fabsf(sm[n - 1]), 1.0f) >= kVisible;
+        bool tail = n > 0 && lo(fabsf(sm[n - 1]), 1.0f) >= kVisible;
         int xe = clearing || tail ? a.W - 1 : min(r[n - 1].x, a.W - 1);
         for (int x = xs + lane; x <= xe; x += 32) {
             float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);

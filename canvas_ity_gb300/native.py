@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import time
 from typing import List, Optional, Tuple
 
 import numpy as np
@@ -109,6 +110,9 @@ def _batch_lib() -> ctypes.CDLL:
     lib.cy_frame_set_profiling.argtypes = [vp, ctypes.c_int]
     lib.cy_frame_profile.restype = ctypes.c_int
     lib.cy_frame_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+    lib.cy_canvases_from_traces.restype = ctypes.c_int
+    lib.cy_canvases_from_traces.argtypes = [ctypes.POINTER(vp), c_size_p, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, ctypes.POINTER(vp)]
     lib.cy_frame_stats.restype = ctypes.c_int
     lib.cy_frame_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]
     lib._batch_ready = True
@@ -124,21 +128,28 @@ class Frame:
     host into a canvas whose reads are deferred, then one frame renders all
     of them (engine 0: persistent strip kernel; 1: per-draw launches)."""
 
-    def __init__(self, traces, engine: int = 0):
+    def __init__(self, traces, engine: int = 0, threads: int = 0):
         self.lib = _batch_lib()
         self.canvases = []
         self.frame = ctypes.c_void_p()
         try:
-            for t in traces:
-                st = ctypes.c_int(0)
-                c = self.lib.cy_canvas_from_trace(t, len(t), ctypes.byref(st))
-                if not c:
-                    raise RuntimeError(f"replay into a deferred canvas failed with status {st.value}")
-                self.canvases.append(c)
+            n = len(traces)
+            bufs = (ctypes.c_void_p * n)(*[ctypes.cast(ctypes.c_char_p(t), ctypes.c_void_p).value
+                                           for t in traces])
+            lens = (ctypes.c_size_t * n)(*[len(t) for t in traces])
+            out = (ctypes.c_void_p * n)()
+            t0 = time.perf_counter()
+            rc = self.lib.cy_canvases_from_traces(bufs, lens, n, int(engine), int(threads), out)
+            if rc != 0:
+                raise RuntimeError(f"replay into deferred canvases failed with status {rc}")
+            self.canvases = [out[i] for i in range(n)]
+            t1 = time.perf_counter()
             ctxs = (ctypes.c_void_p * len(self.canvases))(*[self.lib.cy_canvas_ctx(c) for c in self.canvases])
             rc = self.lib.cy_frame_create(ctxs, len(self.canvases), int(engine), ctypes.byref(self.frame))
             if rc != 0:
                 raise RuntimeError(f"cy_frame_create failed with status {rc}")
+            # host seconds: replaying the call lists, building + first run of the frame
+            self.timing = {"replay_s": t1 - t0, "create_s": time.perf_counter() - t1}
             self.ctxs = [ctxs[i] for i in range(len(self.canvases))]
         except Exception:
             self.close()
@@ -176,9 +187,11 @@ class Frame:
         return {self.PHASES[i]: float(arr[i]) for i in range(min(n, len(self.PHASES)))}
 
     def finish(self) -> List[bytes]:
+        t0 = time.perf_counter()
         rc = self.lib.cy_frame_finish(self.frame)
         if rc != 0:
             raise RuntimeError(f"cy_frame_finish failed with status {rc}")
+        t1 = time.perf_counter()
         out = []
         for ctx in self.ctxs:
             n = ctypes.c_size_t(0)
@@ -188,6 +201,8 @@ class Frame:
             if rc != 0:
                 raise RuntimeError(f"cy_ctx_take_reads failed with status {rc}")
             out.append(buf.raw[: n.value])
+        self.timing["finish_s"] = t1 - t0
+        self.timing["reads_s"] = time.perf_counter() - t1
         return out
 
     def close(self) -> None:

@@ -21,6 +21,7 @@ extern "C" {
 #endif
 
 typedef struct cy_frame cy_frame;
+struct cy_canvas;   /* canvas_ity_c.h */
 
 /* Contexts created afterwards in this thread queue their reads (1) or
  * flush on every read as the reference API requires (0, default). */
@@ -48,7 +49,11 @@ void *cy_frame_stream(cy_frame *frame);
 /* Copy the reads out, release queued resources. */
 int cy_frame_finish(cy_frame *frame);
 
+/* Destroying a frame keeps its device and pinned buffers (one set per
+ * device) for the next cy_frame_create, which then allocates only what
+ * grows.  cy_frame_workspace_release frees what is kept. */
 void cy_frame_destroy(cy_frame *frame);
+void cy_frame_workspace_release(void);
 
 /* Profiling: when on, each run records CUDA events on the frame's stream at
  * its phase boundaries.  cy_frame_profile waits for the stream and writes
@@ -63,6 +68,14 @@ int cy_frame_profile(cy_frame *frame, float *phase_ms, int n);
  * runs of draws, rows of draws, shadow image floats, read-back bytes,
  * uploaded bytes, kernel launches per run, shadows, clips. */
 int cy_frame_stats(cy_frame *frame, long long *stats, int n);
+
+/* Replay n call lists (cy_trace.h) into n new canvases whose reads are
+ * deferred, on `threads` host threads (0: one per core); engine as for
+ * cy_set_engine.  out[i] receives canvas i (release with
+ * cy_canvas_delete); cy_canvas_ctx gives the contexts for cy_frame_create.
+ * On failure no canvas is kept and the first failing status is returned. */
+int cy_canvases_from_traces(const void *const *traces, const size_t *lens, int n, int engine, int threads,
+                            struct cy_canvas **out);
 
 /* Deferred reads of a context, concatenated in call order (compact RGBA8
  * rectangles); -2 if cap is too small (*len holds the size). */
