@@ -758,10 +758,11 @@ int frame::run() {
         int rc = clip_passes(t);
         if (rc) return rc;
         int segs_nc = static_cast<int>(nc_segs), segs_cl = static_cast<int>(pass_n[4]);
-        int grid_nc = std::max(1, std::min((segs_nc + 127) / 128, 152 * 64));
-        int grid_cl = std::max(1, std::min((segs_cl + 127) / 128, 152 * 64));
-        if (segs_nc > 0) k_runs<false, false><<<grid_nc, 128, 0, stream>>>(t, segs_nc);
-        if (segs_cl > 0) k_runs<false, true><<<grid_cl, 128, 0, stream>>>(t, segs_cl);
+        const int seg_per_block = kRunsWarps * 32;
+        int grid_nc = std::max(1, std::min((segs_nc + seg_per_block - 1) / seg_per_block, 152 * 16));
+        int grid_cl = std::max(1, std::min((segs_cl + seg_per_block - 1) / seg_per_block, 152 * 16));
+        if (segs_nc > 0) k_runs<false, false><<<grid_nc, kRunsWarps * 32, 0, stream>>>(t, segs_nc);
+        if (segs_cl > 0) k_runs<false, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl);
         rc = scan64(row_cnt.as<int32_t>(), row_off.as<int64_t>(), static_cast<int>(nr) + 1);
         if (rc) return rc;
         if (!sized) {
@@ -800,8 +801,8 @@ int frame::run() {
         }
         t.row_off = row_off.as<int64_t>();
         t.runs = runs.as<cyg::run>();
-        if (segs_nc > 0) k_runs<true, false><<<grid_nc, 128, 0, stream>>>(t, segs_nc);
-        if (segs_cl > 0) k_runs<true, true><<<grid_cl, 128, 0, stream>>>(t, segs_cl);
+        if (segs_nc > 0) k_runs<true, false><<<grid_nc, kRunsWarps * 32, 0, stream>>>(t, segs_nc);
+        if (segs_cl > 0) k_runs<true, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl);
         int rgrid = static_cast<int>(std::min<size_t>((nr + kRowsWarps - 1) / kRowsWarps, 152 * 32));
         if (!ok(cudaMemsetAsync(n_long.p, 0, 4, stream))) return status;
         k_rows<<<std::max(rgrid, 1), kRowsWarps * 32, 0, stream>>>(

@@ -347,85 +347,108 @@ struct job_tables {
     run *runs;
 };
 
-// One thread per segment: every row of it, clamped to the job's rectangle
-// as scan does before add_runs (hpp:2236-2238).
+// Segments go to warps 32 at a time: each lane prepares one segment
+// (clamped to its job's rectangle as scan does before add_runs,
+// hpp:2236-2238), then the warp deals all rows of the 32 segments out to its
+// lanes, so a long segment no longer holds one thread while the rest idle.
+// Any row can be rebuilt on its own (dda_exit), so the split is exact.
+static constexpr int kRunsWarps = 4;   // warps per block in k_runs
+
 template <bool EMIT, bool CLIPPED>
-__global__ void k_runs(job_tables t, int total_segments) {
-    int stride = gridDim.x * blockDim.x;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < total_segments; s += stride) {
-        int ji;
-        float2 a, b;
-        if (CLIPPED) {
-            ji = t.cl_job[s];
-            a = t.cl_pts[t.cl_prev[s]];
-            b = t.cl_pts[s];
-        } else {
-            int c = table_find(t.tab, t.n_tab, s);
-            ji = t.tab[c].y;
-            const scan_job &jj = t.jobs[ji];
-            int k = jj.line_first + (s - t.tab[c].x);
-            int g = jj.geom ? 1 : 0;
-            float2 pb = t.pts[g][k];
-            float2 pa = t.pts[g][t.prev[g][k]];
-            a = f2(jj.offx + pa.x, jj.offy + pa.y);
-            b = f2(jj.offx + pb.x, jj.offy + pb.y);
-        }
-        const scan_job &j = t.jobs[ji];
-        a = f2(lo(hi(a.x, 0.0f), j.width), lo(hi(a.y, 0.0f), j.height));
-        b = f2(lo(hi(b.x, 0.0f), j.width), lo(hi(b.y, 0.0f), j.height));
-        int x0 = 0x7fffffff, x1 = -0x7fffffff, y0 = 0x7fffffff, y1 = -0x7fffffff;
-        long long first = 0x7fffffffffffffffll;
+__global__ void __launch_bounds__(kRunsWarps * 32) k_runs(job_tables t, int total_segments) {
+    __shared__ dda_piece pieces[kRunsWarps][32];
+    __shared__ int seg_job[kRunsWarps][32];
+    __shared__ int seg_end[kRunsWarps][32];   // inclusive prefix of row counts
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kRunsWarps + w, nw = gridDim.x * kRunsWarps;
+    for (int base = gw * 32; base < total_segments; base += nw * 32) {
+        int s = base + lane;
+        int rows_here = 0, ji = 0;
         dda_piece p;
-        if (dda_setup(a, b, p)) {
-            int nrows = p.nrows < j.rows + 2 ? p.nrows : j.rows + 2;
-            float2 entry = f2(p.fx, p.fy);
-            for (int r = 0; r < nrows; ++r) {
-                float2 ex = dda_exit(p, r);
-                int ps, pe;
-                dda_span(p, r, entry, ex, ps, pe);
-                int row = dda_row_index(p, r);
-                if (row >= 0 && row < j.rows) {
-                    int n = pe - ps + 2;
-                    int grow = j.row_base + row;
-                    if (!EMIT) {
-                        atomicAdd(t.row_cnt + grow, n);
-                        long long key = (static_cast<long long>(row) << 32) | static_cast<long long>(ps < 0 ? 0 : ps);
-                        if (key < first) first = key;
-                    } else {
-                        int base = atomicAdd(t.row_cur + grow, n);
-                        int64_t cap = t.row_off[grow + 1] - t.row_off[grow];
-                        if (base + n <= cap) {
-                            run *out = t.runs + t.row_off[grow] + base;
-                            int i = 0;
-                            int cols = j.cols;
-                            auto emit = [&](int x, float d) {
-                                bool okx = x >= 0 && x < cols;
-                                out[i++] = run{okx ? x : 0, okx ? d : 0.0f};
-                                if (okx && d != 0.0f) {
-                                    x0 = x < x0 ? x : x0;
-                                    x1 = x > x1 ? x : x1;
-                                    y0 = row < y0 ? row : y0;
-                                    y1 = row > y1 ? row : y1;
-                                }
-                            };
-                            dda_cells(p, entry, ex, ps, pe, emit);
-                        }
-                    }
+        p.nrows = 0;
+        if (s < total_segments) {
+            float2 a, b;
+            if (CLIPPED) {
+                ji = t.cl_job[s];
+                a = t.cl_pts[t.cl_prev[s]];
+                b = t.cl_pts[s];
+            } else {
+                int c = table_find(t.tab, t.n_tab, s);
+                ji = t.tab[c].y;
+                const scan_job &jj = t.jobs[ji];
+                int k = jj.line_first + (s - t.tab[c].x);
+                int g = jj.geom ? 1 : 0;
+                float2 pb = t.pts[g][k];
+                float2 pa = t.pts[g][t.prev[g][k]];
+                a = f2(jj.offx + pa.x, jj.offy + pa.y);
+                b = f2(jj.offx + pb.x, jj.offy + pb.y);
+            }
+            const scan_job &j = t.jobs[ji];
+            a = f2(lo(hi(a.x, 0.0f), j.width), lo(hi(a.y, 0.0f), j.height));
+            b = f2(lo(hi(b.x, 0.0f), j.width), lo(hi(b.y, 0.0f), j.height));
+            if (dda_setup(a, b, p)) rows_here = p.nrows < j.rows + 2 ? p.nrows : j.rows + 2;
+        }
+        int incl = rows_here;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        pieces[w][lane] = p;
+        seg_job[w][lane] = ji;
+        seg_end[w][lane] = incl;
+        int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        for (int q = lane; q < total; q += 32) {
+            int lo_i = 0, hi_i = 31;   // first segment whose inclusive end exceeds q
+            while (lo_i < hi_i) {
+                int mid = (lo_i + hi_i) >> 1;
+                if (seg_end[w][mid] > q) hi_i = mid; else lo_i = mid + 1;
+            }
+            const dda_piece &pp = pieces[w][lo_i];
+            const int jq = seg_job[w][lo_i];
+            const scan_job &j = t.jobs[jq];
+            int k = q - (lo_i ? seg_end[w][lo_i - 1] : 0);
+            float2 entry = k == 0 ? f2(pp.fx, pp.fy) : dda_exit(pp, k - 1);
+            float2 ex = dda_exit(pp, k);
+            int ps, pe;
+            dda_span(pp, k, entry, ex, ps, pe);
+            int row = dda_row_index(pp, k);
+            if (row < 0 || row >= j.rows) continue;
+            int n = pe - ps + 2;
+            int grow = j.row_base + row;
+            if (!EMIT) {
+                atomicAdd(t.row_cnt + grow, n);
+                if (j.need_box) {
+                    long long key = (static_cast<long long>(row) << 32) | static_cast<long long>(ps < 0 ? 0 : ps);
+                    atomicMin(reinterpret_cast<long long *>(&t.boxes[jq].first_key), key);
                 }
-                entry = ex;
+            } else {
+                int at = atomicAdd(t.row_cur + grow, n);
+                int64_t cap = t.row_off[grow + 1] - t.row_off[grow];
+                if (at + n > cap) continue;
+                run *out = t.runs + t.row_off[grow] + at;
+                int i = 0, x0 = 0x7fffffff, x1 = -0x7fffffff;
+                int cols = j.cols;
+                auto emit = [&](int x, float d) {
+                    bool okx = x >= 0 && x < cols;
+                    out[i++] = run{okx ? x : 0, okx ? d : 0.0f};
+                    if (okx && d != 0.0f) {
+                        x0 = x < x0 ? x : x0;
+                        x1 = x > x1 ? x : x1;
+                    }
+                };
+                dda_cells(pp, entry, ex, ps, pe, emit);
+                if (j.need_box && x0 <= x1) {
+                    cover_box *box = t.boxes + jq;
+                    atomicMin(&box->x0, x0);
+                    atomicMax(&box->x1, x1);
+                    atomicMin(&box->y0, row);
+                    atomicMax(&box->y1, row);
+                }
             }
         }
-        if (j.need_box) {
-            cover_box *box = t.boxes + ji;
-            if (EMIT && x0 <= x1) {
-                atomicMin(&box->x0, x0);
-                atomicMax(&box->x1, x1);
-                atomicMin(&box->y0, y0);
-                atomicMax(&box->y1, y1);
-            }
-            if (!EMIT && first != 0x7fffffffffffffffll)
-                atomicMin(reinterpret_cast<long long *>(&box->first_key), first);
-        }
+        __syncwarp();
     }
 }
 

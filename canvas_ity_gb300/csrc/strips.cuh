@@ -78,6 +78,10 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
             if (cv.flags & 1) v = cv.bitmap[static_cast<size_t>(y0 + ly) * W + x];
             px[ly * W + x] = v;
         }
+        // Canvas rows this warp's chunks span: draws wholly above or below
+        // them are skipped by the warp (the fixed chunk ownership needs no
+        // agreement between warps).
+        const int wy0 = y0 + (cb < ce ? cb / cpr : 0), wy1 = y0 + (cb < ce ? (ce - 1) / cpr : -1);
         for (int ci = cv.cmd_first; ci < cv.cmd_first + cv.cmd_count; ++ci) {
             const command &c = P.cmds[ci];
             const strip_cmd &e = P.ext[ci];
@@ -113,7 +117,7 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
                 const float *img = P.shadow_imgs + e.shadow_img;
                 int b = c.sh_border;
                 int sx0 = max(0, r.left - b), sx1 = min(W, r.right - b);
-                if (r.width > 0 && r.height > 0) {
+                if (r.width > 0 && r.height > 0 && r.top - b <= wy1 && r.bottom - b - 1 >= wy0) {
                     for (int ch = cb; ch < ce; ++ch) {
                         int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
                         int y = y0 + ly;
@@ -128,6 +132,9 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
                     }
                 }
             }
+            // Rows [gy0, gy1] hold all of the draw's runs; elsewhere only a
+            // clearing operation changes pixels.
+            if (!clearing && (c.gy1 < wy0 || c.gy0 > wy1)) continue;
             // render_main (hpp:2551-2605).  Walk each row's sorted runs with a
             // warp-wide cursor: the coverage sum in force at a pixel is the
             // running sum after the last run at or left of it.
@@ -188,6 +195,15 @@ __global__ void __launch_bounds__(256) k_strips(strip_params P) {
                 if (upto) v = from_run;
                 if (k > 0) carry = __shfl_sync(0xffffffffu, rs, k - 1);
                 j += k;
+                if (!clearing && k == 0 && lo(fabsf(carry), 1.0f) < kVisible) {
+                    // Nothing visible here nor up to the next run: jump to
+                    // the chunk that holds it (or past this row).
+                    int nx = __shfl_sync(0xffffffffu, rx, 0);
+                    int row_end = ly * cpr + cpr;
+                    int target = (nx < W && nx <= xe) ? ly * cpr + (nx >> 5) : row_end;
+                    if (target > ch + 1) ch = min(target, row_end) - 1;
+                    continue;
+                }
                 int x = x0 + lane;
                 if (x < xs || x > xe) continue;
                 int y = y0 + ly;
@@ -288,28 +304,78 @@ __global__ void k_shadow_raster_all(const shadow_job *sj, const command *cmds, p
 // the reference's sequential sums.  The row pass works on the column-major
 // raster, the image is then transposed, and the column pass works row-major,
 // so neighbouring threads always touch neighbouring addresses.
+//
+// The three passes of a line run as one sweep: pass k produces its value at
+// x once its input is known up to x + r + 1, so after reading element t the
+// passes emit x = t - (r+1), t - 2(r+1), t - 3(r+1).  Each pass keeps its
+// input window [x - r - 2, x + r + 1] in a 32-entry ring; the additions are
+// the reference's, in its order, so the result is the same as three full
+// passes.  Output lags input, so the line is blurred in place.
+static constexpr int kBlurRing = 32;
+static constexpr int kBlurMaxFused = (kBlurRing - 4) / 2;   // radius the rings hold
+
+struct blur_pass {
+    float acc;
+    float ring[kBlurRing];
+};
+
+// Value of one pass at x (0 <= x < n) from its input ring (hpp:2461-2478).
+__device__ __forceinline__ float blur_step(blur_pass &p, int x, int n, int r, float w1, float w2) {
+    const int m = kBlurRing - 1;
+    if (x == 0) {
+        float acc = r + 1 < n ? w1 * p.ring[(r + 1) & m] : 0.0f;
+        for (int i = 0; i <= r && i < n; ++i) acc += (w1 + w2) * p.ring[i & m];
+        p.acc = acc;
+        return acc;
+    }
+    float acc = p.acc;
+    if (x >= r + 1) acc -= w2 * p.ring[(x - r - 1) & m];
+    if (x >= r + 2) acc -= w1 * p.ring[(x - r - 2) & m];
+    if (x + r < n) acc += w2 * p.ring[(x + r) & m];
+    if (x + r + 1 < n) acc += w1 * p.ring[(x + r + 1) & m];
+    p.acc = acc;
+    return acc;
+}
+
+// Three blur passes over line[i * stride], i < n, in place.
+__device__ void blur_line_fused(float *line, size_t stride, int n, int r, float w1, float w2) {
+    const int m = kBlurRing - 1, L = r + 1;
+    blur_pass p[3];
+    for (int t = 0; t < n + 3 * L; ++t) {
+        if (t < n) p[0].ring[t & m] = line[static_cast<size_t>(t) * stride];
+        int x1 = t - L, x2 = t - 2 * L, x3 = t - 3 * L;
+        if (x1 >= 0 && x1 < n) p[1].ring[x1 & m] = blur_step(p[0], x1, n, r, w1, w2);
+        if (x2 >= 0 && x2 < n) p[2].ring[x2 & m] = blur_step(p[1], x2, n, r, w1, w2);
+        if (x3 >= 0 && x3 < n) line[static_cast<size_t>(x3) * stride] = blur_step(p[2], x3, n, r, w1, w2);
+    }
+}
+
+// The same three passes with a full copy of the line per pass (any radius).
+__device__ void blur_line_copy(float *line, float *tmp, size_t stride, size_t n, size_t r, float w1, float w2) {
+    for (int pass = 0; pass < 3; ++pass) {
+        for (size_t x = 0; x < n; ++x) tmp[x * stride] = line[x * stride];
+        float acc = r + 1 < n ? w1 * tmp[(r + 1) * stride] : 0.0f;
+        for (size_t x = 0; x <= r && x < n; ++x) acc += (w1 + w2) * tmp[x * stride];
+        if (n > 0) line[0] = acc;
+        for (size_t x = 1; x < n; ++x) {
+            if (x >= r + 1) acc -= w2 * tmp[(x - r - 1) * stride];
+            if (x >= r + 2) acc -= w1 * tmp[(x - r - 2) * stride];
+            if (x + r < n) acc += w2 * tmp[(x + r) * stride];
+            if (x + r + 1 < n) acc += w1 * tmp[(x + r + 1) * stride];
+            line[x * stride] = acc;
+        }
+    }
+}
+
 __global__ void k_blur_rows_all(const shadow_job *sj, const shadow_rect *rects, float *imgs, float *scratch) {
     const shadow_job &s = sj[blockIdx.y];
     const shadow_rect rc = rects[s.cmd];
     int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= rc.height) return;
-    size_t width = rc.width, h = rc.height, r = s.radius;
-    float *row = imgs + s.img + y;
-    float *t = scratch + s.img + y;
-    float w1 = s.w1, w2 = s.w2;
-    for (int pass = 0; pass < 3; ++pass) {
-        for (size_t x = 0; x < width; ++x) t[x * h] = row[x * h];
-        float acc = r + 1 < width ? w1 * t[(r + 1) * h] : 0.0f;
-        for (size_t x = 0; x <= r && x < width; ++x) acc += (w1 + w2) * t[x * h];
-        row[0] = acc;
-        for (size_t x = 1; x < width; ++x) {
-            if (x >= r + 1) acc -= w2 * t[(x - r - 1) * h];
-            if (x >= r + 2) acc -= w1 * t[(x - r - 2) * h];
-            if (x + r < width) acc += w2 * t[(x + r) * h];
-            if (x + r + 1 < width) acc += w1 * t[(x + r + 1) * h];
-            row[x * h] = acc;
-        }
-    }
+    if (s.radius <= kBlurMaxFused)
+        blur_line_fused(imgs + s.img + y, rc.height, rc.width, s.radius, s.w1, s.w2);
+    else
+        blur_line_copy(imgs + s.img + y, scratch + s.img + y, rc.height, rc.width, s.radius, s.w1, s.w2);
 }
 
 // Column-major -> row-major, 32x32 tiles (blockIdx.z selects the shadow).
@@ -338,23 +404,10 @@ __global__ void k_blur_cols_all(const shadow_job *sj, const shadow_rect *rects, 
     const shadow_rect rc = rects[s.cmd];
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= rc.width) return;
-    size_t width = rc.width, height = rc.height, r = s.radius;
-    float *img = imgs + s.img;
-    float *tmp = scratch + s.img;
-    float w1 = s.w1, w2 = s.w2;
-    for (int pass = 0; pass < 3; ++pass) {
-        for (size_t y = 0; y < height; ++y) tmp[y * width + x] = img[y * width + x];
-        float acc = r + 1 < height ? w1 * tmp[(r + 1) * width + x] : 0.0f;
-        for (size_t y = 0; y <= r && y < height; ++y) acc += (w1 + w2) * tmp[y * width + x];
-        if (height > 0) img[x] = acc;
-        for (size_t y = 1; y < height; ++y) {
-            if (y >= r + 1) acc -= w2 * tmp[(y - r - 1) * width + x];
-            if (y >= r + 2) acc -= w1 * tmp[(y - r - 2) * width + x];
-            if (y + r < height) acc += w2 * tmp[(y + r) * width + x];
-            if (y + r + 1 < height) acc += w1 * tmp[(y + r + 1) * width + x];
-            img[y * width + x] = acc;
-        }
-    }
+    if (s.radius <= kBlurMaxFused)
+        blur_line_fused(imgs + s.img + x, rc.width, rc.height, s.radius, s.w1, s.w2);
+    else
+        blur_line_copy(imgs + s.img + x, scratch + s.img + x, rc.width, rc.height, s.radius, s.w1, s.w2);
 }
 
 }  // namespace cyg
