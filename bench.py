@@ -269,6 +269,8 @@ def gpu_arm(args, world, rank, local):
     frame = native.Frame(traces, 0)
     stats = frame.stats()
     stream = torch.cuda.ExternalStream(frame.stream())
+    tuned = frame.autotune() if args.autotune else None
+    frame.capture()   # every later run is one CUDA graph launch
     for _ in range(max(args.warmup, 3)):
         frame.run()
     frame.sync()
@@ -358,7 +360,9 @@ def gpu_arm(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "canvases": len(traces), "pixels": px, "engine": "tile",
-                   "strip_pixels": args.strip_pixels or 4096, "commands": stats["commands"],
+                   "strip_pixels": tuned["strip_pixels"] if tuned else (args.strip_pixels or 4096),
+                   "strip_threads": tuned["threads"] if tuned else (args.strip_threads or 256),
+                   "autotuned": bool(tuned), "cuda_graph": True, "commands": stats["commands"],
                    "segments": stats["segments"], "runs": stats["runs"], "shadows": stats["shadows"],
                    "clips": stats["clips"], "l2": "inputs larger than L2 (runs and outputs are GBs)",
                    "parallelism": f"replicas x{world}", "generate_s": round(gen_s, 1)},
@@ -393,6 +397,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=64)
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--parity-sample", type=int, default=8)
+    ap.add_argument("--autotune", type=int, default=1, help="pick the strip configuration by timing (1) or not (0)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--strip-pixels", type=int, default=0)
     ap.add_argument("--strip-threads", type=int, default=256)

@@ -216,9 +216,25 @@ struct frame {
     }
     bool ext_built = false;
     bool strips_built = false;
+    int strip_threads = 256;
+    cudaGraphExec_t graph_exec = nullptr;   // captured device-only run (after sizing)
+    // inputs of the strip launch, kept by run() so the paint stage can be
+    // launched again on its own (autotuning)
+    row_view last_rv;
+    paint_src last_src;
+    const command *last_cmds = nullptr;
+    const uint8_t *last_put = nullptr;
+    const float *last_lut = nullptr;
+    int launch_strips();
+    int build_strips();
+    void drop_graph() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+    }
 
     // Forget the previous frame's commands but keep its device buffers.
     void reset() {
+        drop_graph();
         status = 0;
         cvs.clear();
         all.clear();
@@ -247,6 +263,7 @@ struct frame {
     }
 
     ~frame() {
+        drop_graph();
         for (cudaEvent_t e : ev) if (e) cudaEventDestroy(e);
         dbuf *b[] = {&arena, &flat_pts, &flat_prev, &item_cnt, &item_off, &pat_f4, &jobs_dev, &boxes, &row_cnt,
                      &row_off, &row_cur, &row_len, &long_rows, &n_long, &runs, &sums, &tabs_dev, &cp_cnt, &cp_off,
@@ -908,6 +925,12 @@ int frame::run() {
     }
     if (engine == 1) {
         // Plain engine: per-draw launches over each canvas's float bitmap.
+        // A fresh deferred canvas starts blank on every run, so running the
+        // frame again (timing, graph replay) gives the same pixels.
+        for (cy_ctx *cv : cvs)
+            if (cv->deferred && !cv->has_content &&
+                !ok(cudaMemsetAsync(cv->bitmap, 0, static_cast<size_t>(cv->W) * cv->H * sizeof(float4), stream)))
+                return status;
         for (size_t i = 0; i < cmds.size(); ++i) {
             const command &c = cmds[i];
             cy_ctx *cv = cvs[cmd_cv[i]];
@@ -958,77 +981,103 @@ int frame::run() {
         return ok(cudaGetLastError()) ? CY_OK : status;
     }
     // Tile engine: one persistent launch over (canvas, strip) work items.
-    size_t smem = static_cast<size_t>(strip_pixels) * sizeof(float4);
     if (!strips_built) {
-        strips_built = true;
-        strip_pixels = g_strip_pixels;
-        smem = static_cast<size_t>(strip_pixels) * sizeof(float4);
-        scv.resize(cvs.size());
-        std::vector<std::pair<int64_t, int2>> work;
-        int cursor = 0;
-        for (size_t ci = 0; ci < cvs.size(); ++ci) {
-            cy_ctx *cv = cvs[ci];
-            if (cv->W > strip_pixels) return fail(CY_EINVAL);   // a row must fit in one strip
-            strip_canvas &s = scv[ci];
-            s.W = cv->W;
-            s.H = cv->H;
-            s.TH = std::max(1, std::min(cv->H, strip_pixels / std::max(1, cv->W)));
-            s.cmd_first = cursor;
-            s.cmd_count = static_cast<int32_t>(cv->q.cmds.size());
-            cursor += s.cmd_count;
-            s.flags = (cv->has_content ? 1 : 0) | (cv->deferred ? 0 : 2);
-            s.bitmap = cv->bitmap;
-            int64_t cost = static_cast<int64_t>(s.TH) * s.W * (s.cmd_count + 1);
-            for (int y = 0; y < s.H; y += s.TH) work.push_back({cost, make_int2(static_cast<int>(ci), y)});
-        }
-        std::stable_sort(work.begin(), work.end(),
-                         [](const std::pair<int64_t, int2> &a, const std::pair<int64_t, int2> &b) {
-                             return a.first > b.first;
-                         });
-        items_host.resize(work.size());
-        for (size_t k = 0; k < work.size(); ++k) items_host[k] = work[k].second;
-        n_items = static_cast<int>(items_host.size());
-        if (!scv_dev.ensure(scv.size() * sizeof(strip_canvas)) ||
-            !items_dev.ensure(std::max<size_t>(items_host.size(), 1) * sizeof(int2)) ||
-            !ext_dev.ensure(std::max<size_t>(ext.size(), 1) * sizeof(strip_cmd)) || !counter.ensure(4))
-            return fail(CY_ENOMEM, __LINE__);
-        if (!ok(cudaMemcpyAsync(scv_dev.p, scv.data(), scv.size() * sizeof(strip_canvas), cudaMemcpyHostToDevice,
-                                stream)))
-            return status;
-        if (n_items > 0 && !ok(cudaMemcpyAsync(items_dev.p, items_host.data(), items_host.size() * sizeof(int2),
-                                               cudaMemcpyHostToDevice, stream)))
-            return status;
-        if (!ext.empty() && !ok(cudaMemcpyAsync(ext_dev.p, ext.data(), ext.size() * sizeof(strip_cmd),
-                                                cudaMemcpyHostToDevice, stream)))
-            return status;
-        if (!ok(cudaFuncSetAttribute(k_strips, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))))
-            return status;
+        int rc = build_strips();
+        if (rc) return rc;
     }
+    last_rv = rv;
+    last_src = src;
+    last_cmds = d_cmds;
+    last_put = d_put;
+    last_lut = lut;
+    int rc = launch_strips();
+    mark();   // 4: paint done
+    return rc;
+}
+
+// Strip layout of the frame for the current strip configuration: per
+// canvas its strip height, work items (canvas, first row) in decreasing
+// cost, uploaded with the per-command extras.
+int frame::build_strips() {
+    strips_built = true;
+    strip_pixels = g_strip_pixels;
+    strip_threads = g_strip_threads;
+    size_t smem = static_cast<size_t>(strip_pixels) * sizeof(float4);
+    scv.resize(cvs.size());
+    std::vector<std::pair<int64_t, int2>> work;
+    int cursor = 0;
+    for (size_t ci = 0; ci < cvs.size(); ++ci) {
+        cy_ctx *cv = cvs[ci];
+        if (cv->W > strip_pixels) return fail(CY_EINVAL);   // a row must fit in one strip
+        strip_canvas &s = scv[ci];
+        s.W = cv->W;
+        s.H = cv->H;
+        s.TH = std::max(1, std::min(cv->H, strip_pixels / std::max(1, cv->W)));
+        s.cmd_first = cursor;
+        s.cmd_count = static_cast<int32_t>(cv->q.cmds.size());
+        cursor += s.cmd_count;
+        s.flags = (cv->has_content ? 1 : 0) | (cv->deferred ? 0 : 2);
+        s.bitmap = cv->bitmap;
+        int64_t cost = static_cast<int64_t>(s.TH) * s.W * (s.cmd_count + 1);
+        for (int y = 0; y < s.H; y += s.TH) work.push_back({cost, make_int2(static_cast<int>(ci), y)});
+    }
+    std::stable_sort(work.begin(), work.end(),
+                     [](const std::pair<int64_t, int2> &a, const std::pair<int64_t, int2> &b) {
+                         return a.first > b.first;
+                     });
+    items_host.resize(work.size());
+    for (size_t k = 0; k < work.size(); ++k) items_host[k] = work[k].second;
+    n_items = static_cast<int>(items_host.size());
+    if (!scv_dev.ensure(scv.size() * sizeof(strip_canvas)) ||
+        !items_dev.ensure(std::max<size_t>(items_host.size(), 1) * sizeof(int2)) ||
+        !ext_dev.ensure(std::max<size_t>(ext.size(), 1) * sizeof(strip_cmd)) || !counter.ensure(4))
+        return fail(CY_ENOMEM, __LINE__);
+    if (!ok(cudaMemcpyAsync(scv_dev.p, scv.data(), scv.size() * sizeof(strip_canvas), cudaMemcpyHostToDevice,
+                            stream)))
+        return status;
+    if (n_items > 0 && !ok(cudaMemcpyAsync(items_dev.p, items_host.data(), items_host.size() * sizeof(int2),
+                                           cudaMemcpyHostToDevice, stream)))
+        return status;
+    if (!ext.empty() && !ok(cudaMemcpyAsync(ext_dev.p, ext.data(), ext.size() * sizeof(strip_cmd),
+                                            cudaMemcpyHostToDevice, stream)))
+        return status;
+    if (!ok(cudaFuncSetAttribute(k_strips<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))) ||
+        !ok(cudaFuncSetAttribute(k_strips<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))) ||
+        !ok(cudaFuncSetAttribute(k_strips<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))))
+        return status;
+    return CY_OK;
+}
+
+// The persistent strip kernel over all (canvas, strip) items, with the
+// inputs of the last run.
+int frame::launch_strips() {
     if (n_items == 0) return CY_OK;
+    size_t smem = static_cast<size_t>(strip_pixels) * sizeof(float4);
     if (!ok(cudaMemsetAsync(counter.p, 0, 4, stream))) return status;
     strip_params P;
     P.canvases = scv_dev.as<strip_canvas>();
     P.items = items_dev.as<int2>();
     P.n_items = n_items;
     P.counter = counter.as<int>();
-    P.cmds = d_cmds;
+    P.cmds = last_cmds;
     P.ext = ext_dev.as<strip_cmd>();
-    P.rv = rv;
-    P.src = src;
+    P.rv = last_rv;
+    P.src = last_src;
     P.rects = rects.as<shadow_rect>();
     P.shadow_imgs = sh_scratch.as<float>();
-    P.put_px = d_put;
-    P.lut = lut;
+    P.put_px = last_put;
+    P.lut = last_lut;
     P.get_buf = get_dev.as<uint8_t>();
     P.strip_pixels = strip_pixels;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_strips, g_strip_threads, smem);
-    int sms = 152;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    int per_sm = 0, dev = 0, sms = 152;
+    auto kern = strip_threads == 128 ? k_strips<128> : strip_threads == 512 ? k_strips<512> : k_strips<256>;
+    int threads = strip_threads == 128 || strip_threads == 512 ? strip_threads : 256;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int grid = std::max(1, std::min(n_items, sms * std::max(per_sm, 1)));
-    k_strips<<<grid, g_strip_threads, smem, stream>>>(P);
+    kern<<<grid, threads, smem, stream>>>(P);
     ++launches;
-    mark();   // 4: paint done
     return ok(cudaGetLastError()) ? CY_OK : status;
 }
 
@@ -1669,7 +1718,114 @@ int cy_frame_create(cy_ctx *const *ctxs, int n, int engine, cy_frame **out) {
     return CY_OK;
 }
 
-int cy_frame_run(cy_frame *fr) { return fr ? fr->f->run() : CY_EINVAL; }
+int cy_frame_run(cy_frame *fr) {
+    if (!fr) return CY_EINVAL;
+    frame &f = *fr->f;
+    if (f.graph_exec && !f.profiling) {
+        if (f.status) return f.status;
+        if (cudaGraphLaunch(f.graph_exec, fr->stream) != cudaSuccess) {
+            cudaGetLastError();
+            return f.fail(CY_ECUDA);
+        }
+        return CY_OK;
+    }
+    return f.run();
+}
+
+int cy_frame_autotune(cy_frame *fr, int *best_pixels, int *best_threads, float *best_ms) {
+    if (!fr) return CY_EINVAL;
+    frame &f = *fr->f;
+    if (f.status) return f.status;
+    if (!f.sized || f.engine != 0) return CY_EINVAL;
+    int max_w = 1;
+    for (cy_ctx *cv : f.cvs) {
+        if (!cv->deferred) return CY_EINVAL;   // the paint stage must be repeatable
+        max_w = std::max(max_w, cv->W);
+    }
+    const int pixels[] = {2048, 4096, 8192, 12288};
+    const int threads[] = {128, 256, 512};
+    int keep_p = g_strip_pixels, keep_t = g_strip_threads;
+    int bp = 0, bt = 0;
+    float bms = 0.0f;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        cudaGetLastError();
+        if (a) cudaEventDestroy(a);
+        return CY_ECUDA;
+    }
+    f.drop_graph();
+    int rc = CY_OK;
+    for (int px : pixels) {
+        if (px < max_w) continue;
+        for (int th : threads) {
+            g_strip_pixels = px;
+            g_strip_threads = th;
+            f.strips_built = false;
+            rc = f.build_strips();
+            if (rc == CY_OK) rc = f.launch_strips();   // warm-up
+            float ms = 0.0f;
+            for (int rep = 0; rep < 2 && rc == CY_OK; ++rep) {
+                cudaEventRecord(a, fr->stream);
+                rc = f.launch_strips();
+                cudaEventRecord(b, fr->stream);
+                float t = 0.0f;
+                if (rc == CY_OK && (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&t, a, b) != cudaSuccess)) {
+                    cudaGetLastError();
+                    rc = f.fail(CY_ECUDA);
+                }
+                if (rep == 0 || t < ms) ms = t;
+            }
+            if (rc != CY_OK) break;
+            if (bp == 0 || ms < bms) { bp = px; bt = th; bms = ms; }
+        }
+        if (rc != CY_OK) break;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    g_strip_pixels = bp ? bp : keep_p;
+    g_strip_threads = bt ? bt : keep_t;
+    if (rc != CY_OK) return rc;
+    f.strips_built = false;
+    rc = f.build_strips();
+    if (rc != CY_OK) return rc;
+    if (best_pixels) *best_pixels = bp;
+    if (best_threads) *best_threads = bt;
+    if (best_ms) *best_ms = bms;
+    return bp ? CY_OK : CY_EINVAL;
+}
+
+int cy_frame_capture(cy_frame *fr) {
+    if (!fr) return CY_EINVAL;
+    frame &f = *fr->f;
+    if (f.status) return f.status;
+    if (!f.sized) return CY_EINVAL;   // the first run sizes the buffers with host read-backs
+    f.drop_graph();
+    bool was_profiling = f.profiling;
+    f.profiling = false;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(fr->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        f.profiling = was_profiling;
+        return CY_ECUDA;
+    }
+    int rc = f.run();
+    cudaError_t e = cudaStreamEndCapture(fr->stream, &g);
+    f.profiling = was_profiling;
+    if (rc != CY_OK || e != cudaSuccess || !g) {
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        return rc != CY_OK ? rc : f.fail(CY_ECUDA);
+    }
+    cudaGraphExec_t x = nullptr;
+    e = cudaGraphInstantiate(&x, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return CY_ECUDA;
+    }
+    f.graph_exec = x;
+    return CY_OK;
+}
 
 int cy_frame_finish(cy_frame *fr) { return fr ? fr->f->finish() : CY_EINVAL; }
 

@@ -51,7 +51,8 @@ struct strip_params {
     int strip_pixels;
 };
 
-__global__ void __launch_bounds__(256) k_strips(strip_params P) {
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
     extern __shared__ float4 px[];
     __shared__ int item_slot;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;

@@ -95,7 +95,7 @@ def _batch_lib() -> ctypes.CDLL:
     lib.cy_canvas_delete.argtypes = [vp]
     lib.cy_frame_create.restype = ctypes.c_int
     lib.cy_frame_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
-    for name in ("cy_frame_run", "cy_frame_sync", "cy_frame_finish"):
+    for name in ("cy_frame_run", "cy_frame_sync", "cy_frame_finish", "cy_frame_capture"):
         getattr(lib, name).restype = ctypes.c_int
         getattr(lib, name).argtypes = [vp]
     lib.cy_frame_destroy.restype = None
@@ -110,6 +110,8 @@ def _batch_lib() -> ctypes.CDLL:
     lib.cy_frame_set_profiling.argtypes = [vp, ctypes.c_int]
     lib.cy_frame_profile.restype = ctypes.c_int
     lib.cy_frame_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+    lib.cy_frame_autotune.restype = ctypes.c_int
+    lib.cy_frame_autotune.argtypes = [vp, c_int_p, c_int_p, ctypes.POINTER(ctypes.c_float)]
     lib.cy_canvases_from_traces.restype = ctypes.c_int
     lib.cy_canvases_from_traces.argtypes = [ctypes.POINTER(vp), c_size_p, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, ctypes.POINTER(vp)]
@@ -159,6 +161,21 @@ class Frame:
         rc = self.lib.cy_frame_run(self.frame)
         if rc != 0:
             raise RuntimeError(f"cy_frame_run failed with status {rc}")
+
+    def autotune(self) -> dict:
+        """Pick the fastest strip size / block size for this frame's paint
+        stage; it also becomes the process's strip configuration."""
+        p, t, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_float(0.0)
+        rc = self.lib.cy_frame_autotune(self.frame, ctypes.byref(p), ctypes.byref(t), ctypes.byref(ms))
+        if rc != 0:
+            raise RuntimeError(f"cy_frame_autotune failed with status {rc}")
+        return {"strip_pixels": p.value, "threads": t.value, "paint_ms": round(ms.value, 3)}
+
+    def capture(self) -> None:
+        """Capture a device-only run into a CUDA graph; later runs launch it."""
+        rc = self.lib.cy_frame_capture(self.frame)
+        if rc != 0:
+            raise RuntimeError(f"cy_frame_capture failed with status {rc}")
 
     def sync(self) -> None:
         rc = self.lib.cy_frame_sync(self.frame)

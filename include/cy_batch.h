@@ -40,6 +40,21 @@ int cy_frame_create(cy_ctx *const *ctxs, int n, int engine, cy_frame **out);
  * synchronisation); for timing. */
 int cy_frame_run(cy_frame *frame);
 
+/* Autotuner of the tile engine: times the frame's paint stage (the strip
+ * kernel alone, which a frame of deferred canvases can repeat) for strip
+ * sizes 2048..12288 pixels (no narrower than the widest canvas) and 128,
+ * 256 or 512 threads per block, keeps the fastest for this frame and makes
+ * it the process's strip configuration (cy_set_strip_config).  After the
+ * frame's first run; CY_EINVAL for the plain engine or non-deferred
+ * contexts. */
+int cy_frame_autotune(cy_frame *frame, int *strip_pixels, int *threads, float *paint_ms);
+
+/* Capture one device-only run of the frame (after its first run) into a
+ * CUDA graph; later cy_frame_run calls launch the graph instead of issuing
+ * each kernel.  Not used while profiling is on.  CY_EINVAL before the first
+ * run; a capture that fails leaves the frame running without a graph. */
+int cy_frame_capture(cy_frame *frame);
+
 /* Wait for the frame's stream. */
 int cy_frame_sync(cy_frame *frame);
 

@@ -184,6 +184,46 @@ def test_batched_frame_matches_oracle(engine_id):
             assert_images_close(g, w, "batched")
 
 
+@pytest.mark.parametrize("engine_id", [0, 1], ids=["tile", "plain"])
+def test_graph_captured_frame_matches_oracle(engine_id):
+    """A frame run replayed from its captured CUDA graph gives the same
+    reads as the oracle (and as the run that sized it)."""
+    traces = [scenes.small_scene(cfg, 5) for cfg in ("c0_small", "c1_small", "c2_small", "mixed_small")]
+    with native.Frame(traces, engine_id) as f:
+        f.capture()
+        for _ in range(2):
+            f.run()
+        f.sync()
+        outs = f.finish()
+    for tb, raw in zip(traces, outs):
+        got = G.split_images(tb, raw)
+        want = G.split_images(tb, oracle.replay(tb)[0])
+        for g, w in zip(got, want):
+            assert_images_close(g, w, "graph")
+
+
+def test_autotuned_frame_matches_oracle():
+    """The autotuner times the paint stage over strip configurations, keeps
+    the fastest, and the frame then renders with it unchanged."""
+    traces = [scenes.small_scene(cfg, 7) for cfg in ("c0_small", "c1_small", "c2_small", "mixed_small")]
+    try:
+        with native.Frame(traces, 0) as f:
+            tuned = f.autotune()
+            assert tuned["strip_pixels"] in (2048, 4096, 8192, 12288)
+            assert tuned["threads"] in (128, 256, 512) and tuned["paint_ms"] > 0
+            f.capture()
+            f.run()
+            f.sync()
+            outs = f.finish()
+        for tb, raw in zip(traces, outs):
+            got = G.split_images(tb, raw)
+            want = G.split_images(tb, oracle.replay(tb)[0])
+            for g, w in zip(got, want):
+                assert_images_close(g, w, f"autotuned {tuned}")
+    finally:
+        native.set_strip_config(4096, 256)
+
+
 @pytest.mark.parametrize("strip_pixels", [1024, 4096, 8192])
 def test_tile_engine_strip_sizes(strip_pixels):
     native.set_strip_config(strip_pixels, 256)
