@@ -42,15 +42,21 @@ def _gen_chunk(args):
     return [scenes.c3_canvas(i, base) for i in range(first, first + count)]
 
 
-def generate(count, base_seed, workers):
+def _gen_requests(args):
+    first, count, base = args
+    from canvas_ity_gb300 import scenes
+    return [scenes.c4_request(i, base) for i in range(first, first + count)]
+
+
+def generate(count, base_seed, workers, fn=_gen_chunk):
     """Seeded call lists, generated in a spawn pool (before any GPU use)."""
     import multiprocessing as mp
     chunk = max(1, count // (workers * 4))
     jobs = [(i, min(chunk, count - i), base_seed) for i in range(0, count, chunk)]
     if workers <= 1:
-        return [t for j in jobs for t in _gen_chunk(j)]
+        return [t for j in jobs for t in fn(j)]
     with mp.get_context("spawn").Pool(workers) as pool:
-        parts = pool.map(_gen_chunk, jobs)
+        parts = pool.map(fn, jobs)
     return [t for p in parts for t in p]
 
 
@@ -233,6 +239,8 @@ def gpu_arm(args, world, rank, local):
     base_seed = args.seed + 100003 * rank
     t_gen = time.perf_counter()
     traces = generate(args.canvases, base_seed, min(cores, 16))
+    requests = generate(args.serve_requests, base_seed, min(cores, 16), _gen_requests) if (
+        rank == 0 and args.serve_requests > 0) else []
     gen_s = time.perf_counter() - t_gen
     # CPU baseline on a bounded sample (rank 0 only), before the GPU is used.
     cpu = None
@@ -330,6 +338,22 @@ def gpu_arm(args, world, rank, local):
         f.finish()
         f.close()
     plain = pixels_of(sample) / (plain_ms / 1e3) / 1e6 if plain_ms > 0 else None
+    # Serving: Poisson arrivals of mixed-size requests, continuous batching
+    # under a 150 GB admission budget (rank 0).
+    serving_out = None
+    if requests:
+        from canvas_ity_gb300 import serving
+        serving_out = {"requests_per_rate": len(requests), "budget_gb": 150, "workers": args.serve_workers,
+                       "workload": "c4: sides log-uniform 32-2048 px, 1-512 paths from the c0/c1/c2 mixture",
+                       "rates": []}
+        with serving.Server(budget_bytes=150 * 10**9, workers=args.serve_workers) as srv:
+            serving.run_poisson(srv, requests[: max(1, len(requests) // 8)], 2000.0, seed=0)   # warm-up
+            for rate in (2000.0, 10000.0, 20000.0):
+                serving_out["rates"].append(serving.run_poisson(srv, requests, rate, seed=int(rate)))
+            st = srv.stats()
+        serving_out["frames"] = st["frames"]
+        serving_out["max_batch"] = st["max_batch"]
+        serving_out["max_admitted_gb"] = round(st["max_bytes_admitted"] / 1e9, 2)
     # Roofline of the dominant kernel.
     peak, peak_kind = measured_peaks()
     per_run_ms = elapsed_ms / args.steps
@@ -376,6 +400,7 @@ def gpu_arm(args, world, rank, local):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "parity": {"canvases": len(check), "max_lsb": worst, "max_frac_pixels_differing": round(diff_frac, 6)},
+        "serving": serving_out,
         "clocks": clocks.summary(),
         "gpu_launches": stats["launches"] * args.steps,
     }
@@ -398,6 +423,8 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--parity-sample", type=int, default=8)
     ap.add_argument("--autotune", type=int, default=1, help="pick the strip configuration by timing (1) or not (0)")
+    ap.add_argument("--serve-requests", type=int, default=240, help="requests per arrival rate (0: no serving run)")
+    ap.add_argument("--serve-workers", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--strip-pixels", type=int, default=0)
     ap.add_argument("--strip-threads", type=int, default=256)

@@ -18,7 +18,7 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIB_DIR, "libcanvas_ity_gb300.so")
 
 CUDA_SOURCES = ["engine.cu"]
-HOST_SOURCES = ["canvas.cpp", "capi.cpp"]
+HOST_SOURCES = ["canvas.cpp", "capi.cpp", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v"]
@@ -55,9 +55,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
         jobs.append((cmd, src))
         objs.append(obj)
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
     for src in HOST_SOURCES:
         obj = os.path.join(BUILD, src + ".o")
-        cmd = ["g++", *HOST_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = ["g++", *HOST_FLAGS, "-I", cuda_inc, "-c", os.path.join(CSRC, src), "-o", obj]
         jobs.append((cmd, src))
         objs.append(obj)
     procs = [(subprocess.Popen(c, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True), s)

@@ -1630,8 +1630,8 @@ struct cy_frame {
     cudaStream_t stream = nullptr;
 };
 
-// Device workspaces of finished frames, at most one per device: the next
-// frame reuses its buffers instead of allocating them again.
+// Device workspaces of finished frames, a few per device: the next frames
+// reuse their buffers instead of allocating them again.
 namespace {
 std::mutex g_ws_lock;
 std::vector<std::pair<int, std::unique_ptr<frame>>> g_ws;
@@ -1645,6 +1645,8 @@ std::unique_ptr<frame> take_workspace() {
     return nullptr;
 }
 
+constexpr int kWorkspacesPerDevice = 4;   // concurrent frames (server workers) keep theirs
+
 void give_workspace(std::unique_ptr<frame> f) {
     int dev = -1;
     if (!f || f->status || cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return; }
@@ -1652,13 +1654,14 @@ void give_workspace(std::unique_ptr<frame> f) {
     std::unique_ptr<frame> spare;
     {
         std::lock_guard<std::mutex> hold(g_ws_lock);
+        int held = 0;
         for (auto &w : g_ws)
             if (w.first == dev) {
                 if (!w.second) { w.second = std::move(f); return; }
-                spare = std::move(f);   // one is kept already: free this one
-                break;
+                ++held;
             }
-        if (f) g_ws.emplace_back(dev, std::move(f));
+        if (held >= kWorkspacesPerDevice) spare = std::move(f);   // enough kept: free this one
+        else g_ws.emplace_back(dev, std::move(f));
     }
 }
 }  // namespace

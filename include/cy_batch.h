@@ -64,8 +64,8 @@ void *cy_frame_stream(cy_frame *frame);
 /* Copy the reads out, release queued resources. */
 int cy_frame_finish(cy_frame *frame);
 
-/* Destroying a frame keeps its device and pinned buffers (one set per
- * device) for the next cy_frame_create, which then allocates only what
+/* Destroying a frame keeps its device and pinned buffers (up to four sets
+ * per device) for the next cy_frame_create, which then allocates only what
  * grows.  cy_frame_workspace_release frees what is kept. */
 void cy_frame_destroy(cy_frame *frame);
 void cy_frame_workspace_release(void);
