@@ -102,6 +102,7 @@ struct canvas_state {
     brush fill, stroke, image;
     polyline path, lines, scratch;
     int mask;  // current clip mask id (0 = whole canvas)
+    bool even_odd = false;   // fill rule of fill(), clip(), is_point_in_path() (extension)
     font_face face;
     std::vector<saved_state> stack;
     // copies of the public members, refreshed before each draw
@@ -714,6 +715,7 @@ void canvas_state::make_state(cy_draw_state &s, bool with_shadow) {
     s.shadow_blur = shadow_blur;
     s.shadow_offset_x = sox;
     s.shadow_offset_y = soy;
+    s.fill_rule = 0;
 }
 
 void canvas_state::draw_lines(const brush &br, bool clamp_edges, bool force_solid, bool with_shadow) {
@@ -735,6 +737,7 @@ void canvas_state::draw_path(const brush &br) {
     cy_draw_state s;
     make_paint(br, false, false, p);
     make_state(s, true);
+    s.fill_rule = even_odd ? 1 : 0;
     counts.resize(path.subs.size());
     for (size_t i = 0; i < path.subs.size(); ++i) counts[i] = static_cast<int>(path.subs[i].count);
     note(cy_fill_path(ctx, reinterpret_cast<const float *>(path.pts.data()), counts.data(),
@@ -992,7 +995,7 @@ void canvas::clip() {
     for (size_t i = 0; i < s.path.subs.size(); ++i) s.counts[i] = static_cast<int>(s.path.subs[i].count);
     int out = s.mask;
     int rc = cy_clip_path(s.ctx, reinterpret_cast<const float *>(s.path.pts.data()), s.counts.data(),
-                          static_cast<int>(s.counts.size()), s.mask, &out);
+                          static_cast<int>(s.counts.size()), s.mask, s.even_odd ? 1 : 0, &out);
     s.note(rc);
     if (rc == 0) {
         if (s.mask) s.note(cy_mask_release(s.ctx, s.mask));
@@ -1020,8 +1023,9 @@ bool canvas::is_point_in_path(float x, float y) {
             return true;
         }
     }
-    return winding != 0;
+    return s.even_odd ? (winding & 2) != 0 : winding != 0;   // each crossing edge counts +-1 on each side: twice the winding number
 }
+void canvas::set_fill_rule(fill_rule_style rule) { self->even_odd = rule == even_odd; }
 
 static void rect_lines(detail::canvas_state &s, float x, float y, float w, float h, bool closing_point) {
     s.lines.pts.clear();

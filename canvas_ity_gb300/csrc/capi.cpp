@@ -30,6 +30,11 @@ struct traits {
     typedef canvas_ity::align_style align_style;
     typedef canvas_ity::baseline_style baseline_style;
     static std::unique_ptr<canvas> make(int w, int h) { return std::unique_ptr<canvas>(new canvas(w, h)); }
+    static bool set_fill_rule(canvas &c, int rule) {
+        if (rule != 0 && rule != 1) return false;
+        c.set_fill_rule(rule ? canvas_ity::even_odd : canvas_ity::nonzero);
+        return true;
+    }
 };
 inline canvas_ity::brush_type bt(int t) { return static_cast<canvas_ity::brush_type>(t); }
 }  // namespace
@@ -131,6 +136,9 @@ void cy_canvas_put_image_data(cy_canvas *c, const unsigned char *img, int w, int
 }
 void cy_canvas_save(cy_canvas *c) { c->get().save(); }
 void cy_canvas_restore(cy_canvas *c) { c->get().restore(); }
+void cy_canvas_set_fill_rule(cy_canvas *c, int rule) {
+    c->get().set_fill_rule(rule == 1 ? canvas_ity::even_odd : canvas_ity::nonzero);
+}
 
 int cy_take_thread_status(void);
 

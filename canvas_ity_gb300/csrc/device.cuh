@@ -308,6 +308,13 @@ __device__ __forceinline__ int clip_segment(float2 a, float2 b, float width, flo
     return n;
 }
 
+// Coverage of an accumulated signed area s under a fill rule: nonzero
+// (the reference's, hpp:2568-2570) min(|s|, 1); even-odd the distance from s
+// to the nearest even integer, so each further winding toggles coverage.
+__device__ __forceinline__ float cover_of(float s, int rule) {
+    return rule ? lo(fabsf(s - 2.0f * rintf(0.5f * s)), 1.0f) : lo(fabsf(s), 1.0f);
+}
+
 // ------------------------------------------------------------------ paint
 __device__ __forceinline__ float4 premul(float4 c) { return make_float4(c.x * c.w, c.y * c.w, c.z * c.w, c.w); }
 

@@ -864,6 +864,7 @@ int frame::run() {
             a.n_last_row = nm.last_row;
             a.W = W;
             a.H = H;
+            a.rule = cmds[op.cmd].fill_rule;
             k_clip_rows<<<(H + 127) / 128, 128, 0, stream>>>(a);
             k_mask_prefix<<<(H + 127) / 128, 128, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, H);
             k_mask_fill<<<std::max(1, (H + 7) / 8), 256, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, W, H,
@@ -1184,6 +1185,7 @@ int fill_paint(queue &q, const cy_paint *p, command &c) {
 void fill_state(const cy_draw_state *s, command &c) {
     c.op = s->operation;
     c.alpha = s->global_alpha;
+    c.fill_rule = s->fill_rule == 1 ? 1 : 0;
     c.shadow = 0;
     // render_shadow runs only for a visible shadow colour that is blurred or
     // offset (hpp:2398-2401); its parameters follow hpp:2402-2408, 2453-2459.
@@ -1465,7 +1467,8 @@ int cy_mask_release(cy_ctx *c, int mask) {
     return CY_OK;
 }
 
-int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, int mask_in, int *mask_out) {
+int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, int mask_in, int fill_rule,
+                 int *mask_out) {
     if (!c || !mask_out) return CY_EINVAL;
     if (c->status) return c->status;
     if (mask_in < 0 || mask_in >= static_cast<int>(c->masks.size()) ||
@@ -1475,6 +1478,7 @@ int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, i
     command cmd;
     std::memset(&cmd, 0, sizeof(cmd));
     cmd.kind = CMD_CLIP;
+    cmd.fill_rule = fill_rule == 1 ? 1 : 0;
     cull_rects rects = {static_cast<float>(c->W), static_cast<float>(c->H), false, 0.0f, 0.0f, 0.0f, 0.0f};
     int rc = queue_geometry(q, points, counts, n_sub, true, cmd, rects);
     if (rc != CY_OK) return rc;

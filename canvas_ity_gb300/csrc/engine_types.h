@@ -30,7 +30,7 @@ struct __align__(16) command {
     int32_t stop_first, stop_count;
     int32_t pat_first, pat_w, pat_h, pat_rep;
     // shadow (render_shadow, hpp:2395-2539)
-    int32_t shadow, sh_radius, sh_border, pad0;
+    int32_t shadow, sh_radius, sh_border, fill_rule;   // fill_rule: 0 nonzero, 1 even-odd
     float sh_color[4];
     float sh_w1, sh_w2, sh_offx, sh_offy;
     // put_image_data

@@ -753,10 +753,10 @@ __global__ void k_paint(paint_args a) {
         // sum up to the clip's end (hpp:2572-2600): that matters when the
         // float sum is left above the visibility threshold.
         int xs = clearing ? 0 : r[0].x;
-        bool tail = n > 0 && lo(fabsf(sm[n - 1]), 1.0f) >= kVisible;
+        bool tail = n > 0 && cover_of(sm[n - 1], c.fill_rule) >= kVisible;
         int xe = clearing || tail ? a.W - 1 : min(r[n - 1].x, a.W - 1);
         for (int x = xs + lane; x <= xe; x += 32) {
-            float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+            float cov = cover_of(sum_at(r, sm, n, x), c.fill_rule);
             float vis = a.vis ? a.vis[static_cast<size_t>(y) * a.W + x] : 1.0f;
             if ((cov >= kVisible || clearing) && vis >= kVisible) {
                 float4 *px = a.bitmap + static_cast<size_t>(y) * a.W + x;
@@ -788,6 +788,7 @@ struct clip_args {
     run *n_runs;
     int *n_last_row;
     int W, H;
+    int rule;                // fill rule of the clip path
 };
 
 // clip() (hpp:3057-3099) for one row: merge the path runs with the old mask
@@ -825,7 +826,7 @@ __global__ void k_clip_rows(clip_args a) {
             int nx = which ? p[i1].x : o[i2].x;
             if (which) s1 += p[i1++].delta;
             else s2 += o[i2++].delta;
-            float vis = lo(fabsf(s1), 1.0f) * lo(fabsf(s2), 1.0f);
+            float vis = cover_of(s1, a.rule) * lo(fabsf(s2), 1.0f);
             if (vis == last) continue;
             if (m > 0 && out[m - 1].x == nx) out[m - 1].delta += vis - last;
             else if (m < cap) out[m++] = run{nx, vis - last};
@@ -925,7 +926,7 @@ __global__ void k_shadow_raster(const command *cmd, paint_src src, row_view rv, 
         for (int x = rc.left + lane; x < rc.right; x += 32) {
             float val = 0.0f;
             if (x >= first && x <= last) {
-                float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+                float cov = cover_of(sum_at(r, sm, n, x), c.fill_rule);
                 if (cov >= kVisible) {
                     float px = (static_cast<float>(x) + 0.5f) - c.sh_offx;
                     float py = (static_cast<float>(y) + 0.5f) - c.sh_offy;

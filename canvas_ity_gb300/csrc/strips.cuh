@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
                     first_x = n ? r[0].x : 0x7fffffff;
                     // Past the last run the row's final sum still paints
                     // up to the clip's end when it is visible (see k_paint).
-                    last_x = n ? (lo(fabsf(sm[n - 1]), 1.0f) >= kVisible ? W - 1 : r[n - 1].x) : -1;
+                    last_x = n ? (cover_of(sm[n - 1], c.fill_rule) >= kVisible ? W - 1 : r[n - 1].x) : -1;
                 }
                 int xs = clearing ? 0 : first_x;
                 int xe = clearing ? W - 1 : min(last_x, W - 1);
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
                 if (upto) v = from_run;
                 if (k > 0) carry = __shfl_sync(0xffffffffu, rs, k - 1);
                 j += k;
-                if (!clearing && k == 0 && lo(fabsf(carry), 1.0f) < kVisible) {
+                if (!clearing && k == 0 && cover_of(carry, c.fill_rule) < kVisible) {
                     // Nothing visible here nor up to the next run: jump to
                     // the chunk that holds it (or past this row).
                     int nx = __shfl_sync(0xffffffffu, rx, 0);
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
                 int x = x0 + lane;
                 if (x < xs || x > xe) continue;
                 int y = y0 + ly;
-                float cov = lo(fabsf(v), 1.0f);
+                float cov = cover_of(v, c.fill_rule);
                 float vis = e.vis ? e.vis[static_cast<size_t>(y) * W + x] : 1.0f;
                 if ((cov >= kVisible || clearing) && vis >= kVisible) {
                     float4 p = paint_at(c, P.src, static_cast<float>(x) + 0.5f, static_cast<float>(y) + 0.5f);
@@ -287,7 +287,7 @@ __global__ void k_shadow_raster_all(const shadow_job *sj, const command *cmds, p
         for (int x = rc.left + lane; x < rc.right; x += 32) {
             float val = 0.0f;
             if (x >= first && x <= last) {
-                float cov = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+                float cov = cover_of(sum_at(r, sm, n, x), c.fill_rule);
                 if (cov >= kVisible) {
                     float pxx = (static_cast<float>(x) + 0.5f) - c.sh_offx;
                     float pyy = (static_cast<float>(y) + 0.5f) - c.sh_offy;

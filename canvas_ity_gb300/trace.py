@@ -35,6 +35,8 @@ FILL, STROKE, CLIP, IS_POINT_IN_PATH = 33, 34, 35, 36
 CLEAR_RECTANGLE, FILL_RECTANGLE, STROKE_RECTANGLE = 37, 38, 39
 SET_TEXT_ALIGN, SET_TEXT_BASELINE, SET_FONT, FILL_TEXT, STROKE_TEXT, MEASURE_TEXT = 40, 41, 42, 43, 44, 45
 DRAW_IMAGE, GET_IMAGE_DATA, PUT_IMAGE_DATA, SAVE, RESTORE = 46, 47, 48, 49, 50
+SET_FILL_RULE = 51                    # extension: 0 nonzero, 1 even-odd
+NONZERO, EVEN_ODD = 0, 1
 
 # Public enums (src/canvas_ity.hpp:146-156).
 SOURCE_IN, SOURCE_COPY, SOURCE_OUT, DESTINATION_IN = 1, 2, 3, 4
@@ -179,6 +181,8 @@ class TraceWriter:
         return self._op(PUT_IMAGE_DATA, struct.pack("<5i", w, h, x, y, 0 if image is None else 1),
                         _image_bytes(image, w, h))
 
+    def set_fill_rule(self, rule): return self._ops(SET_FILL_RULE, "i", rule)
+
     def save(self): return self._op(SAVE)
     def restore(self): return self._op(RESTORE)
 
@@ -204,6 +208,7 @@ _FIXED = {  # opcode -> struct format of a fixed-size payload
     BEZIER_CURVE_TO: "6f", ARC_TO: "5f", ARC: "5fi", RECTANGLE: "4f", FILL: "", STROKE: "",
     CLIP: "", IS_POINT_IN_PATH: "ffi", CLEAR_RECTANGLE: "4f", FILL_RECTANGLE: "4f",
     STROKE_RECTANGLE: "4f", SET_TEXT_ALIGN: "i", SET_TEXT_BASELINE: "i", SAVE: "", RESTORE: "",
+    SET_FILL_RULE: "i",
 }
 
 

@@ -43,6 +43,8 @@ enum repetition_style { repeat, repeat_x, repeat_y, no_repeat };
 enum align_style { leftward, rightward, center, start = 0, ending };
 enum baseline_style {
     alphabetic, top, middle, bottom, hanging, ideographic = 3 };
+// Extension, no reference counterpart (the reference fills nonzero only).
+enum fill_rule_style { nonzero, even_odd };
 
 namespace detail { struct canvas_state; }
 
@@ -135,6 +137,11 @@ public:
     // Canvas state (hpp:1126-1145).
     void save();
     void restore();
+
+    // Extension, no reference counterpart: the winding rule of fill(),
+    // clip() and is_point_in_path() (nonzero by default, as in the
+    // reference).  Strokes, text and rectangles always fill nonzero.
+    void set_fill_rule( fill_rule_style rule );
 
     // Extension, no reference counterpart: 0 if every GPU operation so far
     // succeeded, else the first negative status (see cy_gpu.h).  The

@@ -78,6 +78,9 @@ void cy_canvas_put_image_data(cy_canvas *c, const unsigned char *image, int widt
                               int stride, int x, int y);                        /* hpp:1097-1124 */
 void cy_canvas_save(cy_canvas *c);                                              /* hpp:1128-1136 */
 void cy_canvas_restore(cy_canvas *c);                                           /* hpp:1138-1145 */
+/* Extension, no reference counterpart: 0 nonzero (default), 1 even-odd for
+ * fill(), clip() and is_point_in_path(). */
+void cy_canvas_set_fill_rule(cy_canvas *c, int rule);
 
 /* Replay a recorded call list (cy_trace.h) through canvas_ity::canvas.
  * Every non-null get_image_data appends its compact RGBA8 rectangle to

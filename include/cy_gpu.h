@@ -65,6 +65,7 @@ typedef struct cy_draw_state {
     float shadow_color[4];     /* premultiplied linear                        */
     float shadow_blur;
     float shadow_offset_x, shadow_offset_y;
+    int fill_rule;             /* extension: 0 nonzero (the reference's), 1 even-odd */
 } cy_draw_state;
 
 /* canvas::canvas (hpp:2607-2644): transparent W x H canvas, full clip. */
@@ -87,11 +88,12 @@ int cy_fill_path(cy_ctx *ctx, const float *points, const int *subpath_counts, in
 int cy_fill_lines(cy_ctx *ctx, const float *points, const int *subpath_counts, int n_subpaths,
                   const cy_paint *paint, const cy_draw_state *state);
 
-/* clip() (hpp:3057-3099): intersects mask `mask_in` with the nonzero
- * coverage of the Bezier path; the new mask id is written to *mask_out.
- * Mask ids are reference counted: a new mask starts with one reference. */
+/* clip() (hpp:3057-3099): intersects mask `mask_in` with the coverage of
+ * the Bezier path under `fill_rule` (0 nonzero as in the reference, 1
+ * even-odd); the new mask id is written to *mask_out.  Mask ids are
+ * reference counted: a new mask starts with one reference. */
 int cy_clip_path(cy_ctx *ctx, const float *points, const int *subpath_counts, int n_subpaths,
-                 int mask_in, int *mask_out);
+                 int mask_in, int fill_rule, int *mask_out);
 
 /* Reference counting of mask ids for save()/restore() (hpp:3410-3465). */
 int cy_mask_retain(cy_ctx *ctx, int mask);

@@ -295,6 +295,11 @@ int replay(const uint8_t *data, size_t size, output &out,
             c->put_image_data(px, w, h, w * 4, x, y);
             break;
         }
+        case CYT_SET_FILL_RULE: {
+            int32_t rule = in.i32();
+            if (!in.ok || !Traits::set_fill_rule(*c, rule)) return -1;
+            break;
+        }
         case CYT_SAVE: c->save(); break;
         case CYT_RESTORE: c->restore(); break;
         default:

@@ -77,7 +77,8 @@ enum cy_trace_op {
                                     u8[w*h*4] if nonnull && w > 0 && h > 0 */
     CYT_SAVE = 49,
     CYT_RESTORE = 50,
-    CYT_OP_COUNT = 51
+    CYT_SET_FILL_RULE = 51,      /* i32 rule: 0 nonzero, 1 even-odd (extension, no reference counterpart) */
+    CYT_OP_COUNT = 52
 };
 
 #endif /* CY_TRACE_H */

@@ -50,7 +50,10 @@ def build_reference(force: bool = False) -> Optional[str]:
     """Build the reference tools from the read-only sources, if present."""
     if not os.path.isfile(os.path.join(REFERENCE_ROOT, "src", "canvas_ity.hpp")):
         return None
-    if force or not os.path.exists(REF_SO):
+    ours = [os.path.join(HERE, "ref", f) for f in os.listdir(os.path.join(HERE, "ref"))]
+    ours += [os.path.join(HERE, "..", "include", h) for h in ("cy_trace.h", "cy_replay.hpp")]
+    stale = not os.path.exists(REF_SO) or os.path.getmtime(REF_SO) < max(os.path.getmtime(p) for p in ours)
+    if force or stale:
         subprocess.check_call(["sh", os.path.join(HERE, "ref", "build_ref.sh"), REFERENCE_ROOT])
     return REF_SO
 

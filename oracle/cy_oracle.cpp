@@ -183,7 +183,16 @@ public:
     void arc_to(float vx, float vy, float x, float y, float radius);
     void arc(float x, float y, float radius, float a0, float a1, bool ccw = false);
     void rectangle(float x, float y, float w, float h);
-    void fill() { flatten(false); render(fill_br, false); }
+    void fill() {
+        flatten(false);
+        cur_rule = fill_rule;
+        render(fill_br, false);
+        cur_rule = 0;
+    }
+    // Extension (no reference counterpart): the fill rule of fill(), clip()
+    // and is_point_in_path(); 0 nonzero (the reference's only rule), 1
+    // even-odd.  Strokes, text and rectangles always fill nonzero.
+    int fill_rule = 0;
     void stroke() { flatten(true); stroke_outline(); render(stroke_br, false); }
     void clip();
     bool is_point_in_path(float x, float y);
@@ -218,6 +227,13 @@ private:
         std::vector<run> mask; font face;
     };
     int W, H;
+    int cur_rule = 0;   // rule of the draw being rendered
+    // Coverage of an accumulated signed area s: min(|s|, 1) for nonzero;
+    // for even-odd the distance from s to the nearest even integer, so each
+    // further winding toggles coverage.
+    float cover(float s) const {
+        return cur_rule ? lo(fabsf(s - 2.0f * rintf(0.5f * s)), 1.0f) : lo(fabsf(s), 1.0f);
+    }
     mat fwd, inv;
     float g_alpha;
     col sh_color;
@@ -1153,7 +1169,7 @@ void canvas::render_shadow(const brush &br, bool clamp_edges) {
         float sum = 0.0f;
         for (size_t i = 0; i < runs.size(); ++i) {
             run next = runs[i];
-            float coverage = lo(fabsf(sum), 1.0f);
+            float coverage = cover(sum);
             int to = next.y == y ? next.x : x + 1;
             if (coverage >= kVisible)
                 for (; x < to; ++x)
@@ -1234,7 +1250,7 @@ void canvas::render(const brush &br, bool clamp_edges) {
     while (ci < mask.size()) {
         bool from_path = pi < runs.size() && run_before(runs[pi], mask[ci]);
         run next = from_path ? runs[pi] : mask[ci];
-        float coverage = lo(fabsf(psum), 1.0f);
+        float coverage = cover(psum);
         float vis = lo(fabsf(csum), 1.0f);
         int to = next.y == y ? next.x : x + 1;
         if ((coverage >= kVisible || ~op & 8) && vis >= kVisible)
@@ -1259,6 +1275,7 @@ void canvas::render(const brush &br, bool clamp_edges) {
 void canvas::clip() {
     flatten(false);
     scan(mk(0.0f, 0.0f), 0);
+    cur_rule = fill_rule;
     size_t part = runs.size();
     runs.insert(runs.end(), mask.begin(), mask.end());
     mask.clear();
@@ -1276,7 +1293,7 @@ void canvas::clip() {
         }
         if (first) s1 += runs[i1++].delta;
         else s2 += runs[i2++].delta;
-        float vis = lo(fabsf(s1), 1.0f) * lo(fabsf(s2), 1.0f);
+        float vis = cover(s1) * lo(fabsf(s2), 1.0f);
         if (vis == last) continue;
         if (!mask.empty() && mask.back().x == next.x && mask.back().y == next.y) {
             mask.back().delta += vis - last;
@@ -1286,6 +1303,7 @@ void canvas::clip() {
         }
         last = vis;
     }
+    cur_rule = 0;
 }
 
 // ---- hit test (hpp:3101-3132) ----
@@ -1308,7 +1326,7 @@ bool canvas::is_point_in_path(float x, float y) {
             return true;
         }
     }
-    return winding;
+    return fill_rule ? (winding & 2) != 0 : winding != 0;   // each crossing edge counts +-1 on each side: twice the winding number
 }
 
 // ---- rectangles and images (hpp:3134-3346) ----
@@ -1445,6 +1463,11 @@ struct traits {
     typedef cyo::align_style align_style;
     typedef cyo::baseline_style baseline_style;
     static std::unique_ptr<canvas> make(int w, int h) { return std::unique_ptr<canvas>(new canvas(w, h)); }
+    static bool set_fill_rule(canvas &c, int rule) {
+        if (rule != 0 && rule != 1) return false;
+        c.fill_rule = rule;
+        return true;
+    }
 };
 
 }  // namespace cyo

@@ -31,6 +31,8 @@ struct ref_traits {
     static std::unique_ptr<canvas_type> make(int w, int h) {
         return std::unique_ptr<canvas_type>(new canvas_type(w, h));
     }
+    // The reference fills nonzero only.
+    static bool set_fill_rule(canvas_type &, int rule) { return rule == 0; }
 };
 }  // namespace
 

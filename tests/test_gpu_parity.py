@@ -107,6 +107,21 @@ def test_float_canvas_bit_exact_batched_workload(engine, seed):
     assert_float_canvas_exact(scenes.c3_canvas(seed), f"c3 canvas {seed}")
 
 
+def _even_odd(tb):
+    """The same call list with the even-odd fill rule set right after the
+    canvas record (header 8 bytes + canvas record 12 bytes)."""
+    import struct
+    return tb[:20] + struct.pack("<ii", T.SET_FILL_RULE, T.EVEN_ODD) + tb[20:]
+
+
+@pytest.mark.parametrize("config", ["c0_small", "c1_small", "c2_small", "mixed_small"])
+@pytest.mark.parametrize("seed", range(2))
+def test_even_odd_float_canvas_bit_exact(engine, config, seed):
+    """Even-odd fills, clips and shadows (an extension: pinned to the oracle's
+    restatement of the rule, no reference output exists)."""
+    assert_float_canvas_exact(_even_odd(scenes.small_scene(config, seed)), f"even-odd {config}/{seed}")
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_float_coverage(engine, seed):
     """One opaque white nonzero fill on a blank canvas: the linear alpha is the
