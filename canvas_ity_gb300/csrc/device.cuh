@@ -431,15 +431,29 @@ __device__ __forceinline__ float4 blend(float4 back, float4 fore, int op, float 
 }
 
 // get_image_data's per-pixel conversion (hpp:3348-3381): unpremultiply,
-// clamp, delinearize, x255 plus the 4x4 Bayer threshold, truncate.
-__device__ __forceinline__ float delinearize(float v) {
-    return v < 0.0031308f ? 12.92f * v : 1.055f * powf(v, 1.0f / 2.4f) - 0.055f;
+// clamp, delinearize, x255 plus the 4x4 Bayer threshold, truncate.  The
+// colour bytes come from a table built on the host with the reference's own
+// formula: g_srgb_thr[d][q] is the least clamped value whose byte under
+// Bayer cell d is at least q, so the byte is the count of thresholds at or
+// below the value.  A fast estimate lands within a step or two of it and
+// the table settles it; the bytes are then exactly the host formula's.
+__device__ float g_srgb_thr[16][256];
+
+__device__ __constant__ float kBayer[16] = {0.03125f, 0.53125f, 0.15625f, 0.65625f, 0.78125f, 0.28125f,
+                                            0.90625f, 0.40625f, 0.21875f, 0.71875f, 0.09375f, 0.59375f,
+                                            0.96875f, 0.46875f, 0.84375f, 0.34375f};
+
+__device__ __forceinline__ int srgb_byte(float u, int d, float t) {
+    float s = u < 0.0031308f ? 12.92f * u : 1.055f * __powf(u, 1.0f / 2.4f) - 0.055f;
+    int q = __float2int_rz(t + 255.0f * s);
+    q = q < 0 ? 0 : q > 255 ? 255 : q;
+    const float *T = g_srgb_thr[d];
+    while (q < 255 && u >= T[q + 1]) ++q;
+    while (q > 0 && u < T[q]) --q;
+    return q;
 }
+
 __device__ __forceinline__ uchar4 to_srgb8(float4 c, int cx, int cy) {
-    const float bayer[4][4] = {{0.03125f, 0.53125f, 0.15625f, 0.65625f},
-                               {0.78125f, 0.28125f, 0.90625f, 0.40625f},
-                               {0.21875f, 0.71875f, 0.09375f, 0.59375f},
-                               {0.96875f, 0.46875f, 0.84375f, 0.34375f}};
     float4 u;
     if (c.w < kVisible) {
         u = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -451,14 +465,12 @@ __device__ __forceinline__ uchar4 to_srgb8(float4 c, int cx, int cy) {
     u.y = lo(hi(u.y, 0.0f), 1.0f);
     u.z = lo(hi(u.z, 0.0f), 1.0f);
     u.w = lo(hi(u.w, 0.0f), 1.0f);
-    float t = bayer[cy & 3][cx & 3];
-    float r = t + 255.0f * delinearize(u.x);
-    float g = t + 255.0f * delinearize(u.y);
-    float b = t + 255.0f * delinearize(u.z);
+    int d = ((cy & 3) << 2) | (cx & 3);
+    float t = kBayer[d];
     float a = t + 255.0f * u.w;
-    return make_uchar4(static_cast<unsigned char>(__float2int_rz(r) & 0xff),
-                       static_cast<unsigned char>(__float2int_rz(g) & 0xff),
-                       static_cast<unsigned char>(__float2int_rz(b) & 0xff),
+    return make_uchar4(static_cast<unsigned char>(srgb_byte(u.x, d, t)),
+                       static_cast<unsigned char>(srgb_byte(u.y, d, t)),
+                       static_cast<unsigned char>(srgb_byte(u.z, d, t)),
                        static_cast<unsigned char>(__float2int_rz(a) & 0xff));
 }
 

@@ -114,6 +114,62 @@ const float *linear_lut_host() {
     return lut;
 }
 
+// get_image_data's colour byte (hpp:3348-3381, delinearized at hpp:1287-1289)
+// for clamped value u under Bayer threshold t, with host powf.
+int srgb_byte_host(float u, float t) {
+    float s = u < 0.0031308f ? 12.92f * u : 1.055f * powf(u, 1.0f / 2.4f) - 0.055f;
+    return static_cast<int>(t + 255.0f * s);
+}
+
+// thr[d][q]: the least u in [0, 1] whose byte under Bayer cell d is >= q
+// (+inf when none), found by bisection over the float bit patterns; the
+// byte only grows with u, so the byte of u is the count of q >= 1 with
+// thr[d][q] <= u.
+const float *srgb_thresholds_host() {
+    static float thr[16][256];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        static const float bayer[16] = {0.03125f, 0.53125f, 0.15625f, 0.65625f, 0.78125f, 0.28125f,
+                                        0.90625f, 0.40625f, 0.21875f, 0.71875f, 0.09375f, 0.59375f,
+                                        0.96875f, 0.46875f, 0.84375f, 0.34375f};
+        for (int d = 0; d < 16; ++d) {
+            thr[d][0] = 0.0f;
+            for (int q = 1; q < 256; ++q) {
+                uint32_t lo_b = 0, hi_b = 0x3f800000u;   // bit patterns of 0 and 1
+                float one = 1.0f;
+                if (srgb_byte_host(one, bayer[d]) < q) {
+                    thr[d][q] = INFINITY;
+                    continue;
+                }
+                while (lo_b < hi_b) {   // least pattern whose byte reaches q
+                    uint32_t mid = lo_b + (hi_b - lo_b) / 2;
+                    float u;
+                    std::memcpy(&u, &mid, 4);
+                    if (srgb_byte_host(u, bayer[d]) >= q) hi_b = mid; else lo_b = mid + 1;
+                }
+                std::memcpy(&thr[d][q], &lo_b, 4);
+            }
+        }
+    });
+    return &thr[0][0];
+}
+
+// Upload the threshold table to the current device once.
+int ensure_srgb_table() {
+    static std::mutex lock;
+    static bool done[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); return CY_ENODEV; }
+    std::lock_guard<std::mutex> hold(lock);
+    if (done[dev]) return CY_OK;
+    if (cudaMemcpyToSymbol(g_srgb_thr, srgb_thresholds_host(), sizeof(float) * 16 * 256) != cudaSuccess) {
+        cudaGetLastError();
+        return CY_ECUDA;
+    }
+    done[dev] = true;
+    return CY_OK;
+}
+
 inline size_t align256(size_t v) { return (v + 255) & ~static_cast<size_t>(255); }
 
 // Host-side queue of one context.
@@ -532,6 +588,7 @@ static bool needs_clip(const command &c, float wd, float ht, float ox, float oy)
 }
 
 int frame::prepare() {
+    if (int rc = ensure_srgb_table()) return fail(rc);
     gather();
     std::vector<command> &cmds = all.cmds;
     for (cy_ctx *c : cvs) {
@@ -1613,6 +1670,9 @@ extern "C" int cy_get_image_noalloc(cy_ctx *c, unsigned char *image, int w, int 
         g_noalloc_addr[dev] = static_cast<uchar4 *>(addr);
     }
     uchar4 *staging = g_noalloc_addr[dev];
+    // The colour conversion's threshold table (16 KiB, also a fixed array)
+    // is uploaded to the device by its first use in this process.
+    if (int rc = ensure_srgb_table()) return rc;
     // k_get writes every pixel of the w x h rectangle (zero outside the
     // canvas), so nothing in the array has to start at zero.
     dim3 blk(32, 32), grd((w + 31) / 32, (h + 31) / 32);

@@ -128,8 +128,10 @@ int cy_flush(cy_ctx *ctx);
  * cy_get_image, staging in one fixed device array instead of allocated
  * memory, and calls no allocating routine.
  *   - Call with the context's device current.  The first call on a device
- *     looks up the array's device address (cudaGetSymbolAddress); make that
- *     first call before any stream capture on the device.
+ *     looks up the array's device address (cudaGetSymbolAddress) and, if no
+ *     frame has run on the device yet, copies the 16 KiB colour-conversion
+ *     table into its fixed device array; make that first call before any
+ *     stream capture on the device.
  *   - Fails with CY_EINVAL when width*height exceeds
  *     CY_GET_IMAGE_NOALLOC_MAX_PIXELS, when stride < 4*width, or when the
  *     context still holds queued commands (run cy_flush first: a flush may

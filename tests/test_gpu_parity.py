@@ -90,6 +90,25 @@ def assert_float_canvas_exact(tb, what):
 
 
 @pytest.mark.parametrize("entry", MANIFEST, ids=[e["name"] for e in MANIFEST])
+def test_reference_suite_bytes_identical(engine, entry):
+    """Beyond the tolerance: every get_image_data byte of the reference's own
+    suite equals the recorded reference output."""
+    tb = G.load_fixture(entry)
+    got = G.split_images(tb, native.replay(tb)[0])
+    want = [img for _, _, img in T.parse(tb).expected_images()]
+    for i, (g, w) in enumerate(zip(got, want)):
+        assert np.array_equal(g, w), f"{entry['name']} read {i}: {int((g != w).any(axis=-1).sum())} pixels differ"
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_rgba8_identical_to_oracle_on_workload(engine, seed):
+    """RGBA8 bytes of many-canvas workload canvases equal the oracle's with
+    the GPU's order for runs std::sort leaves unordered."""
+    tb = scenes.c3_canvas(100 + seed)
+    assert native.replay(tb)[0] == oracle.replay(tb, ties="sign")[0]
+
+
+@pytest.mark.parametrize("entry", MANIFEST, ids=[e["name"] for e in MANIFEST])
 def test_float_canvas_bit_exact_reference_suite(engine, entry):
     assert_float_canvas_exact(G.load_fixture(entry), entry["name"])
 
