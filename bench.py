@@ -152,13 +152,18 @@ def measured_peaks():
 
 
 def ncu_traffic(kernel):
-    """DRAM bytes per unit of work of a kernel from the committed ncu summary."""
-    path = os.path.join(HERE, "profiles", "ncu_traffic.json")
+    """(DRAM bytes per canvas pixel, issue %, FP32-pipe %) of a kernel from the
+    committed ncu summary profiles/ncu_traffic.md, or None."""
+    path = os.path.join(HERE, "profiles", "ncu_traffic.md")
     try:
         with open(path) as f:
-            return json.load(f).get(kernel)
+            for line in f:
+                cells = [c.strip() for c in line.strip().strip("|").split("|")]
+                if len(cells) == 4 and cells[0] == kernel:
+                    return float(cells[1]), float(cells[2]), float(cells[3])
     except (OSError, ValueError):
         return None
+    return None
 
 
 def dist_setup():
@@ -368,11 +373,13 @@ def gpu_arm(args, world, rank, local):
         alg = 20 * stats["segments"] * 2 + 8 * stats["runs"] * 3 + 16 * stats["rows"]
         kms = scan_ms
     achieved = alg / (kms / 1e3) / 1e9 if kms > 0 else 0.0
-    traffic_per_px = ncu_traffic(kernel)
+    prof = ncu_traffic(kernel)
     roofline = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": (round(traffic_per_px * stats["pixels"]) if traffic_per_px else None),
-                "algorithmic_bytes": alg, "kernel_ms": round(kms, 3)}
+                "traffic": (round(prof[0] * stats["pixels"]) if prof else None),
+                "algorithmic_bytes": alg, "kernel_ms": round(kms, 3),
+                "note": "compute/latency-bound: see issue/fp32 utilisation (ncu, profiles/)",
+                "issue_pct": prof[1] if prof else None, "fp32_pipe_pct": prof[2] if prof else None}
     if rank != 0:
         if world > 1:
             import torch.distributed as dist
