@@ -353,19 +353,46 @@ __device__ float4 paint_at(const command &c, const paint_src &s, float px, float
         float4 total = none;
         float wsum = 0.0f;
         const float4 *tex = s.texels + c.pat_first;
+        // The column weights and wrapped columns are the same for every row
+        // of taps: computed once (same values, same order of the sums).
+        constexpr int kTaps = 8;
+        float wxs[kTaps];
+        int xxs[kTaps];
+        const int ncols = right - left;
+        const bool cached = ncols <= kTaps;
+        int x0w = left % c.pat_w;
+        if (x0w < 0) x0w += c.pat_w;
+        if (cached) {
+            int xx = x0w;
+            for (int j = 0; j < ncols; ++j) {
+                int px_ = left + j;
+                wxs[j] = keys_weight(fabsf(rx * (static_cast<float>(px_) - x)));
+                xxs[j] = c.clamp ? (px_ < 0 ? 0 : (px_ > c.pat_w - 1 ? c.pat_w - 1 : px_)) : xx;
+                if (++xx == c.pat_w) xx = 0;
+            }
+        }
+        int yy = top % c.pat_h;
+        if (yy < 0) yy += c.pat_h;
         for (int py_ = top; py_ < bottom; ++py_) {
             float wy = keys_weight(fabsf(ry * (static_cast<float>(py_) - y)));
-            int yy = py_ % c.pat_h;
-            if (yy < 0) yy += c.pat_h;
-            if (c.clamp) yy = py_ < 0 ? 0 : (py_ > c.pat_h - 1 ? c.pat_h - 1 : py_);
-            const float4 *rowp = tex + static_cast<size_t>(yy) * c.pat_w;
-            for (int px_ = left; px_ < right; ++px_) {
-                float wx = keys_weight(fabsf(rx * (static_cast<float>(px_) - x)));
-                int xx = px_ % c.pat_w;
-                if (xx < 0) xx += c.pat_w;
-                if (c.clamp) xx = px_ < 0 ? 0 : (px_ > c.pat_w - 1 ? c.pat_w - 1 : px_);
+            int ry_ = c.clamp ? (py_ < 0 ? 0 : (py_ > c.pat_h - 1 ? c.pat_h - 1 : py_)) : yy;
+            if (++yy == c.pat_h) yy = 0;
+            const float4 *rowp = tex + static_cast<size_t>(ry_) * c.pat_w;
+            int xx = x0w;
+            for (int j = 0; j < ncols; ++j) {
+                int px_ = left + j;
+                float wx;
+                int col;
+                if (cached) {
+                    wx = wxs[j];
+                    col = xxs[j];
+                } else {
+                    wx = keys_weight(fabsf(rx * (static_cast<float>(px_) - x)));
+                    col = c.clamp ? (px_ < 0 ? 0 : (px_ > c.pat_w - 1 ? c.pat_w - 1 : px_)) : xx;
+                    if (++xx == c.pat_w) xx = 0;
+                }
                 float w = wx * wy;
-                float4 t = rowp[xx];
+                float4 t = rowp[col];
                 total.x = total.x + t.x * w;
                 total.y = total.y + t.y * w;
                 total.z = total.z + t.z * w;
