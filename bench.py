@@ -317,7 +317,7 @@ def gpu_arm(args, world, rank, local):
         t0 = time.perf_counter()
         f = native.Frame(traces, 0)
         st = f.stats()
-        outs = f.finish()
+        outs = f.finish(copy=False)
         t_close = time.perf_counter()
         f.close()
         t_e2e += time.perf_counter() - t0

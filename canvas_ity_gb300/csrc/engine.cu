@@ -172,6 +172,85 @@ int ensure_srgb_table() {
 
 inline size_t align256(size_t v) { return (v + 255) & ~static_cast<size_t>(255); }
 
+// Run fn(i) for i < n on up to 16 host threads (inline for small n).
+template <class Fn>
+void parallel_for(size_t n, Fn fn) {
+    int threads = static_cast<int>(std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 16));
+    if (n < 64 || threads <= 1) {
+        for (size_t i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+        for (size_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) fn(i);
+    };
+    std::vector<std::thread> pool;
+    try {
+        for (int t = 1; t < threads; ++t) pool.emplace_back(work);
+    } catch (...) {
+    }
+    work();
+    for (std::thread &t : pool) t.join();
+}
+
+// Canvas buffers are recycled through a per-device pool of size classes
+// (steps of 1/4 of a power of two), so replaying canvases does not call
+// cudaMalloc/cudaFree (which synchronises the device) for each of them.
+struct canvas_pool {
+    std::mutex m;
+    std::vector<std::pair<size_t, void *>> free;   // (class bytes, buffer)
+    size_t pooled = 0;
+};
+constexpr size_t kPoolCap = size_t(16) << 30;
+canvas_pool g_pools[64];
+
+size_t pool_class(size_t bytes) {
+    size_t c = 256;
+    while (c < bytes) c <<= 1;
+    size_t q = c / 8;   // candidates 5/8, 6/8, 7/8, 8/8 of the power of two
+    for (size_t k = 5; k <= 8; ++k)
+        if (q * k >= bytes) return q * k;
+    return c;
+}
+
+void *pool_get(size_t bytes, size_t *got) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    size_t cls = pool_class(bytes);
+    *got = cls;
+    if (dev >= 0 && dev < 64) {
+        canvas_pool &p = g_pools[dev];
+        std::lock_guard<std::mutex> hold(p.m);
+        for (size_t i = 0; i < p.free.size(); ++i)
+            if (p.free[i].first == cls) {
+                void *b = p.free[i].second;
+                p.free[i] = p.free.back();
+                p.free.pop_back();
+                p.pooled -= cls;
+                return b;
+            }
+    }
+    void *b = nullptr;
+    if (cudaMalloc(&b, cls) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return b;
+}
+
+void pool_put(void *b, size_t cls) {
+    if (!b) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64) {
+        canvas_pool &p = g_pools[dev];
+        std::lock_guard<std::mutex> hold(p.m);
+        if (p.pooled + cls <= kPoolCap) {
+            p.free.emplace_back(cls, b);
+            p.pooled += cls;
+            return;
+        }
+    }
+    cudaFree(b);
+}
+
 // Host-side queue of one context.
 struct queue {
     std::vector<command> cmds;
@@ -207,6 +286,7 @@ struct cy_ctx {
     bool has_content = false;   // bitmap holds more than transparent black
     cudaStream_t stream = nullptr;
     float4 *bitmap = nullptr;
+    size_t bitmap_bytes = 0;        // size class of the pooled buffer
     std::vector<mask_slot> masks;   // id 0 unused (whole canvas)
     std::vector<mask_slot> dead;    // released masks, freed at the next frame
     queue q;
@@ -557,23 +637,7 @@ void frame::stage(char *h) {
         if (!q.put_px.empty())
             std::memcpy(h + o_put + static_cast<size_t>(b.put), q.put_px.data(), q.put_px.size());
     };
-    size_t n = cvs.size();
-    int threads = static_cast<int>(std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), 16));
-    if (n < 64 || threads <= 1) {
-        for (size_t ci = 0; ci < n; ++ci) copy_ctx(ci);
-        return;
-    }
-    std::atomic<size_t> next(0);
-    auto work = [&]() {
-        for (size_t ci = next.fetch_add(1); ci < n; ci = next.fetch_add(1)) copy_ctx(ci);
-    };
-    std::vector<std::thread> pool;
-    try {
-        for (int t = 1; t < threads; ++t) pool.emplace_back(work);
-    } catch (...) {
-    }
-    work();
-    for (std::thread &t : pool) t.join();
+    parallel_for(cvs.size(), copy_ctx);
 }
 
 // Whether a job's points (command bounds moved by the job's offset) can fall
@@ -1074,7 +1138,7 @@ int frame::build_strips() {
         s.cmd_first = cursor;
         s.cmd_count = static_cast<int32_t>(cv->q.cmds.size());
         cursor += s.cmd_count;
-        s.flags = (cv->has_content ? 1 : 0) | (cv->deferred ? 0 : 2);
+        s.flags = (cv->has_content ? 1 : 0) | 2;   // every canvas keeps its pixels for later frames
         s.bitmap = cv->bitmap;
         int64_t cost = static_cast<int64_t>(s.TH) * s.W * (s.cmd_count + 1);
         for (int y = 0; y < s.H; y += s.TH) work.push_back({cost, make_int2(static_cast<int>(ci), y)});
@@ -1145,24 +1209,38 @@ int frame::finish() {
                                              cudaMemcpyDeviceToHost, stream)))
         return status;
     if (!ok(cudaStreamSynchronize(stream))) return status;
-    // Deliver reads: to the caller's buffer, or keep them for deferred readers.
-    size_t g = 0;
-    for (size_t i = 0; i < all.cmds.size(); ++i) {
-        const command &c = all.cmds[i];
-        if (c.kind != CMD_GET) continue;
-        const uint8_t *src = static_cast<const uint8_t *>(get_host.p) + c.get_out;
-        unsigned char *dst = all.get_dst[g];
-        int stride = all.get_stride[g];
-        ++g;
-        cy_ctx *cv = cvs[cmd_cv[i]];
-        if (dst) {
-            for (int row = 0; row < c.get_h; ++row)
-                std::memcpy(dst + static_cast<ptrdiff_t>(row) * stride, src + static_cast<size_t>(row) * c.get_w * 4,
-                            static_cast<size_t>(c.get_w) * 4);
-        } else {
-            cv->deferred_out.insert(cv->deferred_out.end(), src, src + static_cast<size_t>(c.get_w) * c.get_h * 4);
-        }
+    // Deliver reads: to the caller's buffer, or keep them for deferred
+    // readers; contexts in parallel, each context's reads in call order.
+    std::vector<std::vector<std::pair<int, int>>> gets(cvs.size());   // (command, read index)
+    {
+        int g = 0;
+        for (size_t i = 0; i < all.cmds.size(); ++i)
+            if (all.cmds[i].kind == CMD_GET) gets[cmd_cv[i]].emplace_back(static_cast<int>(i), g++);
     }
+    auto deliver = [&](size_t ci) {
+        cy_ctx *cv = cvs[ci];
+        size_t add = 0;
+        for (auto &p : gets[ci]) {
+            const command &c = all.cmds[p.first];
+            if (!all.get_dst[p.second]) add += static_cast<size_t>(c.get_w) * c.get_h * 4;
+        }
+        cv->deferred_out.reserve(cv->deferred_out.size() + add);
+        for (auto &p : gets[ci]) {
+            const command &c = all.cmds[p.first];
+            const uint8_t *src = static_cast<const uint8_t *>(get_host.p) + c.get_out;
+            unsigned char *dst = all.get_dst[p.second];
+            int stride = all.get_stride[p.second];
+            if (dst) {
+                for (int row = 0; row < c.get_h; ++row)
+                    std::memcpy(dst + static_cast<ptrdiff_t>(row) * stride,
+                                src + static_cast<size_t>(row) * c.get_w * 4, static_cast<size_t>(c.get_w) * 4);
+            } else {
+                cv->deferred_out.insert(cv->deferred_out.end(), src,
+                                        src + static_cast<size_t>(c.get_w) * c.get_h * 4);
+            }
+        }
+    };
+    parallel_for(cvs.size(), deliver);
     for (cy_ctx *cv : cvs) {
         queue &q = cv->q;
         for (size_t i = 0; i < q.cmds.size(); ++i) {
@@ -1471,10 +1549,16 @@ int cy_ctx_create(int width, int height, cy_ctx **out) {
         c->fail(e == cudaErrorMemoryAllocation ? CY_ENOMEM : CY_ECUDA);
         return false;
     };
-    bool good = okc(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) &&
-                okc(cudaMalloc(&c->bitmap, npx * sizeof(float4))) &&
-                okc(cudaMemsetAsync(c->bitmap, 0, npx * sizeof(float4), c->stream)) &&
-                okc(cudaStreamSynchronize(c->stream));
+    bool good = okc(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    if (good) {
+        c->bitmap = static_cast<float4 *>(pool_get(npx * sizeof(float4), &c->bitmap_bytes));
+        if (!c->bitmap) good = okc(cudaErrorMemoryAllocation);
+    }
+    // A deferred canvas is painted by frames that treat it as blank until it
+    // has content, so only an immediate one starts from a cleared buffer.
+    if (good && !c->deferred)
+        good = okc(cudaMemsetAsync(c->bitmap, 0, npx * sizeof(float4), c->stream)) &&
+               okc(cudaStreamSynchronize(c->stream));
     if (!good) {
         int rc = c->status;
         cy_ctx_destroy(c);
@@ -1490,7 +1574,7 @@ void cy_ctx_destroy(cy_ctx *c) {
     delete static_cast<frame *>(c->cached_frame);
     for (auto &m : c->masks) m.free_all();
     for (auto &m : c->dead) m.free_all();
-    if (c->bitmap) cudaFree(c->bitmap);
+    if (c->bitmap) pool_put(c->bitmap, c->bitmap_bytes);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1625,6 +1709,10 @@ int cy_read_linear(cy_ctx *c, float *out) {
     int rc = flush_ctx(c);
     if (rc) return rc;
     size_t bytes = static_cast<size_t>(c->W) * c->H * sizeof(float4);
+    if (!c->has_content) {   // never painted: transparent black (a deferred buffer is not cleared)
+        std::memset(out, 0, bytes);
+        return CY_OK;
+    }
     if (cudaMemcpyAsync(out, c->bitmap, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) {
         cudaGetLastError();
@@ -1653,6 +1741,10 @@ extern "C" int cy_get_image_noalloc(cy_ctx *c, unsigned char *image, int w, int 
     if (c->status) return c->status;
     // Queued draws would need a frame run, which allocates: flush them first.
     if (!c->q.cmds.empty()) return CY_EINVAL;
+    if (!c->has_content) {   // never painted: every byte is zero (the buffer itself is not cleared)
+        for (int row = 0; row < h; ++row) std::memset(image + static_cast<size_t>(row) * stride, 0, static_cast<size_t>(w) * 4);
+        return CY_OK;
+    }
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocDevices) {
         cudaGetLastError();
@@ -1938,6 +2030,24 @@ int cy_frame_stats(cy_frame *fr, long long *stats, int n) {
     int m = static_cast<int>(sizeof(v) / sizeof(v[0]));
     for (int i = 0; i < n && i < m; ++i) stats[i] = v[i];
     return m;
+}
+
+int cy_frame_collect(cy_frame *fr, unsigned char *out, size_t cap, size_t *offsets) {
+    if (!fr || !offsets) return CY_EINVAL;
+    frame &f = *fr->f;
+    size_t n = f.cvs.size(), total = 0;
+    for (size_t i = 0; i < n; ++i) {
+        offsets[i] = total;
+        total += f.cvs[i]->deferred_out.size();
+    }
+    offsets[n] = total;
+    if (total > cap || (total && !out)) return -2;
+    parallel_for(n, [&](size_t i) {
+        std::vector<uint8_t> &d = f.cvs[i]->deferred_out;
+        if (!d.empty()) std::memcpy(out + offsets[i], d.data(), d.size());
+        std::vector<uint8_t>().swap(d);
+    });
+    return CY_OK;
 }
 
 int cy_ctx_take_reads(cy_ctx *c, unsigned char *out, size_t cap, size_t *len) {

@@ -338,16 +338,32 @@ __device__ __forceinline__ float blur_step(blur_pass &p, int x, int n, int r, fl
     return acc;
 }
 
-// Three blur passes over line[i * stride], i < n, in place.
+// Three blur passes over line[i * stride], i < n, in place.  Input values
+// are fetched kPrefetch steps ahead so a thread keeps several loads in
+// flight (a line's recurrence is sequential; its loads are not).
+static constexpr int kPrefetch = 8;
+
 __device__ void blur_line_fused(float *line, size_t stride, int n, int r, float w1, float w2) {
     const int m = kBlurRing - 1, L = r + 1;
     blur_pass p[3];
-    for (int t = 0; t < n + 3 * L; ++t) {
-        if (t < n) p[0].ring[t & m] = line[static_cast<size_t>(t) * stride];
-        int x1 = t - L, x2 = t - 2 * L, x3 = t - 3 * L;
-        if (x1 >= 0 && x1 < n) p[1].ring[x1 & m] = blur_step(p[0], x1, n, r, w1, w2);
-        if (x2 >= 0 && x2 < n) p[2].ring[x2 & m] = blur_step(p[1], x2, n, r, w1, w2);
-        if (x3 >= 0 && x3 < n) line[static_cast<size_t>(x3) * stride] = blur_step(p[2], x3, n, r, w1, w2);
+    const int steps = n + 3 * L;
+    for (int t0 = 0; t0 < steps; t0 += kPrefetch) {
+        float in[kPrefetch];
+#pragma unroll
+        for (int k = 0; k < kPrefetch; ++k) {
+            int t = t0 + k;
+            in[k] = t < n ? line[static_cast<size_t>(t) * stride] : 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < kPrefetch; ++k) {
+            int t = t0 + k;
+            if (t >= steps) break;
+            if (t < n) p[0].ring[t & m] = in[k];
+            int x1 = t - L, x2 = t - 2 * L, x3 = t - 3 * L;
+            if (x1 >= 0 && x1 < n) p[1].ring[x1 & m] = blur_step(p[0], x1, n, r, w1, w2);
+            if (x2 >= 0 && x2 < n) p[2].ring[x2 & m] = blur_step(p[1], x2, n, r, w1, w2);
+            if (x3 >= 0 && x3 < n) line[static_cast<size_t>(x3) * stride] = blur_step(p[2], x3, n, r, w1, w2);
+        }
     }
 }
 

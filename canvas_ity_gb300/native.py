@@ -110,6 +110,8 @@ def _batch_lib() -> ctypes.CDLL:
     lib.cy_frame_set_profiling.argtypes = [vp, ctypes.c_int]
     lib.cy_frame_profile.restype = ctypes.c_int
     lib.cy_frame_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+    lib.cy_frame_collect.restype = ctypes.c_int
+    lib.cy_frame_collect.argtypes = [vp, vp, ctypes.c_size_t, c_size_p]
     lib.cy_frame_autotune.restype = ctypes.c_int
     lib.cy_frame_autotune.argtypes = [vp, c_int_p, c_int_p, ctypes.POINTER(ctypes.c_float)]
     lib.cy_canvases_from_traces.restype = ctypes.c_int
@@ -203,21 +205,29 @@ class Frame:
         n = self.lib.cy_frame_profile(self.frame, arr, 8)
         return {self.PHASES[i]: float(arr[i]) for i in range(min(n, len(self.PHASES)))}
 
-    def finish(self) -> List[bytes]:
+    def finish(self, copy: bool = True) -> list:
+        """Copy the reads back; returns each canvas's get_image_data bytes
+        (memoryviews into one buffer when copy=False)."""
         t0 = time.perf_counter()
         rc = self.lib.cy_frame_finish(self.frame)
         if rc != 0:
             raise RuntimeError(f"cy_frame_finish failed with status {rc}")
         t1 = time.perf_counter()
-        out = []
-        for ctx in self.ctxs:
-            n = ctypes.c_size_t(0)
-            self.lib.cy_ctx_take_reads(ctx, None, 0, ctypes.byref(n))
-            buf = ctypes.create_string_buffer(max(n.value, 1))
-            rc = self.lib.cy_ctx_take_reads(ctx, buf, n.value, ctypes.byref(n))
+        n = len(self.ctxs)
+        offs = (ctypes.c_size_t * (n + 1))()
+        rc = self.lib.cy_frame_collect(self.frame, None, 0, offs)
+        total = offs[n]
+        buf = bytearray(total)
+        if total:
+            cbuf = (ctypes.c_char * total).from_buffer(buf)
+            rc = self.lib.cy_frame_collect(self.frame, ctypes.addressof(cbuf), total, offs)
             if rc != 0:
-                raise RuntimeError(f"cy_ctx_take_reads failed with status {rc}")
-            out.append(buf.raw[: n.value])
+                raise RuntimeError(f"cy_frame_collect failed with status {rc}")
+            del cbuf
+        mv = memoryview(buf)
+        out = [mv[offs[i]:offs[i + 1]] for i in range(n)]
+        if copy:
+            out = [bytes(o) for o in out]
         self.timing["finish_s"] = t1 - t0
         self.timing["reads_s"] = time.perf_counter() - t1
         return out

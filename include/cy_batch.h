@@ -92,6 +92,13 @@ int cy_frame_stats(cy_frame *frame, long long *stats, int n);
 int cy_canvases_from_traces(const void *const *traces, const size_t *lens, int n, int engine, int threads,
                             struct cy_canvas **out);
 
+/* After cy_frame_finish: the deferred reads of all the frame's contexts,
+ * context by context (each in call order), copied into `out`;
+ * offsets[0..n] (n = contexts) receive where each context's bytes start and
+ * the total.  -2 if cap is too small (offsets are still filled).  The
+ * contexts' reads are consumed, as by cy_ctx_take_reads. */
+int cy_frame_collect(cy_frame *frame, unsigned char *out, size_t cap, size_t *offsets);
+
 /* Deferred reads of a context, concatenated in call order (compact RGBA8
  * rectangles); -2 if cap is too small (*len holds the size). */
 int cy_ctx_take_reads(cy_ctx *ctx, unsigned char *out, size_t cap, size_t *len);
