@@ -452,6 +452,9 @@ __device__ __forceinline__ float4 blend(float4 back, float4 fore, int op, float 
     float4 b = make_float4(fore.x * mf + back.x * mb, fore.y * mf + back.y * mb, fore.z * mf + back.z * mb,
                            fore.w * mf + back.w * mb);
     b.w = lo(b.w, 1.0f);
+    // Full visibility: visibility * blend + (1 - visibility) * back is blend
+    // (up to the sign of a zero).
+    if (vis == 1.0f) return b;
     float iv = 1.0f - vis;
     return make_float4(b.x * vis + back.x * iv, b.y * vis + back.y * iv, b.z * vis + back.z * iv,
                        b.w * vis + back.w * iv);

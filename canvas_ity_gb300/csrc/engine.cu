@@ -335,7 +335,7 @@ struct frame {
     int strip_pixels = 4096;
     // device
     dbuf arena, flat_pts, flat_prev, item_cnt, item_off, pat_f4, jobs_dev, boxes;
-    dbuf row_cnt, row_off, row_cur, row_len, long_rows, n_long, runs, sums;
+    dbuf row_cnt, row_off, row_cur, row_len, row_meta, long_rows, n_long, runs, sums;
     dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
     hbuf staging, offs_host, rowoff_host, get_host;
@@ -402,7 +402,7 @@ struct frame {
         drop_graph();
         for (cudaEvent_t e : ev) if (e) cudaEventDestroy(e);
         dbuf *b[] = {&arena, &flat_pts, &flat_prev, &item_cnt, &item_off, &pat_f4, &jobs_dev, &boxes, &row_cnt,
-                     &row_off, &row_cur, &row_len, &long_rows, &n_long, &runs, &sums, &tabs_dev, &cp_cnt, &cp_off,
+                     &row_off, &row_cur, &row_len, &row_meta, &long_rows, &n_long, &runs, &sums, &tabs_dev, &cp_cnt, &cp_off,
                      &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev};
         for (dbuf *x : b) x->release();
@@ -812,7 +812,7 @@ int frame::prepare() {
         if (!jobs_dev.ensure(jobs.size() * sizeof(scan_job)) || !row_cnt.ensure((nr + 1) * 4) ||
             !row_off.ensure((nr + 2) * 8) || !row_cur.ensure((nr + 1) * 4) || !row_len.ensure((nr + 1) * 4) ||
             !boxes.ensure(jobs.size() * sizeof(cover_box)) || !rowoff_host.ensure((nr + 1) * 8) ||
-            !long_rows.ensure((nr + 1) * 4) || !n_long.ensure(4))
+            !long_rows.ensure((nr + 1) * 4) || !n_long.ensure(4) || !row_meta.ensure((nr + 1) * sizeof(int4)))
             return fail(CY_ENOMEM, __LINE__);
         if (!ok(cudaMemcpyAsync(jobs_dev.p, jobs.data(), jobs.size() * sizeof(scan_job), cudaMemcpyHostToDevice,
                                 stream)) ||
@@ -877,6 +877,7 @@ int frame::run() {
     row_view rv;
     rv.row_off = row_off.as<int64_t>();
     rv.row_len = row_len.as<int32_t>();
+    rv.meta = row_meta.as<int4>();
     rv.runs = runs.as<cyg::run>();
     rv.sums = sums.as<float>();
     if (n_jobs > 0) {
@@ -946,10 +947,11 @@ int frame::run() {
         k_rows<<<std::max(rgrid, 1), kRowsWarps * 32, 0, stream>>>(
             row_off.as<int64_t>(), row_cnt.as<int32_t>(), row_cur.as<int32_t>(), row_len.as<int32_t>(),
             runs.as<cyg::run>(), sums.as<float>(), static_cast<int>(nr), long_rows.as<int32_t>(),
-            n_long.as<int32_t>());
+            n_long.as<int32_t>(), row_meta.as<int4>());
         k_rows_long<<<152 * 2, kLongThreads, kLongSmem, stream>>>(
             row_off.as<int64_t>(), row_cnt.as<int32_t>(), row_cur.as<int32_t>(), row_len.as<int32_t>(),
-            runs.as<cyg::run>(), sums.as<float>(), long_rows.as<int32_t>(), n_long.as<int32_t>());
+            runs.as<cyg::run>(), sums.as<float>(), long_rows.as<int32_t>(), n_long.as<int32_t>(),
+            row_meta.as<int4>());
         if (!ok(cudaGetLastError())) return status;
         launches += (segs_nc > 0 ? 2 : 0) + (segs_cl > 0 ? 2 : 0) + 2 + scan_launch_count(static_cast<int64_t>(nr) + 1);
     }

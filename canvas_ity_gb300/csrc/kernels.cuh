@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restr
                                                           int32_t *__restrict__ row_cur, int32_t *__restrict__ row_len,
                                                           run *__restrict__ runs, float *__restrict__ sums,
                                                           int total_rows, int32_t *__restrict__ long_rows,
-                                                          int32_t *__restrict__ n_long) {
+                                                          int32_t *__restrict__ n_long, int4 *__restrict__ row_meta) {
     __shared__ run buf[kRowsWarps][kRowCap];
     __shared__ float acc[kRowsWarps][kRowCap];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -603,6 +603,8 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restr
         }
         if (lane == 0) {
             row_len[y] = m;
+            row_meta[y] = m ? make_int4(v[0].x, v[m - 1].x, __float_as_int(acc[w][m - 1]), m)
+                            : make_int4(0x7fffffff, -1, 0, 0);
             row_cnt[y] = 0;
             row_cur[y] = 0;
         }
@@ -618,7 +620,8 @@ __global__ void __launch_bounds__(kLongThreads) k_rows_long(const int64_t *__res
                                                            int32_t *__restrict__ row_len, run *__restrict__ runs,
                                                            float *__restrict__ sums,
                                                            const int32_t *__restrict__ long_rows,
-                                                           const int32_t *__restrict__ n_long) {
+                                                           const int32_t *__restrict__ n_long,
+                                                           int4 *__restrict__ row_meta) {
     extern __shared__ run lbuf[];   // kLongCap runs, then kLongCap floats
     float *lacc = reinterpret_cast<float *>(lbuf + kLongCap);
     __shared__ int warp_cnt[kLongThreads / 32];
@@ -669,7 +672,11 @@ __global__ void __launch_bounds__(kLongThreads) k_rows_long(const int64_t *__res
             for (int i = m + threadIdx.x; i < n2; i += blockDim.x) lbuf[i] = run_pad();
             __syncthreads();
             if (n2 > 1) bitonic_sort(lbuf, n2, threadIdx.x, blockDim.x, block_sync());
-            if (threadIdx.x == 0) total = coalesce_sum(lbuf, lacc, m);
+            if (threadIdx.x == 0) {
+                total = coalesce_sum(lbuf, lacc, m);
+                row_meta[y] = total ? make_int4(lbuf[0].x, lbuf[total - 1].x, __float_as_int(lacc[total - 1]), total)
+                                    : make_int4(0x7fffffff, -1, 0, 0);
+            }
             __syncthreads();
             kept = total;
             for (int i = threadIdx.x; i < kept; i += blockDim.x) {
@@ -693,6 +700,8 @@ __global__ void __launch_bounds__(kLongThreads) k_rows_long(const int64_t *__res
             }
             if (c > 0) sm[c - 1] = (sum += r[c - 1].delta);
             total = c;
+            row_meta[y] = c ? make_int4(r[0].x, r[c - 1].x, __float_as_int(sm[c - 1]), c)
+                            : make_int4(0x7fffffff, -1, 0, 0);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -720,6 +729,7 @@ struct row_view {
     const int32_t *row_len;
     const run *runs;
     const float *sums;
+    const int4 *meta;   // per row: first x, last x, final sum (bits), run count
 };
 
 // ---------------------------------------------------------- main render

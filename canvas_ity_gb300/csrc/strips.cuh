@@ -139,71 +139,88 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
             // render_main (hpp:2551-2605).  Walk each row's sorted runs with a
             // warp-wide cursor: the coverage sum in force at a pixel is the
             // running sum after the last run at or left of it.
-            int cur = -1, n = 0, j = 0, first_x = 0, last_x = -1;
-            const run *r = nullptr;
-            const float *sm = nullptr;
-            float carry = 0.0f;
-            for (int ch = cb; ch < ce; ++ch) {
-                int ly = ch / cpr, x0 = (ch - ly * cpr) << 5;
-                if (ly != cur) {
-                    cur = ly;
+            // Rows of the warp's chunk range; in each, only the chunks from
+            // the first run to the last (all of them for clearing ops).
+            const int ly_first = cb / cpr, ly_last = cb < ce ? (ce - 1) / cpr : -1;
+            for (int ly = ly_first; ly <= ly_last; ++ly) {
+                int n, first_x, last_x, next_x, j = 0;
+                const run *r;
+                const float *sm;
+                float carry = 0.0f;
+                {
                     int row = e.main_row_base + y0 + ly;
-                    n = P.rv.row_len[row];
-                    r = P.rv.runs + P.rv.row_off[row];
-                    sm = P.rv.sums + P.rv.row_off[row];
-                    j = 0;
-                    carry = 0.0f;
-                    first_x = n ? r[0].x : 0x7fffffff;
+                    int4 mt = P.rv.meta[row];   // with the offset: one round trip per row
+                    long long off = P.rv.row_off[row];
+                    n = mt.w;
+                    r = P.rv.runs + off;
+                    sm = P.rv.sums + off;
+                    first_x = mt.x;
+                    next_x = first_x;   // x of run j, the first one not yet in `carry`
                     // Past the last run the row's final sum still paints
                     // up to the clip's end when it is visible (see k_paint).
-                    last_x = n ? (cover_of(sm[n - 1], c.fill_rule) >= kVisible ? W - 1 : r[n - 1].x) : -1;
+                    last_x = n ? (cover_of(__int_as_float(mt.z), c.fill_rule) >= kVisible ? W - 1 : mt.y) : -1;
                 }
-                int xs = clearing ? 0 : first_x;
-                int xe = clearing ? W - 1 : min(last_x, W - 1);
-                if (x0 + 31 < xs || x0 > xe) continue;
-                // Consume the runs left of this chunk (they only set the carry).
-                int rx = 0x7fffffff;
-                float rs = 0.0f;
-                for (;;) {
-                    int idx = j + lane;
-                    rx = idx < n ? r[idx].x : 0x7fffffff;
-                    rs = idx < n ? sm[idx] : 0.0f;
-                    unsigned below = __ballot_sync(0xffffffffu, rx < x0);
-                    int nb = __popc(below);
-                    if (nb > 0) carry = __shfl_sync(0xffffffffu, rs, nb - 1);
-                    j += nb;
-                    if (nb < 32) {
-                        if (nb > 0) {   // realign the window at the new cursor
-                            rx = __shfl_down_sync(0xffffffffu, rx, nb);
-                            rs = __shfl_down_sync(0xffffffffu, rs, nb);
-                            if (lane + nb >= 32) {
-                                int k2 = j + lane;
-                                rx = k2 < n ? r[k2].x : 0x7fffffff;
-                                rs = k2 < n ? sm[k2] : 0.0f;
-                            }
-                        }
-                        break;
+                const int xs = clearing ? 0 : first_x;
+                const int xe = clearing ? W - 1 : min(last_x, W - 1);
+                if (xs > xe) continue;
+                const int row0 = ly * cpr;
+                const int c_hi = min(ce, row0 + (xe >> 5) + 1);
+                for (int ch = max(cb, row0 + (xs >> 5)); ch < c_hi; ++ch) {
+                const int x0 = (ch - row0) << 5;
+                float v;
+                if (next_x >= x0 + 32) {
+                    // No pending run reaches this chunk: every pixel takes
+                    // the carried sum.
+                    v = carry;
+                    if (!clearing && cover_of(carry, c.fill_rule) < kVisible) {
+                        // Nothing visible up to the next run: jump to the
+                        // chunk that holds it (or past this row).
+                        int target = (next_x < W && next_x <= xe) ? row0 + (next_x >> 5) : c_hi;
+                        if (target > ch + 1) ch = min(target, c_hi) - 1;
+                        continue;
                     }
-                }
-                // Runs inside the chunk: at most 32, one per distinct x.
-                bool in_chunk = rx < x0 + 32;
-                unsigned pos_mask = __reduce_or_sync(0xffffffffu, in_chunk ? (1u << (rx - x0)) : 0u);
-                int k = __popc(__ballot_sync(0xffffffffu, in_chunk));
-                unsigned upto = pos_mask & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u));
-                float v = carry;
-                int src = upto ? __popc(upto) - 1 : 0;
-                float from_run = __shfl_sync(0xffffffffu, rs, src);
-                if (upto) v = from_run;
-                if (k > 0) carry = __shfl_sync(0xffffffffu, rs, k - 1);
-                j += k;
-                if (!clearing && k == 0 && cover_of(carry, c.fill_rule) < kVisible) {
-                    // Nothing visible here nor up to the next run: jump to
-                    // the chunk that holds it (or past this row).
-                    int nx = __shfl_sync(0xffffffffu, rx, 0);
-                    int row_end = ly * cpr + cpr;
-                    int target = (nx < W && nx <= xe) ? ly * cpr + (nx >> 5) : row_end;
-                    if (target > ch + 1) ch = min(target, row_end) - 1;
-                    continue;
+                } else {
+                    // Consume the runs left of this chunk (they only set the carry).
+                    int rx = 0x7fffffff;
+                    float rs = 0.0f;
+                    for (;;) {
+                        int idx = j + lane;
+                        rx = idx < n ? r[idx].x : 0x7fffffff;
+                        rs = idx < n ? sm[idx] : 0.0f;
+                        unsigned below = __ballot_sync(0xffffffffu, rx < x0);
+                        int nb = __popc(below);
+                        if (nb > 0) carry = __shfl_sync(0xffffffffu, rs, nb - 1);
+                        j += nb;
+                        if (nb < 32) {
+                            if (nb > 0) {   // realign the window at the new cursor
+                                rx = __shfl_down_sync(0xffffffffu, rx, nb);
+                                rs = __shfl_down_sync(0xffffffffu, rs, nb);
+                                if (lane + nb >= 32) {
+                                    int k2 = j + lane;
+                                    rx = k2 < n ? r[k2].x : 0x7fffffff;
+                                    rs = k2 < n ? sm[k2] : 0.0f;
+                                }
+                            }
+                            break;
+                        }
+                    }
+                    // Runs inside the chunk: at most 32, one per distinct x.
+                    bool in_chunk = rx < x0 + 32;
+                    unsigned pos_mask = __reduce_or_sync(0xffffffffu, in_chunk ? (1u << (rx - x0)) : 0u);
+                    int k = __popc(__ballot_sync(0xffffffffu, in_chunk));
+                    unsigned upto = pos_mask & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u));
+                    v = carry;
+                    int src = upto ? __popc(upto) - 1 : 0;
+                    float from_run = __shfl_sync(0xffffffffu, rs, src);
+                    if (upto) v = from_run;
+                    if (k > 0) carry = __shfl_sync(0xffffffffu, rs, k - 1);
+                    j += k;
+                    next_x = k < 32 ? __shfl_sync(0xffffffffu, rx, k) : (j < n ? r[j].x : 0x7fffffff);
+                    if (!clearing && k == 0 && cover_of(carry, c.fill_rule) < kVisible) {
+                        int target = (next_x < W && next_x <= xe) ? row0 + (next_x >> 5) : c_hi;
+                        if (target > ch + 1) ch = min(target, c_hi) - 1;
+                        continue;
+                    }
                 }
                 int x = x0 + lane;
                 if (x < xs || x > xe) continue;
@@ -215,6 +232,7 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
                     float kk = cov * c.alpha;
                     float4 fore = make_float4(p.x * kk, p.y * kk, p.z * kk, p.w * kk);
                     px[ly * W + x] = blend(px[ly * W + x], fore, op, vis);
+                }
                 }
             }
         }
