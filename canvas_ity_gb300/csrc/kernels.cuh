@@ -524,6 +524,13 @@ __device__ __forceinline__ int coalesce_sum(run *v, float *acc, int m) {
 
 // Bitonic sort of v[0, n2) (n2 a power of two) by run_less, `lanes` threads
 // with ids `id` cooperating; `sync` orders the steps.
+__device__ __forceinline__ bool run_less_xd(int ax, float ad, int bx, float bd) {
+    if (ax != bx) return ax < bx;
+    float fa = fabsf(ad), fb = fabsf(bd);
+    if (fa != fb) return fa < fb;
+    return ad < bd;
+}
+
 struct warp_sync {
     __device__ void operator()() const { __syncwarp(); }
 };
@@ -554,9 +561,10 @@ __device__ __forceinline__ void bitonic_sort(run *v, int n2, int id, int lanes, 
 // std::sort (hpp:2243-2252), then store the running coverage sum after each
 // coalesced cell (the value render_main's walk holds from that cell on).
 // One warp per row: the row's nonzero runs are compacted into shared memory
-// and bitonic-sorted by the warp, then one lane coalesces and sums them in x
-// order (the float additions must follow the reference's order).  Rows with
-// more than kRowCap nonzero runs are listed for k_rows_long.
+// and sorted by the warp (in registers up to 32 runs, else a shared-memory
+// bitonic network); the warp then coalesces equal x and sums the cells in the
+// reference's order of float additions.  Rows with more than kRowCap
+// nonzero runs are listed for k_rows_long.
 __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restrict__ row_off,
                                                           int32_t *__restrict__ row_cnt,
                                                           int32_t *__restrict__ row_cur, int32_t *__restrict__ row_len,
@@ -564,7 +572,6 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restr
                                                           int total_rows, int32_t *__restrict__ long_rows,
                                                           int32_t *__restrict__ n_long, int4 *__restrict__ row_meta) {
     __shared__ run buf[kRowsWarps][kRowCap];
-    __shared__ float acc[kRowsWarps][kRowCap];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int gw = blockIdx.x * kRowsWarps + w, nw = gridDim.x * kRowsWarps;
     run *v = buf[w];
@@ -589,22 +596,74 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restr
             if (lane == 0) long_rows[atomicAdd(n_long, 1)] = y;
             continue;
         }
-        int n2 = 1;
-        while (n2 < m) n2 <<= 1;
-        for (int i = m + lane; i < n2; i += 32) v[i] = run_pad();
         __syncwarp();
-        if (n2 > 1) bitonic_sort(v, n2, lane, 32, warp_sync());
-        if (lane == 0) m = coalesce_sum(v, acc[w], m);
-        m = __shfl_sync(0xffffffffu, m, 0);
+        if (m <= 32) {
+            // One run per lane: a shuffle bitonic network sorts them in registers.
+            int x = 0x7fffffff;
+            float d = 0.0f;
+            if (lane < m) {
+                x = v[lane].x;
+                d = v[lane].delta;
+            }
+            if (m > 1) {
+#pragma unroll
+                for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+                    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                        int ox = __shfl_xor_sync(0xffffffffu, x, jj);
+                        float od = __shfl_xor_sync(0xffffffffu, d, jj);
+                        bool keep_min = ((lane & jj) == 0) == ((lane & k) == 0);
+                        if (keep_min ? run_less_xd(ox, od, x, d) : run_less_xd(x, d, ox, od)) {
+                            x = ox;
+                            d = od;
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane < m) v[lane] = run{x, d};
+        } else {
+            int n2 = 1;
+            while (n2 < m) n2 <<= 1;
+            for (int i = m + lane; i < n2; i += 32) v[i] = run_pad();
+            __syncwarp();
+            bitonic_sort(v, n2, lane, 32, warp_sync());
+        }
         __syncwarp();
-        for (int i = lane; i < m; i += 32) {
-            r[i] = v[i];
-            sm[i] = acc[w][i];
+        // Coalesce and sum, 32 sorted runs at a time: the first run of each
+        // x adds the rest of its x in order (the merged delta), then the
+        // merged deltas are summed strictly left to right, one shuffle per
+        // cell, which is the reference's order of float additions.
+        int groups = 0;
+        float sum = 0.0f;
+        for (int c0 = 0; c0 < m; c0 += 32) {
+            int i = c0 + lane;
+            bool valid = i < m;
+            run e = valid ? v[i] : run{0, 0.0f};
+            bool start = valid && (i == 0 || v[i - 1].x != e.x);
+            float merged = 0.0f;
+            if (start) {
+                merged = e.delta;
+                for (int t = i + 1; t < m && v[t].x == e.x; ++t) merged += v[t].delta;
+            }
+            unsigned bal = __ballot_sync(0xffffffffu, start);
+            int gi = groups + __popc(bal & ((1u << lane) - 1u));
+            float mine = 0.0f;
+            for (unsigned b = bal; b; b &= b - 1) {
+                int src = __ffs(b) - 1;
+                sum += __shfl_sync(0xffffffffu, merged, src);
+                if (lane == src) mine = sum;
+            }
+            if (start) {
+                r[gi] = run{e.x, merged};
+                sm[gi] = mine;
+            }
+            groups += __popc(bal);
         }
         if (lane == 0) {
-            row_len[y] = m;
-            row_meta[y] = m ? make_int4(v[0].x, v[m - 1].x, __float_as_int(acc[w][m - 1]), m)
-                            : make_int4(0x7fffffff, -1, 0, 0);
+            row_len[y] = groups;
+            row_meta[y] = groups ? make_int4(v[0].x, v[m - 1].x, __float_as_int(sum), groups)
+                                 : make_int4(0x7fffffff, -1, 0, 0);
             row_cnt[y] = 0;
             row_cur[y] = 0;
         }
