@@ -486,7 +486,7 @@ __device__ void sort_runs(run *r, int n) {
     }
 }
 
-static constexpr int kRowCap = 256;     // runs per row sorted by one warp in shared memory
+static constexpr int kRowCap = 512;     // runs per row sorted by one warp in shared memory
 static constexpr int kRowsWarps = 8;    // warps per block in k_rows
 static constexpr int kLongCap = 8192;   // runs per row sorted by one block in k_rows_long
 static constexpr int kLongThreads = 512;
