@@ -431,8 +431,23 @@ __device__ float4 paint_at(const command &c, const paint_src &s, float px, float
     }
     const float *stops = s.stop_off + c.stop_first;
     const float4 *cols = s.stop_col + c.stop_first;
+    // std::upper_bound (hpp:2366-2368).  add_color_stop keeps the stops
+    // sorted, so a linear walk finds the same index; the first eight stops
+    // are loaded together before the walk.
     int n = c.stop_count, k = 0;
-    while (k < n && !(offset < stops[k])) ++k;   // std::upper_bound
+    float st[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) st[i] = i < n ? stops[i] : 0.0f;
+    bool done = false;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        if (!done) {
+            if (i < n && !(offset < st[i])) ++k;
+            else done = true;
+        }
+    }
+    if (!done)
+        while (k < n && !(offset < stops[k])) ++k;
     if (k == 0) return premul(cols[0]);
     if (k == n) return premul(cols[n - 1]);
     float t = (offset - stops[k - 1]) / (stops[k] - stops[k - 1]);
