@@ -575,12 +575,27 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restr
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int gw = blockIdx.x * kRowsWarps + w, nw = gridDim.x * kRowsWarps;
     run *v = buf[w];
+    // The next row's bucket offsets and count are fetched while this row is
+    // sorted, so the warp does not wait for them between rows.
+    long long nxt_off = 0, nxt_end = 0;
+    int nxt_cnt = 0;
+    if (gw < total_rows) {
+        nxt_off = row_off[gw];
+        nxt_end = row_off[gw + 1];
+        nxt_cnt = row_cur[gw];
+    }
     for (int y = gw; y < total_rows; y += nw) {
-        int cap = static_cast<int>(row_off[y + 1] - row_off[y]);
-        int n = row_cur[y];
+        const long long off = nxt_off;
+        int cap = static_cast<int>(nxt_end - off);
+        int n = nxt_cnt;
         if (n > cap) n = cap;
-        run *r = runs + row_off[y];
-        float *sm = sums + row_off[y];
+        if (y + nw < total_rows) {
+            nxt_off = row_off[y + nw];
+            nxt_end = row_off[y + nw + 1];
+            nxt_cnt = row_cur[y + nw];
+        }
+        run *r = runs + off;
+        float *sm = sums + off;
         // Compact the nonzero runs.
         int m = 0;
         for (int base = 0; base < n; base += 32) {
