@@ -897,11 +897,21 @@ int frame::run() {
         int rc = clip_passes(t);
         if (rc) return rc;
         int segs_nc = static_cast<int>(nc_segs), segs_cl = static_cast<int>(pass_n[4]);
-        const int seg_per_block = kRunsWarps * 32;
-        int grid_nc = std::max(1, std::min((segs_nc + seg_per_block - 1) / seg_per_block, 152 * 16));
-        int grid_cl = std::max(1, std::min((segs_cl + seg_per_block - 1) / seg_per_block, 152 * 16));
-        if (segs_nc > 0) k_runs<false, false><<<grid_nc, kRunsWarps * 32, 0, stream>>>(t, segs_nc);
-        if (segs_cl > 0) k_runs<false, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl);
+        // Segments per warp round: halved while that leaves fewer than 48
+        // warps per SM of work.
+        auto per_warp = [](int segs) {
+            int s = 32;
+            while (s > 2 && segs / s < 152 * 48) s >>= 1;
+            return s;
+        };
+        const int spw_nc = per_warp(segs_nc), spw_cl = per_warp(segs_cl);
+        auto grid_for = [](int segs, int spw) {
+            int per_block = kRunsWarps * spw;
+            return std::max(1, std::min((segs + per_block - 1) / per_block, 152 * 16));
+        };
+        int grid_nc = grid_for(segs_nc, spw_nc), grid_cl = grid_for(segs_cl, spw_cl);
+        if (segs_nc > 0) k_runs<false, false><<<grid_nc, kRunsWarps * 32, 0, stream>>>(t, segs_nc, spw_nc);
+        if (segs_cl > 0) k_runs<false, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl, spw_cl);
         rc = scan64(row_cnt.as<int32_t>(), row_off.as<int64_t>(), static_cast<int>(nr) + 1);
         if (rc) return rc;
         if (!sized) {
@@ -940,8 +950,8 @@ int frame::run() {
         }
         t.row_off = row_off.as<int64_t>();
         t.runs = runs.as<cyg::run>();
-        if (segs_nc > 0) k_runs<true, false><<<grid_nc, kRunsWarps * 32, 0, stream>>>(t, segs_nc);
-        if (segs_cl > 0) k_runs<true, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl);
+        if (segs_nc > 0) k_runs<true, false><<<grid_nc, kRunsWarps * 32, 0, stream>>>(t, segs_nc, spw_nc);
+        if (segs_cl > 0) k_runs<true, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl, spw_cl);
         int rgrid = static_cast<int>(std::min<size_t>((nr + kRowsWarps - 1) / kRowsWarps, 152 * 32));
         if (!ok(cudaMemsetAsync(n_long.p, 0, 4, stream))) return status;
         k_rows<<<std::max(rgrid, 1), kRowsWarps * 32, 0, stream>>>(

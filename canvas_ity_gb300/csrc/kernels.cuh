@@ -355,18 +355,20 @@ struct job_tables {
 static constexpr int kRunsWarps = 4;   // warps per block in k_runs
 
 template <bool EMIT, bool CLIPPED>
-__global__ void __launch_bounds__(kRunsWarps * 32) k_runs(job_tables t, int total_segments) {
+__global__ void __launch_bounds__(kRunsWarps * 32) k_runs(job_tables t, int total_segments, int seg_per_warp) {
     __shared__ dda_piece pieces[kRunsWarps][32];
     __shared__ int seg_job[kRunsWarps][32];
     __shared__ int seg_end[kRunsWarps][32];   // inclusive prefix of row counts
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int gw = blockIdx.x * kRunsWarps + w, nw = gridDim.x * kRunsWarps;
-    for (int base = gw * 32; base < total_segments; base += nw * 32) {
+    // seg_per_warp (a power of two up to 32) segments per warp round: fewer
+    // when segments are few, so that more warps share their rows.
+    for (int base = gw * seg_per_warp; base < total_segments; base += nw * seg_per_warp) {
         int s = base + lane;
         int rows_here = 0, ji = 0;
         dda_piece p;
         p.nrows = 0;
-        if (s < total_segments) {
+        if (lane < seg_per_warp && s < total_segments) {
             float2 a, b;
             if (CLIPPED) {
                 ji = t.cl_job[s];
