@@ -622,18 +622,17 @@ __global__ void __launch_bounds__(kRowsWarps * 32) k_rows(const int64_t *__restr
                 x = v[lane].x;
                 d = v[lane].delta;
             }
-            if (m > 1) {
-#pragma unroll
-                for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-                    for (int jj = k >> 1; jj > 0; jj >>= 1) {
-                        int ox = __shfl_xor_sync(0xffffffffu, x, jj);
-                        float od = __shfl_xor_sync(0xffffffffu, d, jj);
-                        bool keep_min = ((lane & jj) == 0) == ((lane & k) == 0);
-                        if (keep_min ? run_less_xd(ox, od, x, d) : run_less_xd(x, d, ox, od)) {
-                            x = ox;
-                            d = od;
-                        }
+            // Network over the next power of two >= m (pads sort last).
+            int n2 = 1;
+            while (n2 < m) n2 <<= 1;
+            for (int k = 2; k <= n2; k <<= 1) {
+                for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                    int ox = __shfl_xor_sync(0xffffffffu, x, jj);
+                    float od = __shfl_xor_sync(0xffffffffu, d, jj);
+                    bool keep_min = ((lane & jj) == 0) == ((lane & k) == 0);
+                    if (keep_min ? run_less_xd(ox, od, x, d) : run_less_xd(x, d, ox, od)) {
+                        x = ox;
+                        d = od;
                     }
                 }
             }

@@ -385,6 +385,59 @@ __device__ void blur_line_fused(float *line, size_t stride, int n, int r, float 
     }
 }
 
+// Radius known at compile time: the three rings live in registers (every
+// ring index is a constant once a block of RING steps is unrolled).  RING is
+// the smallest power of two holding a pass's window [x - R - 2, x + R + 1].
+template <int R, int RING>
+__device__ __forceinline__ float blur_step_reg(const float (&ring)[RING], float &acc, int x, int n, float w1,
+                                               float w2, int k) {
+    // k is the step's position in the unrolled block; x % RING == k % RING.
+    constexpr int M = RING - 1;
+    if (x == 0) {
+        float a = R + 1 < n ? w1 * ring[(k + R + 1) & M] : 0.0f;
+#pragma unroll
+        for (int i = 0; i <= R; ++i)
+            if (i < n) a += (w1 + w2) * ring[(k + i) & M];
+        acc = a;
+        return a;
+    }
+    float a = acc;
+    if (x >= R + 1) a -= w2 * ring[(k - R - 1) & M];
+    if (x >= R + 2) a -= w1 * ring[(k - R - 2) & M];
+    if (x + R < n) a += w2 * ring[(k + R) & M];
+    if (x + R + 1 < n) a += w1 * ring[(k + R + 1) & M];
+    acc = a;
+    return a;
+}
+
+template <int R>
+__device__ void blur_line_reg(float *line, size_t stride, int n, float w1, float w2) {
+    constexpr int RING = 2 * R + 4 <= 16 ? 16 : 32;
+    constexpr int M = RING - 1;
+    constexpr int L = R + 1;
+    float r0[RING], r1[RING], r2[RING];
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+    const int steps = n + 3 * L;
+    for (int t0 = 0; t0 < steps; t0 += RING) {
+        float in[RING];
+#pragma unroll
+        for (int k = 0; k < RING; ++k) {
+            int t = t0 + k;
+            in[k] = t < n ? line[static_cast<size_t>(t) * stride] : 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < RING; ++k) {
+            int t = t0 + k;
+            if (t < n) r0[k] = in[k];
+            int x1 = t - L, x2 = t - 2 * L, x3 = t - 3 * L;
+            if (x1 >= 0 && x1 < n) r1[(k - L) & M] = blur_step_reg<R, RING>(r0, a0, x1, n, w1, w2, k - L);
+            if (x2 >= 0 && x2 < n) r2[(k - 2 * L) & M] = blur_step_reg<R, RING>(r1, a1, x2, n, w1, w2, k - 2 * L);
+            if (x3 >= 0 && x3 < n)
+                line[static_cast<size_t>(x3) * stride] = blur_step_reg<R, RING>(r2, a2, x3, n, w1, w2, k - 3 * L);
+        }
+    }
+}
+
 // The same three passes with a full copy of the line per pass (any radius).
 __device__ void blur_line_copy(float *line, float *tmp, size_t stride, size_t n, size_t r, float w1, float w2) {
     for (int pass = 0; pass < 3; ++pass) {
@@ -402,15 +455,30 @@ __device__ void blur_line_copy(float *line, float *tmp, size_t stride, size_t n,
     }
 }
 
+// Three passes over one line: registers for radius 0..7, local rings up to
+// kBlurMaxFused, else full copies.
+__device__ void blur_line(float *line, float *tmp, size_t stride, int n, int r, float w1, float w2) {
+    switch (r) {
+    case 0: blur_line_reg<0>(line, stride, n, w1, w2); return;
+    case 1: blur_line_reg<1>(line, stride, n, w1, w2); return;
+    case 2: blur_line_reg<2>(line, stride, n, w1, w2); return;
+    case 3: blur_line_reg<3>(line, stride, n, w1, w2); return;
+    case 4: blur_line_reg<4>(line, stride, n, w1, w2); return;
+    case 5: blur_line_reg<5>(line, stride, n, w1, w2); return;
+    case 6: blur_line_reg<6>(line, stride, n, w1, w2); return;
+    case 7: blur_line_reg<7>(line, stride, n, w1, w2); return;
+    default: break;
+    }
+    if (r <= kBlurMaxFused) blur_line_fused(line, stride, n, r, w1, w2);
+    else blur_line_copy(line, tmp, stride, n, r, w1, w2);
+}
+
 __global__ void k_blur_rows_all(const shadow_job *sj, const shadow_rect *rects, float *imgs, float *scratch) {
     const shadow_job &s = sj[blockIdx.y];
     const shadow_rect rc = rects[s.cmd];
     int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= rc.height) return;
-    if (s.radius <= kBlurMaxFused)
-        blur_line_fused(imgs + s.img + y, rc.height, rc.width, s.radius, s.w1, s.w2);
-    else
-        blur_line_copy(imgs + s.img + y, scratch + s.img + y, rc.height, rc.width, s.radius, s.w1, s.w2);
+    blur_line(imgs + s.img + y, scratch + s.img + y, rc.height, rc.width, s.radius, s.w1, s.w2);
 }
 
 // Column-major -> row-major, 32x32 tiles (blockIdx.z selects the shadow).
@@ -439,10 +507,7 @@ __global__ void k_blur_cols_all(const shadow_job *sj, const shadow_rect *rects, 
     const shadow_rect rc = rects[s.cmd];
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= rc.width) return;
-    if (s.radius <= kBlurMaxFused)
-        blur_line_fused(imgs + s.img + x, rc.width, rc.height, s.radius, s.w1, s.w2);
-    else
-        blur_line_copy(imgs + s.img + x, scratch + s.img + x, rc.width, rc.height, s.radius, s.w1, s.w2);
+    blur_line(imgs + s.img + x, scratch + s.img + x, rc.width, rc.height, s.radius, s.w1, s.w2);
 }
 
 }  // namespace cyg
