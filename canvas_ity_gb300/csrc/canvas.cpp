@@ -113,6 +113,7 @@ struct canvas_state {
     align_style align;
     baseline_style baseline;
     std::vector<int> counts;  // scratch for subpath counts
+    std::vector<int> closed_flags;
     std::vector<float> stop_colors;
 
     void note(int rc) { if (rc < 0 && status == 0) status = rc; }
@@ -133,6 +134,7 @@ struct canvas_state {
     void make_state(cy_draw_state &s, bool with_shadow);
     void draw_lines(const brush &br, bool clamp_edges, bool force_solid, bool with_shadow);
     void draw_path(const brush &br);
+    void stroke_path(const brush &br);
     void line_to(float x, float y);
     void move_to(float x, float y);
 };
@@ -744,6 +746,40 @@ void canvas_state::draw_path(const brush &br) {
                       static_cast<int>(counts.size()), &p, &s));
 }
 
+// stroke() with the expansion on the device: the path's cubics and the
+// line style go to cy_stroke_path, which flattens, dashes and expands them
+// as path_to_lines(true), dash_lines and stroke_lines do (hpp:1495-1524,
+// 1858-2100) before render_main.
+void canvas_state::stroke_path(const brush &br) {
+    if (singular()) return;
+    cy_paint p;
+    cy_draw_state s;
+    make_paint(br, false, false, p);
+    make_state(s, true);
+    counts.resize(path.subs.size());
+    closed_flags.resize(path.subs.size());
+    for (size_t i = 0; i < path.subs.size(); ++i) {
+        counts[i] = static_cast<int>(path.subs[i].count);
+        closed_flags[i] = path.subs[i].closed ? 1 : 0;
+    }
+    cy_stroke_style st;
+    st.line_width = lw;
+    st.miter_limit = miter_limit;
+    st.line_join = static_cast<int>(join);
+    st.line_cap = static_cast<int>(cap);
+    st.dash = dash.empty() ? nullptr : dash.data();
+    st.n_dash = static_cast<int>(dash.size());
+    st.dash_offset = dash_off;
+    const float f[6] = {fwd.a, fwd.b, fwd.c, fwd.d, fwd.e, fwd.f};
+    const float v[6] = {inv.a, inv.b, inv.c, inv.d, inv.e, inv.f};
+    for (int i = 0; i < 6; ++i) {
+        st.forward[i] = f[i];
+        st.inverse[i] = v[i];
+    }
+    note(cy_stroke_path(ctx, reinterpret_cast<const float *>(path.pts.data()), counts.data(), closed_flags.data(),
+                        static_cast<int>(counts.size()), &st, &p, &s));
+}
+
 }  // namespace detail
 
 using detail::mk;
@@ -984,6 +1020,10 @@ void canvas::fill() {
 void canvas::stroke() {
     // hpp:3050-3055
     sync_public_state();
+    if (cy_device_stroke()) {
+        self->stroke_path(self->stroke);
+        return;
+    }
     self->flatten(true);
     self->stroke_outline();
     self->draw_lines(self->stroke, false, false, true);

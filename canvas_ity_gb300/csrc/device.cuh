@@ -30,14 +30,17 @@ static constexpr float kFixedOne = 4294967296.0f;   // coverage fixed point: 2^3
 static constexpr float kFixedInv = 1.0f / 4294967296.0f;
 
 // ------------------------------------------------------------ flattening
-// Fill-mode flattening of one cubic, hpp:1331-1387 (add_tessellation with
-// angular = -1) and hpp:1398-1487 (add_bezier).  The recursion becomes an
-// explicit depth-first stack; EMIT=false only counts the points.
+// Flattening of one cubic, hpp:1331-1387 (add_tessellation) and
+// hpp:1398-1487 (add_bezier).  angular = -1 is fill mode (end points only);
+// stroking passes the cosine limit of hpp:1499-1500 and also keeps the
+// control points of the flat pieces.  The recursion becomes an explicit
+// depth-first stack; EMIT=false only counts the points.
 struct tess_frame { float2 p1, c1, c2, p2; int limit; };
 
 template <bool EMIT>
-__device__ int tessellate_fill(float2 p1, float2 c1, float2 c2, float2 p2, float2 *out, int cap) {
+__device__ int tessellate(float2 p1, float2 c1, float2 c2, float2 p2, float angular, float2 *out, int cap) {
     const float flat = 0.125f * 0.125f;
+    const bool stroking = angular > -1.0f;
     tess_frame stack[22];
     int depth = 0, n = 0;
     stack[depth++] = {p1, c1, c2, p2, 20};
@@ -51,9 +54,29 @@ __device__ int tessellate_fill(float2 p1, float2 c1, float2 c2, float2 p2, float
             float t2 = lo(hi(dot2(e3, seg) / lsq, 0.0f), 1.0f);
             float2 d1 = sub2(add2(f.p1, scl2(t1, seg)), f.c1);
             float2 d2 = sub2(sub2(f.p2, scl2(t2, seg)), f.c2);
-            if ((dot2(d1, d1) <= flat && dot2(d2, d2) <= flat) || !f.limit) {
-                if (EMIT && n < cap) out[n] = f.p2;
-                ++n;
+            float q1 = 0.0f, q2 = 0.0f, q3 = 0.0f, cosine = 1.0f;
+            if (stroking) {
+                float2 e2 = sub2(f.c2, f.c1);
+                q1 = dot2(e1, e1);
+                q2 = dot2(e2, e2);
+                q3 = dot2(e3, e3);
+                if (q1 * q3 != 0.0f) cosine = dot2(e1, e3) / sqrtf(q1 * q3);
+                else if (q1 * q2 != 0.0f) cosine = dot2(e1, e2) / sqrtf(q1 * q2);
+                else if (q2 * q3 != 0.0f) cosine = dot2(e2, e3) / sqrtf(q2 * q3);
+            }
+            if ((dot2(d1, d1) <= flat && dot2(d2, d2) <= flat && cosine >= angular) || !f.limit) {
+                if (stroking && q1 != 0.0f) {
+                    if (EMIT && n < cap) out[n] = f.c1;
+                    ++n;
+                }
+                if (stroking && q2 != 0.0f) {
+                    if (EMIT && n < cap) out[n] = f.c2;
+                    ++n;
+                }
+                if (!stroking || q3 != 0.0f) {
+                    if (EMIT && n < cap) out[n] = f.p2;
+                    ++n;
+                }
                 break;
             }
             float2 l1 = mix2(f.p1, f.c1, 0.5f), m = mix2(f.c1, f.c2, 0.5f), r2 = mix2(f.c2, f.p2, 0.5f);
@@ -82,7 +105,7 @@ __device__ __forceinline__ void axis_extrema(float a, float b, float c, float *a
 }
 
 template <bool EMIT>
-__device__ int flatten_cubic(float2 p1, float2 c1, float2 c2, float2 p2, float2 *out, int cap) {
+__device__ int flatten_cubic(float2 p1, float2 c1, float2 c2, float2 p2, float angular, float2 *out, int cap) {
     float2 e1 = sub2(c1, p1), e2 = sub2(c2, c1), e3 = sub2(p2, c2);
     if (dot2(e1, e1) == 0.0f && dot2(e3, e3) == 0.0f) {
         if (EMIT && cap > 0) out[0] = p2;
@@ -114,7 +137,7 @@ __device__ int flatten_cubic(float2 p1, float2 c1, float2 c2, float2 p2, float2 
         float2 s2 = mix2(q4, q5, t);
         float2 sc2 = mix2(q4, s2, ratio);
         float2 sc1 = mix2(q6, sc2, ratio);
-        n += tessellate_fill<EMIT>(s1, sc1, sc2, s2, out + (EMIT ? n : 0), cap - n);
+        n += tessellate<EMIT>(s1, sc1, sc2, s2, angular, out + (EMIT ? n : 0), cap - n);
         s1 = s2;
     }
     return n;

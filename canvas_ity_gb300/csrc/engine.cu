@@ -33,6 +33,7 @@
 #include "engine_types.h"
 #include "kernels.cuh"
 #include "strips.cuh"
+#include "stroke.cuh"
 
 using namespace cyg;
 
@@ -259,6 +260,9 @@ struct queue {
     std::vector<int32_t> host_prev;
     std::vector<float2> bez_pts;
     std::vector<flat_item> items;
+    std::vector<stroke_group> groups;   // stroked subpaths (device stroke expansion)
+    std::vector<stroke_style> styles;
+    std::vector<float> dash;
     std::vector<float> stop_off;
     std::vector<float4> stop_col;
     std::vector<uchar4> texels;
@@ -271,6 +275,7 @@ struct queue {
     bool empty() const { return cmds.empty(); }
     void clear() {
         cmds.clear(); mask_ids.clear(); host_pts.clear(); host_prev.clear(); bez_pts.clear(); items.clear();
+        groups.clear(); styles.clear(); dash.clear();
         stop_off.clear(); stop_col.clear(); texels.clear(); put_px.clear(); get_dst.clear(); get_stride.clear();
         bytes = 0; rows = 0; get_bytes = 0;
     }
@@ -310,9 +315,14 @@ struct frame {
     std::vector<cy_ctx *> cvs;
     // combined host data
     queue all;                 // commands and reads of all contexts (geometry stays in their queues)
-    struct ctx_base { int32_t hpts, bez, items, stop, tex; int64_t put; };
+    struct ctx_base { int32_t hpts, bez, items, stop, tex, groups, styles, dash; int64_t put; };
     std::vector<ctx_base> bases;   // where each context's geometry lands in the arena
     int64_t n_hpts = 0, n_bez = 0, n_items_all = 0, n_stop = 0, n_tex = 0, n_put = 0;
+    int64_t n_groups = 0, n_styles = 0, n_dash = 0;
+    // Device stroke expansion: flattened centre lines occupy flat_pts[0,
+    // nflat), the outlines follow at nflat; dashed centre lines are apart.
+    int64_t nflat = 0, n_outline = 0, n_dashed = 0, n_chunks = 0;
+    bool any_dash = false;
     std::vector<int32_t> cmd_cv;
     int64_t get_total = 0;
     std::vector<scan_job> jobs;
@@ -338,9 +348,14 @@ struct frame {
     dbuf row_cnt, row_off, row_cur, row_len, row_meta, long_rows, n_long, runs, sums;
     dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
-    hbuf staging, offs_host, rowoff_host, get_host;
+    dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, st_err, wk_cnt, wk_base, wk_chunks, jn_cnt, jn_sum,
+        jn_off, st_goff;
+    hbuf staging, offs_host, rowoff_host, get_host, stoff_host;
     char *d = nullptr;
     size_t o_cmd = 0, o_hpts = 0, o_hprev = 0, o_bez = 0, o_items = 0, o_soff = 0, o_scol = 0, o_tex = 0, o_put = 0;
+    size_t o_groups = 0, o_styles = 0, o_dash = 0;
+    stroke_in stroke_args() const;
+    int stroke_passes(bool sizing);
     bool sized = false;        // run store and masks sized by the first run
     int64_t n_runs = 0, main_runs = 0, main_rows = 0, h2d_bytes = 0;
     int launches = 0;          // kernel launches of the last run
@@ -376,6 +391,9 @@ struct frame {
         all.clear();
         bases.clear();
         n_hpts = n_bez = n_items_all = n_stop = n_tex = n_put = 0;
+        n_groups = n_styles = n_dash = 0;
+        nflat = n_outline = n_dashed = n_chunks = 0;
+        any_dash = false;
         cmd_cv.clear();
         get_total = 0;
         jobs.clear();
@@ -404,9 +422,11 @@ struct frame {
         dbuf *b[] = {&arena, &flat_pts, &flat_prev, &item_cnt, &item_off, &pat_f4, &jobs_dev, &boxes, &row_cnt,
                      &row_off, &row_cur, &row_len, &row_meta, &long_rows, &n_long, &runs, &sums, &tabs_dev, &cp_cnt, &cp_off,
                      &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
-                     &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev};
+                     &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev, &dash_cnt, &dash_off, &dash_pts,
+                     &dash_subs, &dash_nsub, &st_err, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt, &jn_sum, &jn_off, &st_goff};
         for (dbuf *x : b) x->release();
         staging.release();
+        stoff_host.release();
         offs_host.release();
         rowoff_host.release();
         get_host.release();
@@ -576,6 +596,12 @@ void frame::gather() {
         b.stop = static_cast<int32_t>(n_stop);
         b.tex = static_cast<int32_t>(n_tex);
         b.put = n_put;
+        b.groups = static_cast<int32_t>(n_groups);
+        b.styles = static_cast<int32_t>(n_styles);
+        b.dash = static_cast<int32_t>(n_dash);
+        n_groups += static_cast<int64_t>(q.groups.size());
+        n_styles += static_cast<int64_t>(q.styles.size());
+        n_dash += static_cast<int64_t>(q.dash.size());
         n_hpts += static_cast<int64_t>(q.host_pts.size());
         n_bez += static_cast<int64_t>(q.bez_pts.size());
         n_items_all += static_cast<int64_t>(q.items.size());
@@ -585,7 +611,7 @@ void frame::gather() {
         for (size_t k = 0; k < q.cmds.size(); ++k) {
             command c = q.cmds[k];
             if (c.kind == CMD_FILL || c.kind == CMD_CLIP) {
-                c.first += c.geom == 0 ? b.hpts : b.items;
+                c.first += c.geom == 0 ? b.hpts : c.geom == 1 ? b.items : b.groups;
                 c.stop_first += b.stop;
                 c.pat_first += b.tex;
             } else if (c.kind == CMD_PUT) {
@@ -625,6 +651,23 @@ void frame::stage(char *h) {
             if (it.sub_end >= 0) it.sub_end += b.items;
             items[k] = it;
         }
+        stroke_group *groups = reinterpret_cast<stroke_group *>(h + o_groups) + b.groups;
+        for (size_t k = 0; k < q.groups.size(); ++k) {
+            stroke_group g = q.groups[k];
+            g.head += b.items;
+            g.end += b.items;
+            g.style += b.styles;
+            groups[k] = g;
+        }
+        stroke_style *styles = reinterpret_cast<stroke_style *>(h + o_styles) + b.styles;
+        for (size_t k = 0; k < q.styles.size(); ++k) {
+            stroke_style st = q.styles[k];
+            st.dash_first += b.dash;
+            styles[k] = st;
+        }
+        if (!q.dash.empty())
+            std::memcpy(h + o_dash + static_cast<size_t>(b.dash) * sizeof(float), q.dash.data(),
+                        q.dash.size() * sizeof(float));
         if (!q.stop_off.empty()) {
             std::memcpy(h + o_soff + static_cast<size_t>(b.stop) * sizeof(float), q.stop_off.data(),
                         q.stop_off.size() * sizeof(float));
@@ -651,6 +694,118 @@ static bool needs_clip(const command &c, float wd, float ht, float ox, float oy)
     return !(x0 >= 1.0 && y0 >= 1.0 && x1 <= static_cast<double>(wd) - 1.0 && y1 <= static_cast<double>(ht) - 1.0);
 }
 
+stroke_in frame::stroke_args() const {
+    stroke_in si;
+    si.flat = flat_pts.as<float2>();
+    si.item_off = item_off.as<int32_t>();
+    si.groups = reinterpret_cast<const stroke_group *>(d + o_groups);
+    si.styles = reinterpret_cast<const stroke_style *>(d + o_styles);
+    si.dash = reinterpret_cast<const float *>(d + o_dash);
+    si.dash_pts = dash_pts.as<float2>();
+    si.dash_subs = dash_subs.as<int2>();
+    si.dash_off = dash_off.as<int32_t>();
+    si.dash_nsub = dash_nsub.as<int32_t>();
+    si.nflat = static_cast<int32_t>(nflat);
+    si.n = static_cast<int>(n_groups);
+    si.error = st_err.as<int32_t>();
+    return si;
+}
+
+// Stroke expansion: dash (count, scan, write), walks (count, scan, write),
+// joins (count, scan, write).  Every run does all of it from the centre
+// lines; the first run (`sizing`) reads the sizes back between the steps to
+// allocate, and stops before writing the outlines (flat_pts may move).
+int frame::stroke_passes(bool sizing) {
+    const int ng = static_cast<int>(n_groups);
+    const int sgrid = (ng + kStrokeWarps - 1) / kStrokeWarps;
+    const size_t gn = static_cast<size_t>(ng) + 2;
+    int32_t *hb = static_cast<int32_t *>(stoff_host.p);
+    if (sizing) {
+        if (!st_err.ensure(4) || !dash_cnt.ensure(gn * 4) || !dash_off.ensure(gn * 4) || !dash_nsub.ensure(gn * 4) ||
+            !wk_cnt.ensure(gn * 4) || !wk_base.ensure(gn * 4) || !st_goff.ensure(gn * 8) ||
+            !stoff_host.ensure(gn * 8) || !dash_pts.ensure(256) || !dash_subs.ensure(256))
+            return fail(CY_ENOMEM, __LINE__);
+        hb = static_cast<int32_t *>(stoff_host.p);
+        any_dash = false;
+        for (cy_ctx *cv : cvs)
+            for (const stroke_style &st : cv->q.styles) any_dash = any_dash || st.dash_n > 0;
+        if (!ok(cudaMemsetAsync(st_err.p, 0, 4, stream))) return status;
+    }
+    auto read_back = [&](void *dst, const void *src, size_t bytes) {
+        return ok(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream)) &&
+               ok(cudaStreamSynchronize(stream));
+    };
+    if (any_dash) {
+        k_dash<false><<<sgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), dash_cnt.as<int32_t>());
+        if (!ok(cudaMemsetAsync(dash_cnt.as<int32_t>() + ng, 0, 4, stream))) return status;
+        if (int rc = scan(dash_cnt.as<int32_t>(), dash_off.as<int32_t>(), ng + 1)) return rc;
+        if (sizing) {
+            if (!ok(cudaMemcpyAsync(hb + 1, st_err.p, 4, cudaMemcpyDeviceToHost, stream)) ||
+                !read_back(hb, dash_off.as<int32_t>() + ng, 4))
+                return status;
+            n_dashed = hb[0];
+            if (hb[1] != 0 || n_dashed < 0 || nflat + n_dashed > (static_cast<int64_t>(1) << 30))
+                return fail(CY_ENOMEM, __LINE__);
+            if (!dash_pts.ensure(static_cast<size_t>(n_dashed + 1) * sizeof(float2)) ||
+                !dash_subs.ensure(static_cast<size_t>(n_dashed + 1) * sizeof(int2)))
+                return fail(CY_ENOMEM, __LINE__);
+        }
+        k_dash<true><<<sgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), nullptr);
+        launches += 3 + scan_launch_count(ng + 1);
+    }
+    walk_out wo;
+    wo.chunks = nullptr;
+    wo.chunk_base = nullptr;
+    wo.chunk_count = wk_cnt.as<int32_t>();
+    k_walk<false><<<sgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wo);
+    if (!ok(cudaMemsetAsync(wk_cnt.as<int32_t>() + ng, 0, 4, stream))) return status;
+    if (int rc = scan(wk_cnt.as<int32_t>(), wk_base.as<int32_t>(), ng + 1)) return rc;
+    if (sizing) {
+        if (!read_back(hb, wk_base.as<int32_t>() + ng, 4)) return status;
+        n_chunks = hb[0];
+        if (n_chunks < 0 || n_chunks > (static_cast<int64_t>(1) << 26)) return fail(CY_ENOMEM, __LINE__);
+        size_t nc = static_cast<size_t>(n_chunks) + 1;
+        if (!wk_chunks.ensure(nc * sizeof(walk_chunk)) || !jn_cnt.ensure(nc * 32 * 4) || !jn_sum.ensure(nc * 4) ||
+            !jn_off.ensure(nc * 8))
+            return fail(CY_ENOMEM, __LINE__);
+    }
+    wo.chunks = wk_chunks.as<walk_chunk>();
+    wo.chunk_base = wk_base.as<int32_t>();
+    k_walk<true><<<sgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wo);
+    const int nch = static_cast<int>(n_chunks);
+    const int jgrid = std::max(1, (nch + kStrokeWarps - 1) / kStrokeWarps);
+    k_join<false><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(), nch,
+                                                           jn_cnt.as<int32_t>(), jn_sum.as<int32_t>(), nullptr,
+                                                           nullptr, nullptr, 0, 0);
+    if (!ok(cudaMemsetAsync(jn_sum.as<int32_t>() + nch, 0, 4, stream))) return status;
+    if (int rc = scan64(jn_sum.as<int32_t>(), jn_off.as<int64_t>(), nch + 1)) return rc;
+    k_group_off<<<(ng + 1 + 255) / 256, 256, 0, stream>>>(wk_base.as<int32_t>(), jn_off.as<int64_t>(), ng,
+                                                         st_goff.as<int64_t>());
+    launches += 5 + 2 * scan_launch_count(ng + 1) + scan_launch_count(nch + 1);
+    if (sizing) {
+        int64_t *g64 = static_cast<int64_t *>(stoff_host.p);
+        int32_t *errp = reinterpret_cast<int32_t *>(g64 + ng + 1);
+        if (!ok(cudaMemcpyAsync(errp, st_err.p, 4, cudaMemcpyDeviceToHost, stream)) ||
+            !read_back(g64, st_goff.p, static_cast<size_t>(ng + 1) * 8))
+            return status;
+        int err = *errp;
+        n_outline = g64[ng];
+        if (err != 0 || n_outline < 0 || nflat + n_outline > (static_cast<int64_t>(1) << 30))
+            return fail(CY_ENOMEM, __LINE__);
+        // the outlines go after the centre lines; every run writes both again
+        if (!flat_pts.ensure(static_cast<size_t>(nflat + n_outline + 1) * sizeof(float2)) ||
+            !flat_prev.ensure(static_cast<size_t>(nflat + n_outline + 1) * 4))
+            return fail(CY_ENOMEM, __LINE__);
+        return ok(cudaGetLastError()) ? CY_OK : status;
+    }
+    k_join<true><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(), nch,
+                                                          jn_cnt.as<int32_t>(), nullptr, jn_off.as<int64_t>(),
+                                                          flat_pts.as<float2>() + nflat, flat_prev.as<int32_t>() + nflat,
+                                                          static_cast<int32_t>(nflat), n_outline);
+    ++launches;
+    return ok(cudaGetLastError()) ? CY_OK : status;
+}
+
 int frame::prepare() {
     if (int rc = ensure_srgb_table()) return fail(rc);
     gather();
@@ -665,13 +820,16 @@ int frame::prepare() {
     o_hprev = align256(o_hpts + static_cast<size_t>(n_hpts) * sizeof(float2));
     o_bez = align256(o_hprev + static_cast<size_t>(n_hpts) * sizeof(int32_t));
     o_items = align256(o_bez + static_cast<size_t>(n_bez) * sizeof(float2));
-    o_soff = align256(o_items + static_cast<size_t>(n_items_all) * sizeof(flat_item));
+    o_groups = align256(o_items + static_cast<size_t>(n_items_all) * sizeof(flat_item));
+    o_styles = align256(o_groups + static_cast<size_t>(n_groups) * sizeof(stroke_group));
+    o_dash = align256(o_styles + static_cast<size_t>(n_styles) * sizeof(stroke_style));
+    o_soff = align256(o_dash + static_cast<size_t>(n_dash) * sizeof(float));
     o_scol = align256(o_soff + static_cast<size_t>(n_stop) * sizeof(float));
     o_tex = align256(o_scol + static_cast<size_t>(n_stop) * sizeof(float4));
     o_put = align256(o_tex + static_cast<size_t>(n_tex) * sizeof(uchar4));
     size_t total = align256(o_put + static_cast<size_t>(n_put));
     if (n_hpts > INT32_MAX / 2 || n_bez > INT32_MAX / 2 || n_items_all > INT32_MAX / 2 || n_stop > INT32_MAX / 2 ||
-        n_tex > INT32_MAX / 2)
+        n_tex > INT32_MAX / 2 || n_groups > INT32_MAX / 2 || n_styles > INT32_MAX / 2 || n_dash > INT32_MAX / 2)
         return fail(CY_ENOMEM, __LINE__);
     if (!arena.ensure(total) || !staging.ensure(total)) return fail(CY_ENOMEM, __LINE__);
     char *h = static_cast<char *>(staging.p);
@@ -702,17 +860,30 @@ int frame::prepare() {
             !ok(cudaStreamSynchronize(stream)))
             return status;
         offs_h = static_cast<const int32_t *>(offs_host.p);
-        int64_t nflat = offs_h[n_items];
+        nflat = offs_h[n_items];
         if (nflat < 0 || nflat > (static_cast<int64_t>(1) << 30)) return fail(CY_ENOMEM, __LINE__);
         if (!flat_pts.ensure(static_cast<size_t>(nflat + 1) * sizeof(float2)) ||
             !flat_prev.ensure(static_cast<size_t>(nflat + 1) * 4))
             return fail(CY_ENOMEM, __LINE__);
+        if (n_groups > 0) {
+            // the stroke passes read the centre lines: flatten them now
+            const float2 *d_bez = reinterpret_cast<const float2 *>(d + o_bez);
+            const flat_item *d_items = reinterpret_cast<const flat_item *>(d + o_items);
+            k_flat_emit<<<(n_items + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items, item_off.as<int32_t>(),
+                                                                    flat_pts.as<float2>(), flat_prev.as<int32_t>(),
+                                                                    nflat);
+            if (int rc = stroke_passes(true)) return rc;
+        }
     }
+    const int64_t *stoff_h = static_cast<const int64_t *>(stoff_host.p);
     for (command &c : cmds) {
         if (c.kind != CMD_FILL && c.kind != CMD_CLIP) continue;
         if (c.geom == 0) {
             c.line_first = c.first;
             c.line_count = c.count;
+        } else if (c.geom == 2) {
+            c.line_first = c.count > 0 ? static_cast<int32_t>(nflat + stoff_h[c.first]) : 0;
+            c.line_count = c.count > 0 ? static_cast<int32_t>(stoff_h[c.first + c.count] - stoff_h[c.first]) : 0;
         } else if (c.count == 0 || !offs_h) {
             c.line_first = 0;
             c.line_count = 0;
@@ -863,14 +1034,21 @@ int frame::run() {
     }
     int n_items_flat = static_cast<int>(n_items_all);
     if (n_items_flat > 0) {
-        const int32_t *offs_h = static_cast<const int32_t *>(offs_host.p);
-        int64_t nflat = offs_h[n_items_flat];
+        // flattening counts and offsets, then the points (the first run's
+        // read-back only sized the store)
+        k_flat_count<<<(n_items_flat + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items_flat,
+                                                                    item_cnt.as<int32_t>());
+        if (!ok(cudaMemsetAsync(item_cnt.as<int32_t>() + n_items_flat, 0, 4, stream))) return status;
+        if (int rc = scan(item_cnt.as<int32_t>(), item_off.as<int32_t>(), n_items_flat + 1)) return rc;
         k_flat_emit<<<(n_items_flat + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items_flat,
                                                                     item_off.as<int32_t>(), flat_pts.as<float2>(),
                                                                     flat_prev.as<int32_t>(), nflat);
+        launches += 2 + scan_launch_count(n_items_flat + 1);
     }
     if (n_tex > 0) ++launches;
-    if (n_items_flat > 0) ++launches;
+    if (n_groups > 0 && n_outline > 0) {
+        if (int rc = stroke_passes(false)) return rc;
+    }
     mark();   // 1: patterns and flattening done
     size_t nr = static_cast<size_t>(total_rows);
     int n_jobs = static_cast<int>(jobs.size());
@@ -1446,10 +1624,10 @@ int queue_geometry(queue &q, const float *points, const int *counts, int n_sub, 
             continue;
         }
         int32_t start = static_cast<int32_t>(q.items.size());
-        flat_item head = {pbase + static_cast<int32_t>(at), 0};
+        flat_item head = {pbase + static_cast<int32_t>(at), 0, -1.0f};
         q.items.push_back(head);
         for (int k = 1; k < n; k += 3) {
-            flat_item cub = {pbase + static_cast<int32_t>(at + k - 1), -1};
+            flat_item cub = {pbase + static_cast<int32_t>(at + k - 1), -1, -1.0f};
             q.items.push_back(cub);
         }
         q.items[start].sub_end = static_cast<int32_t>(q.items.size());
@@ -1514,6 +1692,149 @@ int queue_draw(cy_ctx *c, const float *points, const int *counts, int n_sub, boo
     q.mask_ids.push_back(state->mask);
     q.mask_ids.push_back(0);
     if (state->mask > 0) c->masks[state->mask].refs++;   // held until the frame finishes
+    return maybe_flush(c);
+}
+
+std::atomic<int> g_device_stroke(1);
+
+// Bounds of a stroke outline from its path's control points: the outline
+// stays within half * max(2, miter limit if mitred) of the centre line in
+// user space (joins, caps and their control points included), mapped by the
+// forward transform, plus a margin for the rounding of the round trip
+// through user space.
+void stroke_bounds(const float *xy, size_t n, const stroke_style &st, command &c) {
+    bounds_of(xy, n, c);
+    if (c.gx0 <= -1000000000 || c.gy0 <= -1000000000 || c.gx1 >= 1000000000 || c.gy1 >= 1000000000) return;
+    const float *f = st.fwd, *iv = st.inv;
+    double lin = std::sqrt(static_cast<double>(f[0]) * f[0] + static_cast<double>(f[1]) * f[1] +
+                           static_cast<double>(f[2]) * f[2] + static_cast<double>(f[3]) * f[3]);
+    double ilin = std::sqrt(static_cast<double>(iv[0]) * iv[0] + static_cast<double>(iv[1]) * iv[1] +
+                            static_cast<double>(iv[2]) * iv[2] + static_cast<double>(iv[3]) * iv[3]);
+    double r = 2.0 * std::fabs(static_cast<double>(st.half));
+    if (st.join == 0) r = std::max(r, std::sqrt(std::fabs(static_cast<double>(st.ratio))));
+    double big = std::max(std::max(std::fabs(static_cast<double>(c.gx0)), std::fabs(static_cast<double>(c.gx1))),
+                          std::max(std::fabs(static_cast<double>(c.gy0)), std::fabs(static_cast<double>(c.gy1))));
+    double user = ilin * big + std::fabs(static_cast<double>(iv[4])) + std::fabs(static_cast<double>(iv[5]));
+    double margin = r * lin + 2.0 +
+                    1.0e-5 * (big + lin * user + std::fabs(static_cast<double>(f[4])) + std::fabs(static_cast<double>(f[5])));
+    if (!(margin < 1.0e9)) {
+        c.gx0 = c.gy0 = -1000000000;
+        c.gx1 = c.gy1 = 1000000000;
+        return;
+    }
+    auto grow = [&](int32_t &v, double by) {
+        double x = static_cast<double>(v) + by;
+        v = x < -1.0e9 ? -1000000000 : x > 1.0e9 ? 1000000000 : static_cast<int32_t>(std::floor(x));
+    };
+    grow(c.gx0, -margin);
+    grow(c.gy0, -margin);
+    grow(c.gx1, margin + 1.0);
+    grow(c.gy1, margin + 1.0);
+}
+
+// stroke(): the path's cubics are flattened with the stroking angle limit,
+// then dashed and expanded on the device (k_dash, k_stroke).  The dash
+// phase at the start of each subpath is computed here, as in hpp:1867-1876.
+int queue_stroke(cy_ctx *c, const float *points, const int *counts, const int *closed, int n_sub,
+                 const cy_stroke_style *style, const cy_paint *paint, const cy_draw_state *state) {
+    if (!c) return CY_EINVAL;
+    if (c->status) return c->status;
+    if (!paint || !state || !style) return CY_EINVAL;
+    if (state->mask < 0 || state->mask >= static_cast<int>(c->masks.size()) ||
+        (state->mask > 0 && c->masks[state->mask].refs <= 0))
+        return CY_EINVAL;
+    size_t total = 0;
+    if (n_sub < 0 || (n_sub > 0 && (!counts || !points || !closed)) || !valid_counts(counts, n_sub, total))
+        return CY_EINVAL;
+    for (int i = 0; i < n_sub; ++i)
+        if (counts[i] != 0 && (counts[i] - 1) % 3 != 0) return CY_EINVAL;
+    if (style->n_dash < 0 || (style->n_dash > 0 && !style->dash) || style->n_dash > (1 << 20) ||
+        style->line_join < 0 || style->line_join > 2 || style->line_cap < 0 || style->line_cap > 2)
+        return CY_EINVAL;
+    const float *fw = style->forward;
+    // stroke_lines and render_main draw nothing under a singular transform.
+    if (fw[0] * fw[3] - fw[1] * fw[2] == 0.0f) return CY_OK;
+    stroke_style st;
+    std::memset(&st, 0, sizeof(st));
+    st.half = style->line_width * 0.5f;
+    st.ratio = style->miter_limit * style->miter_limit * st.half * st.half;
+    st.join = style->line_join;
+    st.cap = style->line_cap;
+    for (int i = 0; i < 6; ++i) {
+        st.fwd[i] = style->forward[i];
+        st.inv[i] = style->inverse[i];
+    }
+    if (style->n_dash > 0) {
+        const float *dash = style->dash;
+        int nd = style->n_dash;
+        float sum = 0.0f;
+        for (int i = 0; i < nd; ++i) sum = sum + dash[i];
+        float offset = fmodf(style->dash_offset, sum);
+        if (offset < 0.0f) offset += sum;
+        int start = 0, steps = 0;
+        while (offset >= dash[start]) {
+            offset -= dash[start];
+            start = start + 1 < nd ? start + 1 : 0;
+            if (++steps > 4 * nd + 8) return CY_EINVAL;   // offset within two periods of the pattern
+        }
+        st.dash_n = nd;
+        st.dash_start = start;
+        st.dash_next = dash[start] - offset;
+    }
+    float tol = 0.125f;
+    float ratio = tol / (0.5f * style->line_width < tol ? tol : 0.5f * style->line_width);
+    float angular = (ratio - 2.0f) * ratio * 2.0f + 1.0f;   // hpp:1498-1500
+    queue &q = c->q;
+    command cmd;
+    std::memset(&cmd, 0, sizeof(cmd));
+    cmd.kind = CMD_FILL;
+    size_t stops = q.stop_off.size(), tex = q.texels.size();
+    fill_state(state, cmd);
+    cmd.fill_rule = 0;   // render_main fills the outline nonzero
+    int rc = fill_paint(q, paint, cmd);
+    if (rc != CY_OK) {
+        q.stop_off.resize(stops);
+        q.stop_col.resize(stops);
+        q.texels.resize(tex);
+        return rc;
+    }
+    stroke_bounds(points, total, st, cmd);
+    cmd.geom = 2;
+    cmd.first = static_cast<int32_t>(q.groups.size());
+    int32_t style_id = static_cast<int32_t>(q.styles.size());
+    st.dash_first = static_cast<int32_t>(q.dash.size());
+    q.dash.insert(q.dash.end(), style->dash, style->dash + style->n_dash);
+    q.styles.push_back(st);
+    const float2 *p = reinterpret_cast<const float2 *>(points);
+    int32_t pbase = static_cast<int32_t>(q.bez_pts.size());
+    q.bez_pts.insert(q.bez_pts.end(), p, p + total);
+    size_t at = 0;
+    for (int s = 0; s < n_sub; ++s) {
+        int n = counts[s];
+        if (n == 0) continue;
+        stroke_group g;
+        g.head = static_cast<int32_t>(q.items.size());
+        g.closed = closed[s] ? 1 : 0;
+        g.style = style_id;
+        flat_item head = {pbase + static_cast<int32_t>(at), 0, angular};
+        q.items.push_back(head);
+        for (int k = 1; k < n; k += 3) {
+            flat_item cub = {pbase + static_cast<int32_t>(at + k - 1), -1, angular};
+            q.items.push_back(cub);
+        }
+        g.end = static_cast<int32_t>(q.items.size());
+        q.items[g.head].sub_end = g.end;
+        q.groups.push_back(g);
+        at += n;
+    }
+    cmd.count = static_cast<int32_t>(q.groups.size()) - cmd.first;
+    q.bytes += total * 8 + (total / 3 + static_cast<size_t>(n_sub)) * 12 + static_cast<size_t>(cmd.count) * 16 +
+               sizeof(stroke_style) + static_cast<size_t>(style->n_dash) * 4;
+    q.rows += c->H + (cmd.shadow ? c->H + 2 * cmd.sh_border : 0);
+    q.cmds.push_back(cmd);
+    q.mask_ids.push_back(state->mask);
+    q.mask_ids.push_back(0);
+    if (state->mask > 0) c->masks[state->mask].refs++;
     return maybe_flush(c);
 }
 
@@ -1602,6 +1923,14 @@ int cy_fill_lines(cy_ctx *c, const float *points, const int *counts, int n_sub, 
                   const cy_draw_state *state) {
     return queue_draw(c, points, counts, n_sub, false, paint, state);
 }
+
+int cy_stroke_path(cy_ctx *c, const float *points, const int *counts, const int *closed, int n_sub,
+                   const cy_stroke_style *style, const cy_paint *paint, const cy_draw_state *state) {
+    return queue_stroke(c, points, counts, closed, n_sub, style, paint, state);
+}
+
+void cy_set_device_stroke(int on) { g_device_stroke.store(on ? 1 : 0); }
+int cy_device_stroke(void) { return g_device_stroke.load(); }
 
 int cy_mask_retain(cy_ctx *c, int mask) {
     if (!c || mask <= 0 || mask >= static_cast<int>(c->masks.size()) || c->masks[mask].refs <= 0)

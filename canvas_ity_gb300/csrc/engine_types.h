@@ -13,14 +13,33 @@ enum { CMD_FILL = 1, CMD_CLIP = 2, CMD_PUT = 3, CMD_GET = 4 };
 struct flat_item {
     int32_t pt;       // index into the Bezier point array (cubic: its start point)
     int32_t sub_end;  // start items: index of the first item after the subpath; cubics: -1
+    float angular;    // -1: fill mode; stroking: the cosine limit of hpp:1499-1500
+};
+
+// Stroke expansion on the device (stroke_lines, hpp:2070-2100): one style
+// per stroked path and one group per subpath of it.
+struct stroke_style {
+    float half, ratio;            // line_width / 2 and miter_limit^2 * half^2 (hpp:1952-1953)
+    int32_t join, cap;            // join_style / cap_style values (hpp:149-150)
+    int32_t dash_first, dash_n;   // the dash pattern (dash_n 0: solid)
+    int32_t dash_start;           // pattern entry the offset falls in (hpp:1871-1876)
+    float dash_next;              // its remaining length (hpp:1888)
+    float fwd[6], inv[6];         // current transform and its inverse (a, b, c, d, e, f)
+};
+
+struct stroke_group {
+    int32_t head, end;   // flat_item range of the subpath (head: its start item)
+    int32_t closed;
+    int32_t style;
 };
 
 // One queued draw, clip or put_image_data, with everything the kernels need.
 struct __align__(16) command {
     int32_t kind, op;
     float alpha;
-    int32_t geom;         // 0: host polylines, 1: polylines flattened on the GPU
-    int32_t first, count; // geom 0: point range; geom 1: flat_item range
+    int32_t geom;         // 0: host polylines, 1: polylines flattened on the GPU, 2: stroke outlines
+                          // expanded on the GPU
+    int32_t first, count; // geom 0: point range; geom 1: flat_item range; geom 2: stroke_group range
     int32_t line_first, line_count;  // resolved polyline range (filled at flush)
     // paint (paint_pixel, hpp:2265-2377)
     int32_t paint, clamp;

@@ -51,7 +51,7 @@ __global__ void k_flat_count(const float2 *__restrict__ bez, const flat_item *__
     if (i >= n) return;
     flat_item it = items[i];
     if (it.sub_end >= 0) { counts[i] = 1; return; }
-    counts[i] = flatten_cubic<false>(bez[it.pt], bez[it.pt + 1], bez[it.pt + 2], bez[it.pt + 3], nullptr, 0);
+    counts[i] = flatten_cubic<false>(bez[it.pt], bez[it.pt + 1], bez[it.pt + 2], bez[it.pt + 3], it.angular, nullptr, 0);
 }
 
 __global__ void k_flat_emit(const float2 *__restrict__ bez, const flat_item *__restrict__ items, int n,
@@ -68,7 +68,7 @@ __global__ void k_flat_emit(const float2 *__restrict__ bez, const flat_item *__r
         prev[o] = offs[it.sub_end] - 1;   // closing segment from the subpath's last point
         return;
     }
-    flatten_cubic<true>(bez[it.pt], bez[it.pt + 1], bez[it.pt + 2], bez[it.pt + 3], pts + o, cnt);
+    flatten_cubic<true>(bez[it.pt], bez[it.pt + 1], bez[it.pt + 2], bez[it.pt + 3], it.angular, pts + o, cnt);
     for (int k = 0; k < cnt; ++k) prev[o + k] = o + k - 1;
 }
 

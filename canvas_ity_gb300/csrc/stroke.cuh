@@ -1,0 +1,523 @@
+// stroke.cuh -- stroke expansion on the device.
+//
+// The reference turns a stroked path into a fill: the path is flattened with
+// the stroking angle limit (path_to_lines, hpp:1495-1524), split by the dash
+// pattern (dash_lines, hpp:1858-1934) and traced forwards and backwards to
+// add the two half strokes with their joins and caps (add_half_stroke,
+// stroke_lines, hpp:1949-2100).  Every step is sequential along a subpath
+// (the dash phase and the last accepted point are carried from segment to
+// segment), so one thread expands one subpath of the flattened path, once
+// to count its output and once to write it at its scanned offset.  The float
+// operations are the reference's, in its order; the one exception is the
+// round join's acosf/tanf, taken in double precision and rounded to float.
+#ifndef CY_STROKE_CUH
+#define CY_STROKE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device.cuh"
+
+namespace cyg {
+
+static constexpr int kDashCap = 1 << 22;     // dashed points one subpath may produce
+static constexpr int kStrokeCap = 1 << 26;   // outline points one subpath may produce
+
+__device__ __forceinline__ float2 xform(const float *m, float2 p) {
+    return f2(m[0] * p.x + m[2] * p.y + m[4], m[1] * p.x + m[3] * p.y + m[5]);
+}
+__device__ __forceinline__ float len2(float2 a) { return sqrtf(dot2(a, a)); }
+__device__ __forceinline__ float2 unit2(float2 a) { return scl2(1.0f / hi(1.0e-6f, len2(a)), a); }
+
+// One join of add_half_stroke (hpp:1966-2041) at `point` between the
+// accepted segments in_dir/in_len and out_dir/out_len (user space).  Returns
+// the number of device-space points it adds.
+template <bool EMIT>
+__device__ int stroke_join(float2 point, float2 in_dir, float in_len, float2 out_dir, float out_len,
+                           const stroke_style &s, float2 *out, int cap) {
+    const float half = s.half;
+    const float eps = 1.0e-4f;
+    int n = 0;
+    auto put = [&](float2 user) {
+        if (EMIT && n < cap) out[n] = xform(s.fwd, user);
+        ++n;
+    };
+    float2 side_in = add2(point, scl2(half, perp2(in_dir)));
+    float2 side_out = add2(point, scl2(half, perp2(out_dir)));
+    float turn = dot2(perp2(in_dir), out_dir);
+    if (fabsf(turn) < eps) turn = 0.0f;
+    float2 offset = turn == 0.0f ? f2(0.0f, 0.0f) : scl2(half / turn, sub2(out_dir, in_dir));
+    bool tight = dot2(offset, in_dir) < -in_len && dot2(offset, out_dir) > out_len;
+    if (turn > 0.0f && tight) {
+        float2 t = side_in;
+        side_in = side_out;
+        side_out = t;
+        t = in_dir;
+        in_dir = out_dir;
+        out_dir = t;
+        put(side_out);
+        put(point);
+        put(side_in);
+    }
+    if ((turn > 0.0f && !tight) || (turn != 0.0f && s.join == 0 && dot2(offset, offset) <= s.ratio)) {
+        put(add2(point, offset));
+    } else if (s.join == 2) {
+        float cosine = dot2(in_dir, out_dir);
+        float angle = static_cast<float>(acos(static_cast<double>(lo(hi(cosine, -1.0f), 1.0f))));
+        float alpha = 4.0f / 3.0f * static_cast<float>(tan(static_cast<double>(0.25f * angle)));
+        put(side_in);
+        n += flatten_cubic<EMIT>(xform(s.fwd, side_in), xform(s.fwd, add2(side_in, scl2(alpha * half, in_dir))),
+                                 xform(s.fwd, sub2(side_out, scl2(alpha * half, out_dir))), xform(s.fwd, side_out),
+                                 -1.0f, out + (EMIT ? n : 0), cap - n);
+    } else {
+        put(side_in);
+        put(side_out);
+    }
+    if (turn > 0.0f && tight) {
+        put(side_out);
+        put(point);
+        put(side_in);
+    }
+    return n;
+}
+
+// The cap of an open half stroke (hpp:2044-2057) at its last point.
+template <bool EMIT>
+__device__ int stroke_cap(float2 point, float2 in_dir, const stroke_style &s, float2 *out, int cap) {
+    int n = 0;
+    auto put = [&](float2 user) {
+        if (EMIT && n < cap) out[n] = xform(s.fwd, user);
+        ++n;
+    };
+    float2 ahead = scl2(s.half, in_dir);
+    float2 side = perp2(ahead);
+    if (s.cap == 0) {
+        put(add2(point, side));
+        put(sub2(point, side));
+    } else if (s.cap == 1) {
+        put(add2(add2(point, ahead), side));
+        put(sub2(add2(point, ahead), side));
+    } else if (s.cap == 2) {
+        const float k = 0.55228475f;   // 4/3 tan(pi/8)
+        put(add2(point, side));
+        n += flatten_cubic<EMIT>(xform(s.fwd, add2(point, side)), xform(s.fwd, add2(add2(point, side), scl2(k, ahead))),
+                                 xform(s.fwd, add2(add2(point, ahead), scl2(k, side))), xform(s.fwd, add2(point, ahead)),
+                                 -1.0f, out + (EMIT ? n : 0), cap - n);
+        n += flatten_cubic<EMIT>(xform(s.fwd, add2(point, ahead)), xform(s.fwd, sub2(add2(point, ahead), scl2(k, side))),
+                                 xform(s.fwd, add2(sub2(point, side), scl2(k, ahead))), xform(s.fwd, sub2(point, side)),
+                                 -1.0f, out + (EMIT ? n : 0), cap - n);
+    }
+    return n;
+}
+
+// Inputs of the stroke kernels.
+struct stroke_in {
+    const float2 *flat;          // flattened centre lines (flattening output)
+    const int32_t *item_off;     // flattening offsets per flat_item
+    const stroke_group *groups;
+    const stroke_style *styles;
+    const float *dash;           // dash patterns
+    float2 *dash_pts;            // dashed centre lines, group g's at dash_off[g]
+    int2 *dash_subs;             // (count, closed) per dash, group g's at dash_off[g]
+    const int32_t *dash_off;
+    int32_t *dash_nsub;          // dashes per group
+    int32_t nflat;               // centre-line points before the dashed ones in slot numbering
+    int n;
+    int32_t *error;              // set to 1 when a subpath exceeds a cap
+};
+
+static constexpr int kStrokeWarps = 4;   // warps per block of the stroke kernels
+
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Dash pass, one warp per subpath: the lanes measure 32 segments at a time
+// (the user-space lengths of hpp:1895), lane 0 carries the pattern phase
+// through them in order.  EMIT=false writes each group's dashed point count
+// (0 without a pattern); EMIT=true writes the dashes.
+template <bool EMIT>
+__global__ void __launch_bounds__(kStrokeWarps * 32) k_dash(stroke_in in, int32_t *__restrict__ counts) {
+    __shared__ float lens[kStrokeWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int g = blockIdx.x * kStrokeWarps + w;
+    if (g >= in.n) return;
+    stroke_group gr = in.groups[g];
+    const stroke_style s = in.styles[gr.style];
+    if (s.dash_n <= 0) {
+        if (!EMIT && lane == 0) counts[g] = 0;
+        return;
+    }
+    const float *dash = in.dash + s.dash_first;
+    const int a = in.item_off[gr.head], n = in.item_off[gr.end] - a;
+    const float2 *pts = in.flat + a;
+    int o = 0, cap = 0;
+    float2 *out = nullptr;
+    int2 *subs = nullptr;
+    if (EMIT) {
+        o = in.dash_off[g];
+        cap = in.dash_off[g + 1] - o;
+        out = in.dash_pts + o;
+        subs = in.dash_subs + o;
+        if (cap <= 0) {
+            if (lane == 0) in.dash_nsub[g] = 0;
+            return;
+        }
+    }
+    // lane 0's state (hpp:1880-1888)
+    int np = 0, ns = 0, first = 0, seg = s.dash_start;
+    bool emit = (~s.dash_start & 1) != 0;
+    const bool merge_emit = emit;
+    float next = s.dash_next;
+    bool over = false;
+    for (int c = 0; c + 1 < n; c += 32) {
+        int i = c + lane;
+        float line = 0.0f;
+        if (i + 1 < n) line = len2(sub2(xform(s.inv, pts[i + 1]), xform(s.inv, pts[i])));
+        lens[w][lane] = line;
+        __syncwarp();
+        if (lane == 0 && !over) {
+            int m = min(32, n - 1 - c);
+            for (int k = 0; k < m; ++k) {
+                float2 from = pts[c + k], to = pts[c + k + 1];
+                float len = lens[w][k];
+                if (emit) {
+                    if (EMIT && np < cap) out[np] = from;
+                    ++np;
+                }
+                while (next < len) {
+                    if (np >= kDashCap) {
+                        over = true;
+                        break;
+                    }
+                    if (EMIT && np < cap) out[np] = mix2(from, to, next / len);
+                    ++np;
+                    if (emit) {
+                        if (EMIT && ns < cap) subs[ns] = make_int2(np - first, 0);
+                        ++ns;
+                        first = np;
+                    }
+                    seg = seg + 1 < s.dash_n ? seg + 1 : 0;
+                    emit = !emit;
+                    next += dash[seg];
+                }
+                if (over) break;
+                next -= len;
+            }
+        }
+        __syncwarp();
+    }
+    int count = 0;   // dashed point count of the rotation below (lane 0)
+    if (lane == 0 && !over && n > 0) {
+        if (emit) {
+            if (EMIT && np < cap) out[np] = pts[n - 1];
+            ++np;
+            if (EMIT && ns < cap) subs[ns] = make_int2(np - first, 0);
+            ++ns;
+            if (gr.closed && merge_emit) {
+                if (ns == 1) {
+                    if (EMIT) subs[0].y = 1;
+                } else {
+                    count = np - first;
+                    if (EMIT) subs[0].x += count;
+                    --ns;
+                }
+            }
+        }
+    }
+    if (!EMIT) {
+        if (lane == 0) {
+            if (over) atomicOr(in.error, 1);
+            counts[g] = over ? 0 : np;
+        }
+        return;
+    }
+    // Closed subpath whose first and last dashes are drawn: the last dash
+    // moves in front of the first (std::rotate by three reversals).
+    count = __shfl_sync(0xffffffffu, count, 0);
+    np = __shfl_sync(0xffffffffu, np, 0);
+    if (count > 0 && np == cap) {
+        auto reverse = [&](int lo_, int hi_) {
+            int len = hi_ - lo_;
+            for (int t = lane; t < len / 2; t += 32) {
+                float2 x = out[lo_ + t];
+                out[lo_ + t] = out[hi_ - 1 - t];
+                out[hi_ - 1 - t] = x;
+            }
+            __syncwarp();
+        };
+        reverse(0, np - count);
+        reverse(np - count, np);
+        reverse(0, np);
+    }
+    if (lane == 0) in.dash_nsub[g] = np == cap ? ns : 0;
+}
+
+// ------------------------------------------------------------ the walks
+// stroke_lines (hpp:2070-2100) traces every piece (subpath after dashing)
+// forwards and backwards with add_half_stroke.  A walk accepts a point when
+// it lies at least eps from the last accepted one, and each accepted point
+// after the first two completes the join at the accepted point before it; a
+// closed walk wraps around until it reaches the position of its first join,
+// an open one ends with a cap.  So once the accepted points are known, every
+// join is independent: k_walk resolves acceptance 32 walk positions at a
+// time into chunk records, and k_join computes the joins of all chunks of
+// all canvases in parallel, one warp per chunk.
+
+// One chunk of up to 32 consecutive positions of one walk.
+struct walk_chunk {
+    int32_t pts;          // unified index of the piece's first point (centre lines, then dashes)
+    int32_t cnt;          // points of the piece
+    int32_t flags;        // 1 backward, 2 closed, 4 wrap part (positions revisit the first points)
+    int32_t style;
+    uint32_t acc;         // accepted positions (bit = lane)
+    int32_t c1, c2;       // the last two accepted points before the chunk (c2 -1: none yet)
+    int32_t pos0;         // position of lane 0 within its part
+    int32_t n;            // lanes in use
+    int32_t poly0, poly1; // chunks of the chunk's polygon: [poly0, poly1)
+    int32_t pad;
+};
+
+struct walk_out {
+    walk_chunk *chunks;
+    const int32_t *chunk_base;   // first chunk of each group (write pass)
+    int32_t *chunk_count;        // chunks of each group (count pass)
+};
+
+__device__ __forceinline__ const float2 *piece_points(const stroke_in &in, int32_t base) {
+    return base < in.nflat ? in.flat + base : in.dash_pts + (base - in.nflat);
+}
+
+// Walk position -> point of the piece.
+__device__ __forceinline__ int walk_index(int pos, int cnt, bool backward) { return backward ? cnt - 1 - pos : pos; }
+
+// Position of the first join of a closed walk (where the second point after
+// the start is accepted), or -1: one lane, usually a few steps.
+__device__ int first_join(const float2 *pp, int cnt, bool backward, const stroke_style &s) {
+    const float eps = 1.0e-4f;
+    float2 pt = xform(s.inv, pp[walk_index(0, cnt, backward)]);
+    int seen = 0;
+    for (int pos = 1; pos < cnt; ++pos) {
+        float2 x = xform(s.inv, pp[walk_index(pos, cnt, backward)]);
+        if (len2(sub2(x, pt)) >= eps) {
+            if (++seen == 2) return pos;
+            pt = x;
+        }
+    }
+    return -1;
+}
+
+// k_walk: one warp per group.  WRITE=false counts each group's chunks;
+// WRITE=true writes them from out.chunk_base[g].
+template <bool WRITE>
+__global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, walk_out wo) {
+    const float eps = 1.0e-4f;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int g = blockIdx.x * kStrokeWarps + w;
+    if (g >= in.n) return;
+    stroke_group gr = in.groups[g];
+    const stroke_style s = in.styles[gr.style];
+    int nch = 0;                                     // chunks so far
+    const int cb = WRITE ? wo.chunk_base[g] : 0;
+    // one walk: positions [0, n1) of the first part (n1 = cnt + 1 with the
+    // cap position when open), then the wrap [0, fin)
+    auto walk = [&](int32_t ubase, const float2 *pp, int cnt, bool closed, bool backward, int poly0, int poly1) {
+        const int begin = walk_index(0, cnt, backward);
+        int c1 = begin, c2 = -1;
+        bool synced = true;
+        float2 point = xform(s.inv, pp[begin]);
+        const int n1 = closed ? cnt : cnt + 1;
+        int fin = -1;
+        if (closed) {
+            int f = 0;
+            if (lane == 0) f = first_join(pp, cnt, backward, s);
+            fin = __shfl_sync(full, f, 0);
+        }
+        for (int part = 0; part < 2; ++part) {
+            const int np_all = part == 0 ? n1 : (fin > 0 ? fin : 0);
+            for (int p0 = 0; p0 < np_all; p0 += 32) {
+                const int np = min(32, np_all - p0);
+                const int pos = p0 + lane;
+                const bool point_lane = lane < np && pos < cnt;   // not the cap position
+                const int idx = point_lane ? walk_index(pos, cnt, backward) : begin;
+                float2 q = xform(s.inv, pp[idx]);
+                float2 qprev = q;
+                if (point_lane) {
+                    int pp_pos = pos > 0 ? pos - 1 : (part == 1 ? cnt - 1 : 0);
+                    qprev = xform(s.inv, pp[walk_index(pp_pos, cnt, backward)]);
+                }
+                const bool is_start = part == 0 && pos == 0;
+                bool ok = !point_lane || is_start || len2(sub2(q, qprev)) >= eps;
+                unsigned acc;
+                if (synced && __all_sync(full, ok)) {
+                    acc = __ballot_sync(full, point_lane && !is_start);
+                } else {
+                    unsigned m = 0;
+                    if (lane == 0) {
+                        float2 pt = point;
+                        for (int t = 0; t < np; ++t) {
+                            int ps = p0 + t;
+                            if ((part == 0 && ps == 0) || ps >= cnt) continue;
+                            float2 x = xform(s.inv, pp[walk_index(ps, cnt, backward)]);
+                            if (len2(sub2(x, pt)) >= eps) {
+                                m |= 1u << t;
+                                pt = x;
+                            }
+                        }
+                    }
+                    acc = __shfl_sync(full, m, 0);
+                }
+                if (WRITE && lane == 0) {
+                    walk_chunk h;
+                    h.pts = ubase;
+                    h.cnt = cnt;
+                    h.flags = (backward ? 1 : 0) | (closed ? 2 : 0) | (part == 1 ? 4 : 0);
+                    h.style = gr.style;
+                    h.acc = acc;
+                    h.c1 = c1;
+                    h.c2 = c2;
+                    h.pos0 = p0;
+                    h.n = np;
+                    h.poly0 = cb + poly0;
+                    h.poly1 = cb + poly1;
+                    h.pad = 0;
+                    wo.chunks[cb + nch] = h;
+                }
+                ++nch;
+                if (acc) {
+                    int hb = 31 - __clz(acc);
+                    unsigned rest = acc & ~(1u << hb);
+                    c2 = rest ? walk_index(p0 + (31 - __clz(rest)), cnt, backward) : c1;
+                    c1 = walk_index(p0 + hb, cnt, backward);
+                    point = xform(s.inv, pp[c1]);
+                }
+                // in step when the last position with a point was accepted
+                int last = min(np, cnt - p0) - 1;
+                synced = last >= 0 && (((acc >> last) & 1u) || (part == 0 && p0 + last == 0));
+            }
+        }
+    };
+    // chunks of a walk: used to place polygons before the walks run
+    auto walk_chunks = [&](const float2 *pp, int cnt, bool closed, bool backward) {
+        int n1 = closed ? cnt : cnt + 1, fin = 0;
+        if (closed) {
+            int f = 0;
+            if (lane == 0) f = first_join(pp, cnt, backward, s);
+            fin = max(__shfl_sync(full, f, 0), 0);
+        }
+        return (n1 + 31) / 32 + (fin + 31) / 32;
+    };
+    auto piece = [&](int32_t ubase, int cnt, bool closed) {
+        if (cnt < 2) return;
+        const float2 *pp = piece_points(in, ubase);
+        const int start = nch;
+        const int nf = walk_chunks(pp, cnt, closed, false);
+        const int nb = walk_chunks(pp, cnt, closed, true);
+        if (closed) {
+            walk(ubase, pp, cnt, true, false, start, start + nf);
+            walk(ubase, pp, cnt, true, true, start + nf, start + nf + nb);
+        } else {
+            walk(ubase, pp, cnt, false, false, start, start + nf + nb);
+            walk(ubase, pp, cnt, false, true, start, start + nf + nb);
+        }
+    };
+    if (s.dash_n > 0) {
+        const int d0 = in.dash_off[g];
+        const int ns = in.dash_nsub[g];
+        int q = 0;
+        for (int k = 0; k < ns; ++k) {
+            int2 sub = in.dash_subs[d0 + k];
+            piece(in.nflat + d0 + q, sub.x, sub.y != 0);
+            q += sub.x;
+        }
+    } else {
+        const int a = in.item_off[gr.head], b = in.item_off[gr.end];
+        piece(a, b - a, gr.closed != 0);
+    }
+    if (!WRITE && lane == 0) wo.chunk_count[g] = nch;
+}
+
+// k_join: one warp per chunk.  EMIT=false writes each position's point
+// count to jcnt[32 * chunk + lane] and each chunk's total to csum[chunk];
+// EMIT=true writes the joins (and caps) at coff[chunk] + the counts of the
+// lanes before, with prev links: the point before, except for a polygon's
+// first point, linked to the polygon's last.
+template <bool EMIT>
+__global__ void __launch_bounds__(kStrokeWarps * 32) k_join(stroke_in in, const walk_chunk *__restrict__ chunks,
+                                                            int n_chunks, int32_t *__restrict__ jcnt,
+                                                            int32_t *__restrict__ csum, const int64_t *__restrict__ coff,
+                                                            float2 *__restrict__ out, int32_t *__restrict__ prev,
+                                                            int32_t base, int64_t cap) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int c = blockIdx.x * kStrokeWarps + w;
+    if (c >= n_chunks) return;
+    const walk_chunk h = chunks[c];
+    const stroke_style s = in.styles[h.style];
+    const float2 *pp = piece_points(in, h.pts);
+    const bool backward = h.flags & 1, closed = h.flags & 2;
+    const int cnt = h.cnt;
+    const int pos = h.pos0 + lane;
+    const bool valid = lane < h.n;
+    const bool is_cap = valid && !closed && !(h.flags & 4) && pos == cnt;
+    // the two accepted points before this lane's position
+    unsigned below = h.acc & ((1u << lane) - 1u);
+    int p1 = h.c1, p2 = h.c2;
+    if (below) {
+        int b1 = 31 - __clz(below);
+        p1 = walk_index(h.pos0 + b1, cnt, backward);
+        unsigned rest = below & ~(1u << b1);
+        p2 = rest ? walk_index(h.pos0 + (31 - __clz(rest)), cnt, backward) : h.c1;
+    }
+    const bool join = ((h.acc >> lane) & 1u) && p2 >= 0;
+    const bool capped = is_cap && p2 >= 0;
+    float2 jp = f2(0.0f, 0.0f), din = jp, dout = jp;
+    if (join || capped) {
+        jp = xform(s.inv, pp[p1]);
+        din = sub2(jp, xform(s.inv, pp[p2]));
+    }
+    if (join) dout = sub2(xform(s.inv, pp[walk_index(pos, cnt, backward)]), jp);
+    int n = 0;
+    if (!EMIT) {
+        if (join) n = stroke_join<false>(jp, unit2(din), len2(din), unit2(dout), len2(dout), s, nullptr, 0);
+        else if (capped) n = stroke_cap<false>(jp, unit2(din), s, nullptr, 0);
+        if (n > (1 << 24)) {   // a join or cap far beyond any canvas (line width ~1e11)
+            atomicOr(in.error, 1);
+            n = 0;
+        }
+        jcnt[32LL * c + lane] = n;
+        int t = warp_sum(n);
+        if (lane == 0) csum[c] = t;
+        return;
+    }
+    n = valid ? jcnt[32LL * c + lane] : 0;
+    int incl = n;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int t = __shfl_up_sync(full, incl, d);
+        if (lane >= d) incl += t;
+    }
+    const int64_t at = coff[c] + incl - n;
+    if (n == 0 || at < 0 || at + n > cap) return;
+    if (join) stroke_join<true>(jp, unit2(din), len2(din), unit2(dout), len2(dout), s, out + at, n);
+    else stroke_cap<true>(jp, unit2(din), s, out + at, n);
+    const int64_t first = coff[h.poly0], last = coff[h.poly1] - 1;
+    for (int k = 0; k < n; ++k) {
+        int64_t e = at + k;
+        prev[e] = base + static_cast<int32_t>(e == first ? last : e - 1);
+    }
+}
+
+// Output range of each group: goff[g] = coff[chunk_base[g]] (g <= n).
+__global__ void k_group_off(const int32_t *__restrict__ chunk_base, const int64_t *__restrict__ coff, int n,
+                            int64_t *__restrict__ goff) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g <= n) goff[g] = coff[chunk_base[g]];
+}
+
+}  // namespace cyg
+
+#endif

@@ -49,6 +49,22 @@ def set_engine(engine: int) -> None:
     load().cy_set_engine(int(engine))
 
 
+def set_device_stroke(on: bool) -> None:
+    """Expand strokes on the GPU (True, the default) or on the host with the
+    reference's own acosf/tanf (False); applies to the whole process."""
+    lib = load()
+    lib.cy_set_device_stroke.restype = None
+    lib.cy_set_device_stroke.argtypes = [ctypes.c_int]
+    lib.cy_set_device_stroke(1 if on else 0)
+
+
+def device_stroke() -> bool:
+    lib = load()
+    lib.cy_device_stroke.restype = ctypes.c_int
+    lib.cy_device_stroke.argtypes = []
+    return bool(lib.cy_device_stroke())
+
+
 def replay(trace: bytes) -> Tuple[bytes, List[float]]:
     """Replay a call list through canvas_ity::canvas on the GPU.
 
@@ -61,7 +77,8 @@ def replay(trace: bytes) -> Tuple[bytes, List[float]]:
         res = (ctypes.c_float * rcap)()
         n_img, n_res = ctypes.c_size_t(0), ctypes.c_int(0)
         rc = lib.cy_replay(trace, len(trace), img, cap, ctypes.byref(n_img), res, rcap, ctypes.byref(n_res))
-        if rc == -2:
+        if rc == -2 and (n_img.value > cap or n_res.value > rcap):
+            # the outputs did not fit: retry with the sizes reported
             cap, rcap = max(cap, n_img.value), max(rcap, n_res.value)
             continue
         if rc != 0:

@@ -88,6 +88,36 @@ int cy_fill_path(cy_ctx *ctx, const float *points, const int *subpath_counts, in
 int cy_fill_lines(cy_ctx *ctx, const float *points, const int *subpath_counts, int n_subpaths,
                   const cy_paint *paint, const cy_draw_state *state);
 
+/* Stroke style of one stroke() (hpp:375-440, 1858-2100). */
+typedef struct cy_stroke_style {
+    float line_width;
+    float miter_limit;
+    int line_join;             /* canvas_ity::join_style: 0 miter, 1 bevel, 2 rounded */
+    int line_cap;              /* canvas_ity::cap_style: 0 butt, 1 square, 2 circle  */
+    const float *dash;         /* the pattern as set_line_dash stores it, or NULL    */
+    int n_dash;                /* 0: solid                                           */
+    float dash_offset;
+    float forward[6];          /* a b c d e f of the current transform               */
+    float inverse[6];          /* and of its inverse                                 */
+} cy_stroke_style;
+
+/* stroke() with the stroke expansion on the GPU: path_to_lines(true),
+ * dash_lines, stroke_lines and render_main (hpp:3050-3055, 1495-1524,
+ * 1858-2100, 2551-2605).  `points` and `subpath_counts` are laid out as for
+ * cy_fill_path; subpath_closed[i] is the subpath's closed flag.  The
+ * outline is the reference's point for point, except that a round join's
+ * acosf/tanf are taken in double precision and rounded to float.  Fails
+ * with CY_ENOMEM when a subpath would dash into more than 2^22 points. */
+int cy_stroke_path(cy_ctx *ctx, const float *points, const int *subpath_counts, const int *subpath_closed,
+                   int n_subpaths, const cy_stroke_style *style, const cy_paint *paint,
+                   const cy_draw_state *state);
+
+/* Where canvas_ity::canvas::stroke() expands strokes, for every canvas of
+ * the process: 1 (the default) on the GPU through cy_stroke_path, 0 on the
+ * host (the reference's own acosf/tanf) through cy_fill_lines. */
+void cy_set_device_stroke(int on);
+int cy_device_stroke(void);
+
 /* clip() (hpp:3057-3099): intersects mask `mask_in` with the coverage of
  * the Bezier path under `fill_rule` (0 nonzero as in the reference, 1
  * even-odd); the new mask id is written to *mask_out.  Mask ids are

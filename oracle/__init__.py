@@ -18,8 +18,11 @@ from typing import List, Optional, Tuple
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 ORACLE_SO = os.path.join(BUILD_DIR, "libcy_oracle.so")
-# Same restatement with equal-magnitude, opposite-sign runs of a cell ordered
-# negative first (the GPU's order) instead of std::sort's own choice.
+# Variants of the same restatement:
+#  ties="sign": equal-magnitude, opposite-sign runs of a cell ordered negative
+#    first (the GPU's order) instead of std::sort's own choice;
+#  trig="cr": round joins take acos and tan in double precision rounded to
+#    float (the GPU stroke expansion's choice) instead of libm's acosf/tanf.
 ORACLE_SIGN_SO = os.path.join(BUILD_DIR, "libcy_oracle_sign.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libcy_ref.so")
@@ -28,13 +31,23 @@ REFERENCE_ROOT = os.environ.get("CY_REFERENCE_ROOT", "/root/reference")
 _FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
 
 
-def build(force: bool = False, ties: str = "reference") -> str:
+def _variant(ties: str, trig: str) -> Tuple[str, list]:
+    name, extra = "libcy_oracle", []
+    if ties == "sign":
+        name, extra = name + "_sign", extra + ["-DCYO_TIES_BY_SIGN"]
+    if trig == "cr":
+        name, extra = name + "_cr", extra + ["-DCYO_CR_TRIG"]
+    return os.path.join(BUILD_DIR, name + ".so"), extra
+
+
+def build(force: bool = False, ties: str = "reference", trig: str = "libm") -> str:
     """Compile the oracle restatement (fast: one translation unit).
 
     ties="sign" builds the variant whose sort orders equal-magnitude,
-    opposite-sign runs of one cell negative first."""
+    opposite-sign runs of one cell negative first; trig="cr" the variant
+    whose round joins use correctly rounded acos/tan."""
     src = os.path.join(HERE, "cy_oracle.cpp")
-    out, extra = (ORACLE_SIGN_SO, ["-DCYO_TIES_BY_SIGN"]) if ties == "sign" else (ORACLE_SO, [])
+    out, extra = _variant(ties, trig)
     hdrs = [os.path.join(HERE, "..", "include", h) for h in ("cy_trace.h", "cy_replay.hpp")]
     newest = max(os.path.getmtime(p) for p in [src] + hdrs)
     if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
@@ -74,7 +87,7 @@ class _Lib:
             res = (ctypes.c_float * rcap)()
             n_img, n_res = ctypes.c_size_t(0), ctypes.c_int(0)
             rc = self.fn(trace, len(trace), img, cap, ctypes.byref(n_img), res, rcap, ctypes.byref(n_res))
-            if rc == -2:
+            if rc == -2 and (n_img.value > cap or n_res.value > rcap):
                 cap, rcap = max(cap, n_img.value), max(rcap, n_res.value)
                 continue
             if rc != 0:
@@ -86,21 +99,21 @@ _oracles: dict = {}
 _ref: Optional[_Lib] = None
 
 
-def _get(ties: str) -> _Lib:
-    if ties not in _oracles:
-        _oracles[ties] = _Lib(build(ties=ties), "cyo_replay")
-    return _oracles[ties]
+def _get(ties: str, trig: str = "libm") -> _Lib:
+    if (ties, trig) not in _oracles:
+        _oracles[(ties, trig)] = _Lib(build(ties=ties, trig=trig), "cyo_replay")
+    return _oracles[(ties, trig)]
 
 
-def replay(trace: bytes, ties: str = "reference") -> Tuple[bytes, List[float]]:
+def replay(trace: bytes, ties: str = "reference", trig: str = "libm") -> Tuple[bytes, List[float]]:
     """Replay through the oracle: (concatenated get_image_data bytes, results)."""
-    return _get(ties).replay(trace)
+    return _get(ties, trig).replay(trace)
 
 
-def replay_linear(trace: bytes, width: int, height: int, ties: str = "reference"):
+def replay_linear(trace: bytes, width: int, height: int, ties: str = "reference", trig: str = "libm"):
     """Replay through the oracle; return the final float canvas (H, W, 4)."""
     import numpy as np
-    fn = _get(ties).lib.cyo_replay_linear
+    fn = _get(ties, trig).lib.cyo_replay_linear
     fn.restype = ctypes.c_int
     fn.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t,
                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]

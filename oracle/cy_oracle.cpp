@@ -124,6 +124,18 @@ static bool run_before(const run &l, const run &r) {
     return fabsf(l.delta) < fabsf(r.delta);
 }
 
+// The round join's angle (hpp:2006-2008): libm's acosf and tanf, as the
+// reference calls them; built with CYO_CR_TRIG, acos and tan in double
+// precision rounded to float, which is what the GPU's stroke expansion
+// computes (the two differ by one ulp on a small fraction of inputs).
+#ifdef CYO_CR_TRIG
+static float join_acos(float x) { return static_cast<float>(std::acos(static_cast<double>(x))); }
+static float join_tan(float x) { return static_cast<float>(std::tan(static_cast<double>(x))); }
+#else
+static float join_acos(float x) { return acosf(x); }
+static float join_tan(float x) { return tanf(x); }
+#endif
+
 struct brush {
     enum kind_t { solid, linear, radial, image } kind;
     std::vector<col> colors;
@@ -896,8 +908,8 @@ void canvas::half_stroke(size_t begin, size_t end, bool closed) {
                 lines.pts.push_back(apply(fwd, add(point, off)));
             } else if (line_join == rounded) {
                 float cosine = dot(in_dir, out_dir);
-                float angle = acosf(lo(hi(cosine, -1.0f), 1.0f));
-                float alpha = 4.0f / 3.0f * tanf(0.25f * angle);
+                float angle = join_acos(lo(hi(cosine, -1.0f), 1.0f));
+                float alpha = 4.0f / 3.0f * join_tan(0.25f * angle);
                 lines.pts.push_back(apply(fwd, side_in));
                 bezier(apply(fwd, side_in), apply(fwd, add(side_in, scl(alpha * half, in_dir))),
                        apply(fwd, sub(side_out, scl(alpha * half, out_dir))), apply(fwd, side_out), -1.0f);

@@ -12,7 +12,7 @@ INCLUDE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "includ
 
 def declared_functions():
     names = set()
-    for h in ("cy_gpu.h", "canvas_ity_c.h", "cy_batch.h"):
+    for h in ("cy_gpu.h", "canvas_ity_c.h", "cy_batch.h", "cy_serve.h"):
         path = os.path.join(INCLUDE, h)
         if not os.path.exists(path):
             continue

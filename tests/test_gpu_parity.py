@@ -37,6 +37,21 @@ def engine(request):
     return request.param
 
 
+@pytest.fixture(params=["device", "host"])
+def stroke(request):
+    """Where strokes are expanded: on the GPU (the default) or on the host."""
+    native.set_device_stroke(request.param == "device")
+    yield request.param
+    native.set_device_stroke(True)
+
+
+def trig():
+    """The oracle variant whose round joins compute what the library's stroke
+    expansion computes: acos/tan rounded from double on the GPU, libm's
+    acosf/tanf on the host."""
+    return "cr" if native.device_stroke() else "libm"
+
+
 @pytest.mark.parametrize("entry", MANIFEST, ids=[e["name"] for e in MANIFEST])
 def test_reference_suite(engine, entry):
     tb = G.load_fixture(entry)
@@ -84,7 +99,7 @@ def assert_float_canvas_exact(tb, what):
     reference's sort leaves unordered (equal magnitude, opposite sign)."""
     w, h = T.canvas_size(tb)
     got = native.replay_linear(tb, w, h)
-    want = oracle.replay_linear(tb, w, h, ties="sign")
+    want = oracle.replay_linear(tb, w, h, ties="sign", trig=trig())
     bad = np.argwhere(got != want)
     assert bad.size == 0, f"{what}: {len(bad)} float values differ, first at (y, x, c) = {bad[0].tolist()}"
 
@@ -101,26 +116,29 @@ def test_reference_suite_bytes_identical(engine, entry):
 
 
 @pytest.mark.parametrize("seed", range(8))
-def test_rgba8_identical_to_oracle_on_workload(engine, seed):
+def test_rgba8_identical_to_oracle_on_workload(engine, stroke, seed):
     """RGBA8 bytes of many-canvas workload canvases equal the oracle's with
-    the GPU's order for runs std::sort leaves unordered."""
+    the GPU's order for runs std::sort leaves unordered; with strokes
+    expanded on the GPU they also equal the oracle with libm's round joins."""
     tb = scenes.c3_canvas(100 + seed)
-    assert native.replay(tb)[0] == oracle.replay(tb, ties="sign")[0]
+    got = native.replay(tb)[0]
+    assert got == oracle.replay(tb, ties="sign", trig=trig())[0]
+    assert got == oracle.replay(tb, ties="sign")[0]
 
 
 @pytest.mark.parametrize("entry", MANIFEST, ids=[e["name"] for e in MANIFEST])
-def test_float_canvas_bit_exact_reference_suite(engine, entry):
+def test_float_canvas_bit_exact_reference_suite(engine, stroke, entry):
     assert_float_canvas_exact(G.load_fixture(entry), entry["name"])
 
 
 @pytest.mark.parametrize("config", ["c0_small", "c1_small", "c2_small", "mixed_small"])
 @pytest.mark.parametrize("seed", range(3))
-def test_float_canvas_bit_exact_seeded(engine, config, seed):
+def test_float_canvas_bit_exact_seeded(engine, stroke, config, seed):
     assert_float_canvas_exact(scenes.small_scene(config, seed), f"{config}/{seed}")
 
 
 @pytest.mark.parametrize("seed", range(6))
-def test_float_canvas_bit_exact_batched_workload(engine, seed):
+def test_float_canvas_bit_exact_batched_workload(engine, stroke, seed):
     """Canvases of the many-canvas workload (random size, 8-128 paths of the
     c0/c1/c2 mixture, global transform)."""
     assert_float_canvas_exact(scenes.c3_canvas(seed), f"c3 canvas {seed}")
