@@ -321,7 +321,7 @@ struct frame {
     int64_t n_groups = 0, n_styles = 0, n_dash = 0;
     // Device stroke expansion: flattened centre lines occupy flat_pts[0,
     // nflat), the outlines follow at nflat; dashed centre lines are apart.
-    int64_t nflat = 0, n_outline = 0, n_dashed = 0, n_chunks = 0;
+    int64_t nflat = 0, n_outline = 0, n_dashed = 0, n_pieces = 0, n_chunks = 0;
     bool any_dash = false;
     std::vector<int32_t> cmd_cv;
     int64_t get_total = 0;
@@ -348,8 +348,8 @@ struct frame {
     dbuf row_cnt, row_off, row_cur, row_len, row_meta, long_rows, n_long, runs, sums;
     dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
-    dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, st_err, wk_cnt, wk_base, wk_chunks, jn_cnt, jn_sum,
-        jn_off, st_goff;
+    dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, st_err, pc_cnt, pc_base, pc_list, wk_cnt, wk_base,
+        wk_chunks, jn_cnt, jn_sum, jn_off, st_goff;
     hbuf staging, offs_host, rowoff_host, get_host, stoff_host;
     char *d = nullptr;
     size_t o_cmd = 0, o_hpts = 0, o_hprev = 0, o_bez = 0, o_items = 0, o_soff = 0, o_scol = 0, o_tex = 0, o_put = 0;
@@ -392,7 +392,7 @@ struct frame {
         bases.clear();
         n_hpts = n_bez = n_items_all = n_stop = n_tex = n_put = 0;
         n_groups = n_styles = n_dash = 0;
-        nflat = n_outline = n_dashed = n_chunks = 0;
+        nflat = n_outline = n_dashed = n_pieces = n_chunks = 0;
         any_dash = false;
         cmd_cv.clear();
         get_total = 0;
@@ -423,7 +423,8 @@ struct frame {
                      &row_off, &row_cur, &row_len, &row_meta, &long_rows, &n_long, &runs, &sums, &tabs_dev, &cp_cnt, &cp_off,
                      &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev, &dash_cnt, &dash_off, &dash_pts,
-                     &dash_subs, &dash_nsub, &st_err, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt, &jn_sum, &jn_off, &st_goff};
+                     &dash_subs, &dash_nsub, &st_err, &pc_cnt, &pc_base, &pc_list, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt,
+                     &jn_sum, &jn_off, &st_goff};
         for (dbuf *x : b) x->release();
         staging.release();
         stoff_host.release();
@@ -722,7 +723,7 @@ int frame::stroke_passes(bool sizing) {
     int32_t *hb = static_cast<int32_t *>(stoff_host.p);
     if (sizing) {
         if (!st_err.ensure(4) || !dash_cnt.ensure(gn * 4) || !dash_off.ensure(gn * 4) || !dash_nsub.ensure(gn * 4) ||
-            !wk_cnt.ensure(gn * 4) || !wk_base.ensure(gn * 4) || !st_goff.ensure(gn * 8) ||
+            !pc_cnt.ensure(gn * 4) || !pc_base.ensure(gn * 4) || !st_goff.ensure(gn * 8) ||
             !stoff_host.ensure(gn * 8) || !dash_pts.ensure(256) || !dash_subs.ensure(256))
             return fail(CY_ENOMEM, __LINE__);
         hb = static_cast<int32_t *>(stoff_host.p);
@@ -753,15 +754,27 @@ int frame::stroke_passes(bool sizing) {
         k_dash<true><<<sgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), nullptr);
         launches += 3 + scan_launch_count(ng + 1);
     }
-    walk_out wo;
-    wo.chunks = nullptr;
-    wo.chunk_base = nullptr;
-    wo.chunk_count = wk_cnt.as<int32_t>();
-    k_walk<false><<<sgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wo);
-    if (!ok(cudaMemsetAsync(wk_cnt.as<int32_t>() + ng, 0, 4, stream))) return status;
-    if (int rc = scan(wk_cnt.as<int32_t>(), wk_base.as<int32_t>(), ng + 1)) return rc;
+    // pieces (subpaths after dashing), then their walks' chunks
+    const int g256 = (ng + 255) / 256;
+    k_piece_count<<<g256, 256, 0, stream>>>(stroke_args(), pc_cnt.as<int32_t>());
+    if (!ok(cudaMemsetAsync(pc_cnt.as<int32_t>() + ng, 0, 4, stream))) return status;
+    if (int rc = scan(pc_cnt.as<int32_t>(), pc_base.as<int32_t>(), ng + 1)) return rc;
     if (sizing) {
-        if (!read_back(hb, wk_base.as<int32_t>() + ng, 4)) return status;
+        if (!read_back(hb, pc_base.as<int32_t>() + ng, 4)) return status;
+        n_pieces = hb[0];
+        if (n_pieces < 0 || n_pieces > (static_cast<int64_t>(1) << 30)) return fail(CY_ENOMEM, __LINE__);
+        size_t np1 = static_cast<size_t>(n_pieces) + 1;
+        if (!pc_list.ensure(np1 * sizeof(stroke_piece)) || !wk_cnt.ensure(np1 * 4) || !wk_base.ensure(np1 * 4))
+            return fail(CY_ENOMEM, __LINE__);
+    }
+    const int npc = static_cast<int>(n_pieces);
+    k_pieces<<<g256, 256, 0, stream>>>(stroke_args(), pc_base.as<int32_t>(), pc_list.as<stroke_piece>());
+    k_piece_chunks<<<std::max(1, (npc + 255) / 256), 256, 0, stream>>>(stroke_args(), pc_list.as<stroke_piece>(), npc,
+                                                                     wk_cnt.as<int32_t>());
+    if (!ok(cudaMemsetAsync(wk_cnt.as<int32_t>() + npc, 0, 4, stream))) return status;
+    if (int rc = scan(wk_cnt.as<int32_t>(), wk_base.as<int32_t>(), npc + 1)) return rc;
+    if (sizing) {
+        if (!read_back(hb, wk_base.as<int32_t>() + npc, 4)) return status;
         n_chunks = hb[0];
         if (n_chunks < 0 || n_chunks > (static_cast<int64_t>(1) << 26)) return fail(CY_ENOMEM, __LINE__);
         size_t nc = static_cast<size_t>(n_chunks) + 1;
@@ -769,9 +782,8 @@ int frame::stroke_passes(bool sizing) {
             !jn_off.ensure(nc * 8))
             return fail(CY_ENOMEM, __LINE__);
     }
-    wo.chunks = wk_chunks.as<walk_chunk>();
-    wo.chunk_base = wk_base.as<int32_t>();
-    k_walk<true><<<sgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wo);
+    k_walk<<<std::max(1, (npc + kStrokeWarps - 1) / kStrokeWarps), kStrokeWarps * 32, 0, stream>>>(
+        stroke_args(), pc_list.as<stroke_piece>(), npc, wk_base.as<int32_t>(), wk_chunks.as<walk_chunk>());
     const int nch = static_cast<int>(n_chunks);
     const int jgrid = std::max(1, (nch + kStrokeWarps - 1) / kStrokeWarps);
     k_join<false><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(), nch,
@@ -779,9 +791,9 @@ int frame::stroke_passes(bool sizing) {
                                                            nullptr, nullptr, 0, 0);
     if (!ok(cudaMemsetAsync(jn_sum.as<int32_t>() + nch, 0, 4, stream))) return status;
     if (int rc = scan64(jn_sum.as<int32_t>(), jn_off.as<int64_t>(), nch + 1)) return rc;
-    k_group_off<<<(ng + 1 + 255) / 256, 256, 0, stream>>>(wk_base.as<int32_t>(), jn_off.as<int64_t>(), ng,
-                                                         st_goff.as<int64_t>());
-    launches += 5 + 2 * scan_launch_count(ng + 1) + scan_launch_count(nch + 1);
+    k_group_off<<<(ng + 1 + 255) / 256, 256, 0, stream>>>(pc_base.as<int32_t>(), wk_base.as<int32_t>(),
+                                                         jn_off.as<int64_t>(), ng, st_goff.as<int64_t>());
+    launches += 6 + scan_launch_count(ng + 1) + scan_launch_count(npc + 1) + scan_launch_count(nch + 1);
     if (sizing) {
         int64_t *g64 = static_cast<int64_t *>(stoff_host.p);
         int32_t *errp = reinterpret_cast<int32_t *>(g64 + ng + 1);

@@ -280,10 +280,12 @@ struct walk_chunk {
     int32_t pad;
 };
 
-struct walk_out {
-    walk_chunk *chunks;
-    const int32_t *chunk_base;   // first chunk of each group (write pass)
-    int32_t *chunk_count;        // chunks of each group (count pass)
+// One piece to walk (a subpath after dashing).
+struct stroke_piece {
+    int32_t pts;     // unified index of the first point (centre lines, then dashes)
+    int32_t cnt;
+    int32_t closed;
+    int32_t style;
 };
 
 __device__ __forceinline__ const float2 *piece_points(const stroke_in &in, int32_t base) {
@@ -309,35 +311,83 @@ __device__ int first_join(const float2 *pp, int cnt, bool backward, const stroke
     return -1;
 }
 
-// k_walk: one warp per group.  WRITE=false counts each group's chunks;
-// WRITE=true writes them from out.chunk_base[g].
-template <bool WRITE>
-__global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, walk_out wo) {
+// Pieces of each group: 1 without a dash pattern, else its dashes.
+__global__ void k_piece_count(stroke_in in, int32_t *__restrict__ counts) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= in.n) return;
+    const stroke_style &s = in.styles[in.groups[g].style];
+    counts[g] = s.dash_n > 0 ? in.dash_nsub[g] : 1;
+}
+
+// The piece records of each group, from base[g].
+__global__ void k_pieces(stroke_in in, const int32_t *__restrict__ base, stroke_piece *__restrict__ pieces) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= in.n) return;
+    stroke_group gr = in.groups[g];
+    const stroke_style &s = in.styles[gr.style];
+    stroke_piece *out = pieces + base[g];
+    if (s.dash_n > 0) {
+        const int d0 = in.dash_off[g], ns = in.dash_nsub[g];
+        int q = 0;
+        for (int k = 0; k < ns; ++k) {
+            int2 sub = in.dash_subs[d0 + k];
+            out[k] = stroke_piece{in.nflat + d0 + q, sub.x, sub.y, gr.style};
+            q += sub.x;
+        }
+    } else {
+        const int a = in.item_off[gr.head], b = in.item_off[gr.end];
+        out[0] = stroke_piece{a, b - a, gr.closed, gr.style};
+    }
+}
+
+// Chunks of one walk: its first part (an open walk has the cap position
+// after its points), then the wrap of a closed walk up to its first join.
+__device__ __forceinline__ int walk_chunk_count(int cnt, bool closed, int fin) {
+    return ((closed ? cnt : cnt + 1) + 31) / 32 + (closed && fin > 0 ? (fin + 31) / 32 : 0);
+}
+
+// Chunks of each piece (both walks), without walking.
+__global__ void k_piece_chunks(stroke_in in, const stroke_piece *__restrict__ pieces, int n,
+                               int32_t *__restrict__ counts) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    stroke_piece pc = pieces[i];
+    int c = 0;
+    if (pc.cnt >= 2) {
+        const stroke_style &s = in.styles[pc.style];
+        const float2 *pp = piece_points(in, pc.pts);
+        int ff = pc.closed ? first_join(pp, pc.cnt, false, s) : -1;
+        int fb = pc.closed ? first_join(pp, pc.cnt, true, s) : -1;
+        c = walk_chunk_count(pc.cnt, pc.closed != 0, ff) + walk_chunk_count(pc.cnt, pc.closed != 0, fb);
+    }
+    counts[i] = c;
+}
+
+// k_walk: one warp per piece, writing its chunks from chunk_base[piece].
+__global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, const stroke_piece *__restrict__ pieces,
+                                                            int n_pieces, const int32_t *__restrict__ chunk_base,
+                                                            walk_chunk *__restrict__ chunks) {
     const float eps = 1.0e-4f;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int g = blockIdx.x * kStrokeWarps + w;
-    if (g >= in.n) return;
-    stroke_group gr = in.groups[g];
-    const stroke_style s = in.styles[gr.style];
-    int nch = 0;                                     // chunks so far
-    const int cb = WRITE ? wo.chunk_base[g] : 0;
-    // one walk: positions [0, n1) of the first part (n1 = cnt + 1 with the
-    // cap position when open), then the wrap [0, fin)
-    auto walk = [&](int32_t ubase, const float2 *pp, int cnt, bool closed, bool backward, int poly0, int poly1) {
+    const int pi = blockIdx.x * kStrokeWarps + w;
+    if (pi >= n_pieces) return;
+    const stroke_piece pc = pieces[pi];
+    const int cnt = pc.cnt;
+    if (cnt < 2) return;
+    const bool closed = pc.closed != 0;
+    const stroke_style s = in.styles[pc.style];
+    const float2 *pp = piece_points(in, pc.pts);
+    const int cb = chunk_base[pi];
+    int nch = 0;
+    auto walk = [&](bool backward, int fin, int poly0, int poly1) {
         const int begin = walk_index(0, cnt, backward);
         int c1 = begin, c2 = -1;
         bool synced = true;
         float2 point = xform(s.inv, pp[begin]);
         const int n1 = closed ? cnt : cnt + 1;
-        int fin = -1;
-        if (closed) {
-            int f = 0;
-            if (lane == 0) f = first_join(pp, cnt, backward, s);
-            fin = __shfl_sync(full, f, 0);
-        }
         for (int part = 0; part < 2; ++part) {
-            const int np_all = part == 0 ? n1 : (fin > 0 ? fin : 0);
+            const int np_all = part == 0 ? n1 : (closed && fin > 0 ? fin : 0);
             for (int p0 = 0; p0 < np_all; p0 += 32) {
                 const int np = min(32, np_all - p0);
                 const int pos = p0 + lane;
@@ -355,6 +405,7 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, walk_o
                 if (synced && __all_sync(full, ok)) {
                     acc = __ballot_sync(full, point_lane && !is_start);
                 } else {
+                    // lane 0 replays the acceptance from the last accepted point
                     unsigned m = 0;
                     if (lane == 0) {
                         float2 pt = point;
@@ -370,12 +421,12 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, walk_o
                     }
                     acc = __shfl_sync(full, m, 0);
                 }
-                if (WRITE && lane == 0) {
+                if (lane == 0) {
                     walk_chunk h;
-                    h.pts = ubase;
+                    h.pts = pc.pts;
                     h.cnt = cnt;
                     h.flags = (backward ? 1 : 0) | (closed ? 2 : 0) | (part == 1 ? 4 : 0);
-                    h.style = gr.style;
+                    h.style = pc.style;
                     h.acc = acc;
                     h.c1 = c1;
                     h.c2 = c2;
@@ -384,7 +435,7 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, walk_o
                     h.poly0 = cb + poly0;
                     h.poly1 = cb + poly1;
                     h.pad = 0;
-                    wo.chunks[cb + nch] = h;
+                    chunks[cb + nch] = h;
                 }
                 ++nch;
                 if (acc) {
@@ -400,44 +451,24 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, walk_o
             }
         }
     };
-    // chunks of a walk: used to place polygons before the walks run
-    auto walk_chunks = [&](const float2 *pp, int cnt, bool closed, bool backward) {
-        int n1 = closed ? cnt : cnt + 1, fin = 0;
-        if (closed) {
-            int f = 0;
-            if (lane == 0) f = first_join(pp, cnt, backward, s);
-            fin = max(__shfl_sync(full, f, 0), 0);
+    int ff = -1, fb = -1;
+    if (closed) {
+        int a = 0, b = 0;
+        if (lane == 0) {
+            a = first_join(pp, cnt, false, s);
+            b = first_join(pp, cnt, true, s);
         }
-        return (n1 + 31) / 32 + (fin + 31) / 32;
-    };
-    auto piece = [&](int32_t ubase, int cnt, bool closed) {
-        if (cnt < 2) return;
-        const float2 *pp = piece_points(in, ubase);
-        const int start = nch;
-        const int nf = walk_chunks(pp, cnt, closed, false);
-        const int nb = walk_chunks(pp, cnt, closed, true);
-        if (closed) {
-            walk(ubase, pp, cnt, true, false, start, start + nf);
-            walk(ubase, pp, cnt, true, true, start + nf, start + nf + nb);
-        } else {
-            walk(ubase, pp, cnt, false, false, start, start + nf + nb);
-            walk(ubase, pp, cnt, false, true, start, start + nf + nb);
-        }
-    };
-    if (s.dash_n > 0) {
-        const int d0 = in.dash_off[g];
-        const int ns = in.dash_nsub[g];
-        int q = 0;
-        for (int k = 0; k < ns; ++k) {
-            int2 sub = in.dash_subs[d0 + k];
-            piece(in.nflat + d0 + q, sub.x, sub.y != 0);
-            q += sub.x;
-        }
-    } else {
-        const int a = in.item_off[gr.head], b = in.item_off[gr.end];
-        piece(a, b - a, gr.closed != 0);
+        ff = __shfl_sync(full, a, 0);
+        fb = __shfl_sync(full, b, 0);
     }
-    if (!WRITE && lane == 0) wo.chunk_count[g] = nch;
+    const int nf = walk_chunk_count(cnt, closed, ff), nb = walk_chunk_count(cnt, closed, fb);
+    if (closed) {
+        walk(false, ff, 0, nf);
+        walk(true, fb, nf, nf + nb);
+    } else {
+        walk(false, ff, 0, nf + nb);
+        walk(true, fb, 0, nf + nb);
+    }
 }
 
 // k_join: one warp per chunk.  EMIT=false writes each position's point
@@ -511,11 +542,12 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_join(stroke_in in, const 
     }
 }
 
-// Output range of each group: goff[g] = coff[chunk_base[g]] (g <= n).
-__global__ void k_group_off(const int32_t *__restrict__ chunk_base, const int64_t *__restrict__ coff, int n,
-                            int64_t *__restrict__ goff) {
+// Output range of each group: goff[g] = coff of its first piece's first
+// chunk (g <= n).
+__global__ void k_group_off(const int32_t *__restrict__ piece_base, const int32_t *__restrict__ chunk_base,
+                            const int64_t *__restrict__ coff, int n, int64_t *__restrict__ goff) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g <= n) goff[g] = coff[chunk_base[g]];
+    if (g <= n) goff[g] = coff[chunk_base[piece_base[g]]];
 }
 
 }  // namespace cyg

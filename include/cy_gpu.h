@@ -82,8 +82,9 @@ void cy_ctx_destroy(cy_ctx *ctx);
 int cy_fill_path(cy_ctx *ctx, const float *points, const int *subpath_counts, int n_subpaths,
                  const cy_paint *paint, const cy_draw_state *state);
 
-/* render_main on ready polylines (hpp:2551-2605): strokes after host stroke
- * expansion, rectangles, images and text.  Every subpath is implicitly
+/* render_main on ready polylines (hpp:2551-2605): strokes expanded on the
+ * host (stroke_rectangle, stroke_text, or cy_set_device_stroke(0)),
+ * rectangles, images and text.  Every subpath is implicitly
  * closed, as in lines_to_runs (hpp:2193-2253). */
 int cy_fill_lines(cy_ctx *ctx, const float *points, const int *subpath_counts, int n_subpaths,
                   const cy_paint *paint, const cy_draw_state *state);
