@@ -349,7 +349,7 @@ struct frame {
     dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
     dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, st_err, pc_cnt, pc_base, pc_list, wk_cnt, wk_base,
-        wk_chunks, jn_cnt, jn_sum, jn_off, st_goff;
+        wk_chunks, jn_cnt, jn_alpha, jn_sum, jn_off, st_goff;
     hbuf staging, offs_host, rowoff_host, get_host, stoff_host;
     char *d = nullptr;
     size_t o_cmd = 0, o_hpts = 0, o_hprev = 0, o_bez = 0, o_items = 0, o_soff = 0, o_scol = 0, o_tex = 0, o_put = 0;
@@ -424,7 +424,7 @@ struct frame {
                      &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev, &dash_cnt, &dash_off, &dash_pts,
                      &dash_subs, &dash_nsub, &st_err, &pc_cnt, &pc_base, &pc_list, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt,
-                     &jn_sum, &jn_off, &st_goff};
+                     &jn_alpha, &jn_sum, &jn_off, &st_goff};
         for (dbuf *x : b) x->release();
         staging.release();
         stoff_host.release();
@@ -778,7 +778,8 @@ int frame::stroke_passes(bool sizing) {
         n_chunks = hb[0];
         if (n_chunks < 0 || n_chunks > (static_cast<int64_t>(1) << 26)) return fail(CY_ENOMEM, __LINE__);
         size_t nc = static_cast<size_t>(n_chunks) + 1;
-        if (!wk_chunks.ensure(nc * sizeof(walk_chunk)) || !jn_cnt.ensure(nc * 32 * 4) || !jn_sum.ensure(nc * 4) ||
+        if (!wk_chunks.ensure(nc * sizeof(walk_chunk)) || !jn_cnt.ensure(nc * 32 * 4) ||
+            !jn_alpha.ensure(nc * 32 * 4) || !jn_sum.ensure(nc * 4) ||
             !jn_off.ensure(nc * 8))
             return fail(CY_ENOMEM, __LINE__);
     }
@@ -787,7 +788,8 @@ int frame::stroke_passes(bool sizing) {
     const int nch = static_cast<int>(n_chunks);
     const int jgrid = std::max(1, (nch + kStrokeWarps - 1) / kStrokeWarps);
     k_join<false><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(), nch,
-                                                           jn_cnt.as<int32_t>(), jn_sum.as<int32_t>(), nullptr,
+                                                           jn_cnt.as<int32_t>(), jn_alpha.as<float>(),
+                                                           jn_sum.as<int32_t>(), nullptr,
                                                            nullptr, nullptr, 0, 0);
     if (!ok(cudaMemsetAsync(jn_sum.as<int32_t>() + nch, 0, 4, stream))) return status;
     if (int rc = scan64(jn_sum.as<int32_t>(), jn_off.as<int64_t>(), nch + 1)) return rc;
@@ -811,7 +813,8 @@ int frame::stroke_passes(bool sizing) {
         return ok(cudaGetLastError()) ? CY_OK : status;
     }
     k_join<true><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(), nch,
-                                                          jn_cnt.as<int32_t>(), nullptr, jn_off.as<int64_t>(),
+                                                          jn_cnt.as<int32_t>(), jn_alpha.as<float>(), nullptr,
+                                                          jn_off.as<int64_t>(),
                                                           flat_pts.as<float2>() + nflat, flat_prev.as<int32_t>() + nflat,
                                                           static_cast<int32_t>(nflat), n_outline);
     ++launches;

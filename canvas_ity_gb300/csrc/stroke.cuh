@@ -29,12 +29,21 @@ __device__ __forceinline__ float2 xform(const float *m, float2 p) {
 __device__ __forceinline__ float len2(float2 a) { return sqrtf(dot2(a, a)); }
 __device__ __forceinline__ float2 unit2(float2 a) { return scl2(1.0f / hi(1.0e-6f, len2(a)), a); }
 
+// A round join's or round cap's curve, flattened in fill mode: one copy of
+// the flattening code for all call sites of a kernel.
+template <bool EMIT>
+__device__ __noinline__ int curve_points(float2 a, float2 b, float2 c, float2 d, float2 *out, int cap) {
+    return flatten_cubic<EMIT>(a, b, c, d, -1.0f, out, cap);
+}
+
 // One join of add_half_stroke (hpp:1966-2041) at `point` between the
 // accepted segments in_dir/in_len and out_dir/out_len (user space).  Returns
-// the number of device-space points it adds.
+// the number of device-space points it adds.  A round join's factor
+// 4/3 tan(angle / 4) is computed when counting (EMIT=false) and stored in
+// `alpha`; writing (EMIT=true) takes it from there.
 template <bool EMIT>
 __device__ int stroke_join(float2 point, float2 in_dir, float in_len, float2 out_dir, float out_len,
-                           const stroke_style &s, float2 *out, int cap) {
+                           const stroke_style &s, float2 *out, int cap, float &alpha) {
     const float half = s.half;
     const float eps = 1.0e-4f;
     int n = 0;
@@ -62,13 +71,15 @@ __device__ int stroke_join(float2 point, float2 in_dir, float in_len, float2 out
     if ((turn > 0.0f && !tight) || (turn != 0.0f && s.join == 0 && dot2(offset, offset) <= s.ratio)) {
         put(add2(point, offset));
     } else if (s.join == 2) {
-        float cosine = dot2(in_dir, out_dir);
-        float angle = static_cast<float>(acos(static_cast<double>(lo(hi(cosine, -1.0f), 1.0f))));
-        float alpha = 4.0f / 3.0f * static_cast<float>(tan(static_cast<double>(0.25f * angle)));
+        if (!EMIT) {
+            float cosine = dot2(in_dir, out_dir);
+            float angle = static_cast<float>(acos(static_cast<double>(lo(hi(cosine, -1.0f), 1.0f))));
+            alpha = 4.0f / 3.0f * static_cast<float>(tan(static_cast<double>(0.25f * angle)));
+        }
         put(side_in);
-        n += flatten_cubic<EMIT>(xform(s.fwd, side_in), xform(s.fwd, add2(side_in, scl2(alpha * half, in_dir))),
-                                 xform(s.fwd, sub2(side_out, scl2(alpha * half, out_dir))), xform(s.fwd, side_out),
-                                 -1.0f, out + (EMIT ? n : 0), cap - n);
+        n += curve_points<EMIT>(xform(s.fwd, side_in), xform(s.fwd, add2(side_in, scl2(alpha * half, in_dir))),
+                                xform(s.fwd, sub2(side_out, scl2(alpha * half, out_dir))), xform(s.fwd, side_out),
+                                out + (EMIT ? n : 0), cap - n);
     } else {
         put(side_in);
         put(side_out);
@@ -100,12 +111,12 @@ __device__ int stroke_cap(float2 point, float2 in_dir, const stroke_style &s, fl
     } else if (s.cap == 2) {
         const float k = 0.55228475f;   // 4/3 tan(pi/8)
         put(add2(point, side));
-        n += flatten_cubic<EMIT>(xform(s.fwd, add2(point, side)), xform(s.fwd, add2(add2(point, side), scl2(k, ahead))),
-                                 xform(s.fwd, add2(add2(point, ahead), scl2(k, side))), xform(s.fwd, add2(point, ahead)),
-                                 -1.0f, out + (EMIT ? n : 0), cap - n);
-        n += flatten_cubic<EMIT>(xform(s.fwd, add2(point, ahead)), xform(s.fwd, sub2(add2(point, ahead), scl2(k, side))),
-                                 xform(s.fwd, add2(sub2(point, side), scl2(k, ahead))), xform(s.fwd, sub2(point, side)),
-                                 -1.0f, out + (EMIT ? n : 0), cap - n);
+        n += curve_points<EMIT>(xform(s.fwd, add2(point, side)), xform(s.fwd, add2(add2(point, side), scl2(k, ahead))),
+                                xform(s.fwd, add2(add2(point, ahead), scl2(k, side))), xform(s.fwd, add2(point, ahead)),
+                                out + (EMIT ? n : 0), cap - n);
+        n += curve_points<EMIT>(xform(s.fwd, add2(point, ahead)), xform(s.fwd, sub2(add2(point, ahead), scl2(k, side))),
+                                xform(s.fwd, add2(sub2(point, side), scl2(k, ahead))), xform(s.fwd, sub2(point, side)),
+                                out + (EMIT ? n : 0), cap - n);
     }
     return n;
 }
@@ -141,6 +152,8 @@ __device__ __forceinline__ int warp_sum(int v) {
 template <bool EMIT>
 __global__ void __launch_bounds__(kStrokeWarps * 32) k_dash(stroke_in in, int32_t *__restrict__ counts) {
     __shared__ float lens[kStrokeWarps][32];
+    __shared__ float2 ends[kStrokeWarps][33];   // the chunk's points (segment ends)
+    __shared__ float pat[kStrokeWarps][64];     // the pattern, when it has at most 64 entries
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int g = blockIdx.x * kStrokeWarps + w;
     if (g >= in.n) return;
@@ -151,6 +164,11 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_dash(stroke_in in, int32_
         return;
     }
     const float *dash = in.dash + s.dash_first;
+    if (s.dash_n <= 64) {
+        for (int i = lane; i < s.dash_n; i += 32) pat[w][i] = dash[i];
+        __syncwarp();
+        dash = pat[w];
+    }
     const int a = in.item_off[gr.head], n = in.item_off[gr.end] - a;
     const float2 *pts = in.flat + a;
     int o = 0, cap = 0;
@@ -175,13 +193,15 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_dash(stroke_in in, int32_
     for (int c = 0; c + 1 < n; c += 32) {
         int i = c + lane;
         float line = 0.0f;
+        if (i < n) ends[w][lane] = pts[i];
+        if (lane == 0 && c + 32 < n) ends[w][32] = pts[c + 32];
         if (i + 1 < n) line = len2(sub2(xform(s.inv, pts[i + 1]), xform(s.inv, pts[i])));
         lens[w][lane] = line;
         __syncwarp();
         if (lane == 0 && !over) {
             int m = min(32, n - 1 - c);
             for (int k = 0; k < m; ++k) {
-                float2 from = pts[c + k], to = pts[c + k + 1];
+                float2 from = ends[w][k], to = ends[w][k + 1];
                 float len = lens[w][k];
                 if (emit) {
                     if (EMIT && np < cap) out[np] = from;
@@ -472,13 +492,15 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, const 
 }
 
 // k_join: one warp per chunk.  EMIT=false writes each position's point
-// count to jcnt[32 * chunk + lane] and each chunk's total to csum[chunk];
+// count to jcnt[32 * chunk + lane] (and a round join's factor to
+// jalpha[32 * chunk + lane]) and each chunk's total to csum[chunk];
 // EMIT=true writes the joins (and caps) at coff[chunk] + the counts of the
 // lanes before, with prev links: the point before, except for a polygon's
 // first point, linked to the polygon's last.
 template <bool EMIT>
 __global__ void __launch_bounds__(kStrokeWarps * 32) k_join(stroke_in in, const walk_chunk *__restrict__ chunks,
                                                             int n_chunks, int32_t *__restrict__ jcnt,
+                                                            float *__restrict__ jalpha,
                                                             int32_t *__restrict__ csum, const int64_t *__restrict__ coff,
                                                             float2 *__restrict__ out, int32_t *__restrict__ prev,
                                                             int32_t base, int64_t cap) {
@@ -512,9 +534,11 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_join(stroke_in in, const 
     }
     if (join) dout = sub2(xform(s.inv, pp[walk_index(pos, cnt, backward)]), jp);
     int n = 0;
+    float alpha = 0.0f;
     if (!EMIT) {
-        if (join) n = stroke_join<false>(jp, unit2(din), len2(din), unit2(dout), len2(dout), s, nullptr, 0);
+        if (join) n = stroke_join<false>(jp, unit2(din), len2(din), unit2(dout), len2(dout), s, nullptr, 0, alpha);
         else if (capped) n = stroke_cap<false>(jp, unit2(din), s, nullptr, 0);
+        jalpha[32LL * c + lane] = alpha;
         if (n > (1 << 24)) {   // a join or cap far beyond any canvas (line width ~1e11)
             atomicOr(in.error, 1);
             n = 0;
@@ -533,7 +557,8 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_join(stroke_in in, const 
     }
     const int64_t at = coff[c] + incl - n;
     if (n == 0 || at < 0 || at + n > cap) return;
-    if (join) stroke_join<true>(jp, unit2(din), len2(din), unit2(dout), len2(dout), s, out + at, n);
+    alpha = jalpha[32LL * c + lane];
+    if (join) stroke_join<true>(jp, unit2(din), len2(din), unit2(dout), len2(dout), s, out + at, n, alpha);
     else stroke_cap<true>(jp, unit2(din), s, out + at, n);
     const int64_t first = coff[h.poly0], last = coff[h.poly1] - 1;
     for (int k = 0; k < n; ++k) {
