@@ -1,7 +1,12 @@
 // capi.cpp -- flat C binding of canvas_ity::canvas and the call-list replay
 // entry point (include/canvas_ity_c.h).
+#include <cuda_runtime.h>
+
 #include <atomic>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <mutex>
 #include <memory>
 #include <new>
 #include <thread>
@@ -233,6 +238,147 @@ int cy_canvases_from_traces(const void *const *traces, const size_t *lens, int n
         }
     }
     return rc;
+}
+
+int cy_render_traces(const void *const *traces, const size_t *lens, int n, int engine, long long frame_pixels,
+                     unsigned char *out, const size_t *offsets, long long *stats) {
+    if (n < 0 || (n > 0 && (!traces || !lens || !offsets || (!out && offsets[n] > 0)))) return CY_EINVAL;
+    if (stats) stats[0] = stats[1] = stats[2] = 0;
+    if (n == 0) return CY_OK;
+    if (frame_pixels <= 0) frame_pixels = 64LL << 20;
+    // frames: consecutive call lists up to frame_pixels canvas pixels
+    std::vector<int> starts;
+    long long acc = 0;
+    for (int i = 0; i < n; ++i) {
+        int w = 0, h = 0;
+        if (lens[i] >= 20) {
+            std::memcpy(&w, static_cast<const unsigned char *>(traces[i]) + 12, 4);
+            std::memcpy(&h, static_cast<const unsigned char *>(traces[i]) + 16, 4);
+        }
+        long long px = static_cast<long long>(w > 0 ? w : 0) * (h > 0 ? h : 0);
+        if (starts.empty() || (acc > 0 && acc + px > frame_pixels)) {
+            starts.push_back(i);
+            acc = 0;
+        }
+        acc += px;
+    }
+    starts.push_back(n);
+    struct job { cy_frame *f = nullptr; std::vector<cy_canvas *> cv; int first = 0; };
+    const int nf = static_cast<int>(starts.size()) - 1;
+    std::vector<job> slots(static_cast<size_t>(nf));
+    std::vector<char> ready(static_cast<size_t>(nf), 0);
+    std::mutex m;
+    std::condition_variable cv_ready, cv_space;
+    int taken = 0, inflight = 0;
+    bool producers_done = false;
+    const int max_inflight = 3;
+    std::atomic<int> failure(0);
+    std::atomic<long long> up(0), down(0);
+    auto fail = [&](int rc) { int none = 0; failure.compare_exchange_strong(none, rc); };
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return CY_ENODEV;
+    }
+    // Producers (two): replay a frame's call lists and create the frame,
+    // which uploads it and queues its first run.  While one waits for its
+    // frame's size read-backs, the other replays the next frame.
+    auto produce = [&]() {
+        cudaSetDevice(dev);
+        for (;;) {
+            int fi;
+            {
+                std::unique_lock<std::mutex> hold(m);
+                cv_space.wait(hold, [&] { return inflight < max_inflight || failure.load() != 0; });
+                if (failure.load() != 0 || taken >= nf) return;
+                fi = taken++;
+                ++inflight;
+            }
+            job j;
+            j.first = starts[fi];
+            const int k = starts[fi + 1] - j.first;
+            j.cv.assign(static_cast<size_t>(k), nullptr);
+            int rc = cy_canvases_from_traces(traces + j.first, lens + j.first, k, engine, 0, j.cv.data());
+            if (rc == CY_OK) {
+                std::vector<cy_ctx *> ctx(static_cast<size_t>(k));
+                for (int i = 0; i < k; ++i) ctx[i] = static_cast<cy_ctx *>(cy_canvas_ctx(j.cv[i]));
+                rc = cy_frame_create(ctx.data(), k, engine, &j.f);
+                if (rc == CY_OK) {
+                    long long st[10] = {};
+                    if (cy_frame_stats(j.f, st, 10) >= 10) up += st[9];
+                }
+            }
+            if (rc) fail(rc);
+            {
+                std::lock_guard<std::mutex> hold(m);
+                slots[fi] = std::move(j);
+                ready[fi] = 1;
+            }
+            cv_ready.notify_all();
+        }
+    };
+    // Finisher: frames in order; waits for each, copies its reads out and
+    // frees it.
+    std::thread finisher([&]() {
+        cudaSetDevice(dev);
+        for (int fi = 0; fi < nf; ++fi) {
+            job j;
+            {
+                std::unique_lock<std::mutex> hold(m);
+                cv_ready.wait(hold, [&] { return ready[fi] || (producers_done && fi >= taken); });
+                if (!ready[fi]) return;
+                j = std::move(slots[fi]);
+            }
+            const int k = static_cast<int>(j.cv.size());
+            if (j.f && failure.load() == 0) {
+                std::vector<size_t> offs(static_cast<size_t>(k) + 1);
+                const unsigned char *data = nullptr;
+                int rc = cy_frame_finish_views(j.f, &data, offs.data());
+                if (rc) fail(rc);
+                for (int i = 0; rc == 0 && i < k; ++i)
+                    if (offs[i + 1] - offs[i] != offsets[j.first + i + 1] - offsets[j.first + i]) {
+                        fail(CY_EINVAL);
+                        rc = CY_EINVAL;
+                    }
+                if (rc == 0) {
+                    down += static_cast<long long>(offs[k]);
+                    // copy out on a few threads
+                    const int t = std::max(1, std::min(8, k));
+                    std::vector<std::thread> pool;
+                    for (int a = 0; a < t; ++a)
+                        pool.emplace_back([&, a]() {
+                            for (int i = a; i < k; i += t) {
+                                size_t len = offs[i + 1] - offs[i];
+                                if (len) std::memcpy(out + offsets[j.first + i], data + offs[i], len);
+                            }
+                        });
+                    for (std::thread &th : pool) th.join();
+                }
+            }
+            if (j.f) cy_frame_destroy(j.f);
+            for (cy_canvas *c : j.cv) delete c;
+            {
+                std::lock_guard<std::mutex> hold(m);
+                --inflight;
+            }
+            cv_space.notify_all();
+        }
+    });
+    std::thread second(produce);
+    produce();
+    second.join();
+    {
+        std::lock_guard<std::mutex> hold(m);
+        producers_done = true;
+    }
+    cv_ready.notify_all();
+    finisher.join();
+    if (stats) {
+        stats[0] = nf;
+        stats[1] = up.load();
+        stats[2] = down.load();
+    }
+    return failure.load();
 }
 
 }  // extern "C"

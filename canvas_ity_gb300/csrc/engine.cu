@@ -317,6 +317,8 @@ struct frame {
     queue all;                 // commands and reads of all contexts (geometry stays in their queues)
     struct ctx_base { int32_t hpts, bez, items, stop, tex, groups, styles, dash; int64_t put; };
     std::vector<ctx_base> bases;   // where each context's geometry lands in the arena
+    std::vector<int64_t> get_base; // where each context's reads start in the read-back buffer
+    bool keep_reads = false;       // finish leaves deferred reads in get_host
     int64_t n_hpts = 0, n_bez = 0, n_items_all = 0, n_stop = 0, n_tex = 0, n_put = 0;
     int64_t n_groups = 0, n_styles = 0, n_dash = 0;
     // Device stroke expansion: flattened centre lines occupy flat_pts[0,
@@ -390,6 +392,8 @@ struct frame {
         cvs.clear();
         all.clear();
         bases.clear();
+        get_base.clear();
+        keep_reads = false;
         n_hpts = n_bez = n_items_all = n_stop = n_tex = n_put = 0;
         n_groups = n_styles = n_dash = 0;
         nflat = n_outline = n_dashed = n_pieces = n_chunks = 0;
@@ -627,6 +631,7 @@ void frame::gather() {
         }
         all.get_dst.insert(all.get_dst.end(), q.get_dst.begin(), q.get_dst.end());
         all.get_stride.insert(all.get_stride.end(), q.get_stride.begin(), q.get_stride.end());
+        get_base.push_back(get_total);
         get_total += q.get_bytes;
     }
 }
@@ -1439,7 +1444,7 @@ int frame::finish() {
                 for (int row = 0; row < c.get_h; ++row)
                     std::memcpy(dst + static_cast<ptrdiff_t>(row) * stride,
                                 src + static_cast<size_t>(row) * c.get_w * 4, static_cast<size_t>(c.get_w) * 4);
-            } else {
+            } else if (!keep_reads) {
                 cv->deferred_out.insert(cv->deferred_out.end(), src,
                                         src + static_cast<size_t>(c.get_w) * c.get_h * 4);
             }
@@ -2049,8 +2054,7 @@ int cy_get_image(cy_ctx *c, unsigned char *image, int w, int h, int stride, int 
     cmd.kind = CMD_GET;
     cmd.get_x = x; cmd.get_y = y; cmd.get_w = w; cmd.get_h = h;
     cmd.get_out = q.get_bytes;
-    q.get_bytes += static_cast<int64_t>(w) * h * 4;
-    q.get_bytes = (q.get_bytes + 15) & ~static_cast<int64_t>(15);
+    q.get_bytes += static_cast<int64_t>(w) * h * 4;   // packed: a context's reads are one range
     q.cmds.push_back(cmd);
     q.mask_ids.push_back(0);
     q.mask_ids.push_back(0);
@@ -2343,6 +2347,20 @@ int cy_frame_capture(cy_frame *fr) {
 }
 
 int cy_frame_finish(cy_frame *fr) { return fr ? fr->f->finish() : CY_EINVAL; }
+
+int cy_frame_finish_views(cy_frame *fr, const unsigned char **data, size_t *offsets) {
+    if (!fr || !data || !offsets) return CY_EINVAL;
+    frame &f = *fr->f;
+    f.keep_reads = true;
+    int rc = f.finish();
+    f.keep_reads = false;
+    if (rc) return rc;
+    size_t n = f.cvs.size();
+    for (size_t i = 0; i < n; ++i) offsets[i] = static_cast<size_t>(f.get_base[i]);
+    offsets[n] = static_cast<size_t>(f.get_total);
+    *data = static_cast<const unsigned char *>(f.get_host.p);
+    return CY_OK;
+}
 
 int cy_frame_sync(cy_frame *fr) {
     if (!fr) return CY_EINVAL;

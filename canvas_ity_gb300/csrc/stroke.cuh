@@ -4,12 +4,14 @@
 // the stroking angle limit (path_to_lines, hpp:1495-1524), split by the dash
 // pattern (dash_lines, hpp:1858-1934) and traced forwards and backwards to
 // add the two half strokes with their joins and caps (add_half_stroke,
-// stroke_lines, hpp:1949-2100).  Every step is sequential along a subpath
-// (the dash phase and the last accepted point are carried from segment to
-// segment), so one thread expands one subpath of the flattened path, once
-// to count its output and once to write it at its scanned offset.  The float
-// operations are the reference's, in its order; the one exception is the
-// round join's acosf/tanf, taken in double precision and rounded to float.
+// stroke_lines, hpp:1949-2100).  The dash phase is a float running sum
+// carried along a subpath (one warp per subpath, lane 0 carries it); the
+// walk's point acceptance is resolved 32 positions at a time (one warp per
+// piece), after which every join and cap is independent and computed by one
+// warp per 32 walk positions over all canvases at once.  Each pass counts,
+// scans, then writes.  The float operations are the reference's, in its
+// order; the one exception is the round join's acosf/tanf, taken in double
+// precision and rounded to float.
 #ifndef CY_STROKE_CUH
 #define CY_STROKE_CUH
 

@@ -212,7 +212,7 @@ class Frame:
         n = self.lib.cy_frame_stats(self.frame, arr, len(self.STAT_NAMES))
         return {k: int(arr[i]) for i, k in enumerate(self.STAT_NAMES[:n])}
 
-    PHASES = ("flatten", "scan_convert", "masks_shadows", "paint")
+    PHASES = ("flatten_stroke", "scan_convert", "masks_shadows", "paint")
 
     def set_profiling(self, on: bool) -> None:
         self.lib.cy_frame_set_profiling(self.frame, 1 if on else 0)
@@ -223,8 +223,11 @@ class Frame:
         return {self.PHASES[i]: float(arr[i]) for i in range(min(n, len(self.PHASES)))}
 
     def finish(self, copy: bool = True) -> list:
-        """Copy the reads back; returns each canvas's get_image_data bytes
-        (memoryviews into one buffer when copy=False)."""
+        """Copy the reads back; returns each canvas's get_image_data bytes.
+        With copy=False they are memoryviews into the frame's pinned
+        read-back buffer (no host copy), valid until the frame is closed."""
+        if not copy:
+            return self._finish_views()
         t0 = time.perf_counter()
         rc = self.lib.cy_frame_finish(self.frame)
         if rc != 0:
@@ -249,6 +252,25 @@ class Frame:
         self.timing["reads_s"] = time.perf_counter() - t1
         return out
 
+    def _finish_views(self) -> list:
+        t0 = time.perf_counter()
+        n = len(self.ctxs)
+        offs = (ctypes.c_size_t * (n + 1))()
+        data = ctypes.c_void_p()
+        self.lib.cy_frame_finish_views.restype = ctypes.c_int
+        self.lib.cy_frame_finish_views.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                                                   ctypes.POINTER(ctypes.c_size_t)]
+        rc = self.lib.cy_frame_finish_views(self.frame, ctypes.byref(data), offs)
+        if rc != 0:
+            raise RuntimeError(f"cy_frame_finish_views failed with status {rc}")
+        t1 = time.perf_counter()
+        total = offs[n]
+        mv = memoryview((ctypes.c_ubyte * total).from_address(data.value)).cast("B") if total else memoryview(b"")
+        out = [mv[offs[i]:offs[i + 1]] for i in range(n)]
+        self.timing["finish_s"] = t1 - t0
+        self.timing["reads_s"] = time.perf_counter() - t1
+        return out
+
     def close(self) -> None:
         if self.frame:
             self.lib.cy_frame_destroy(self.frame)
@@ -262,6 +284,38 @@ class Frame:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def render_traces(traces, engine: int = 0, frame_pixels: int = 0, out=None, offsets=None):
+    """End to end through cy_render_traces: call lists in host memory to
+    RGBA8 reads in host memory, frames pipelined (host work of one frame
+    under the device work of the previous).  `out` (a writable buffer) and
+    `offsets` (n + 1 entries) can be given to reuse them; returns
+    (per-canvas memoryviews into out, stats dict)."""
+    from . import trace as T
+    lib = _batch_lib()
+    lib.cy_render_traces.restype = ctypes.c_int
+    lib.cy_render_traces.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
+    n = len(traces)
+    if offsets is None:
+        offsets = np.zeros(n + 1, np.uint64)
+        offsets[1:] = np.cumsum([T.read_bytes(t) for t in traces], dtype=np.uint64)
+    total = int(offsets[n])
+    if out is None:
+        out = np.zeros(max(total, 1), np.uint8)
+    bufs = (ctypes.c_void_p * n)(*[ctypes.cast(ctypes.c_char_p(t), ctypes.c_void_p).value for t in traces])
+    lens = (ctypes.c_size_t * n)(*[len(t) for t in traces])
+    offs = np.ascontiguousarray(offsets, np.uint64)
+    stats = (ctypes.c_longlong * 3)()
+    out_arr = np.frombuffer(out, np.uint8)
+    rc = lib.cy_render_traces(bufs, lens, n, int(engine), int(frame_pixels), out_arr.ctypes.data,
+                              offs.ctypes.data, stats)
+    if rc != 0:
+        raise RuntimeError(f"cy_render_traces failed with status {rc}")
+    mv = memoryview(out_arr)
+    views = [mv[int(offs[i]):int(offs[i + 1])] for i in range(n)]
+    return views, {"frames": stats[0], "upload_bytes": stats[1], "read_bytes": stats[2]}
 
 
 def render_batch(traces, engine: int = 0) -> List[bytes]:

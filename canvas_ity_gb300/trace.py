@@ -252,6 +252,18 @@ def _read(buf: bytes, at: int, fmt: str):
     return struct.unpack_from("<" + fmt, buf, at), at + size
 
 
+def read_bytes(buf: bytes) -> int:
+    """Bytes a replay of this call list reads back: its non-null
+    get_image_data calls, compact RGBA8."""
+    total = 0
+    for r in parse(buf).records:
+        if r.op == GET_IMAGE_DATA:
+            w, h, nonnull = r.args[0], r.args[1], r.args[4]
+            if nonnull and w > 0 and h > 0:
+                total += w * h * 4
+    return total
+
+
 def parse(buf: bytes) -> Trace:
     """Parse a trace (raw, or zlib-compressed as stored in fixtures)."""
     if buf[:2] in (b"\x78\x9c", b"\x78\xda", b"\x78\x01"):

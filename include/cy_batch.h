@@ -99,6 +99,26 @@ int cy_canvases_from_traces(const void *const *traces, const size_t *lens, int n
  * contexts' reads are consumed, as by cy_ctx_take_reads. */
 int cy_frame_collect(cy_frame *frame, unsigned char *out, size_t cap, size_t *offsets);
 
+/* cy_frame_finish without moving the reads: the frame keeps them in its
+ * pinned host buffer, which the device->host copy fills directly.  *data
+ * receives that buffer and offsets[0..n] where each context's reads start
+ * and their end (each context's reads in call order, compact RGBA8).  The
+ * bytes stay valid until the frame runs again or is destroyed; the
+ * contexts' own deferred reads stay empty. */
+int cy_frame_finish_views(cy_frame *frame, const unsigned char **data, size_t *offsets);
+
+/* End to end over many call lists: replay on the host, upload, render and
+ * read back, in frames of about `frame_pixels` canvas pixels (0: 64 Mi).
+ * While the device renders one frame, the host replays and stages the
+ * next, and copies out the one before.  Canvas i's reads (compact RGBA8
+ * rectangles in call order) are written to out[offsets[i] .. offsets[i+1]);
+ * the caller knows them from its get_image_data calls, and a canvas whose
+ * reads do not fill its range exactly fails the call with CY_EINVAL.
+ * stats (may be NULL) receives [0] frames, [1] bytes uploaded, [2] bytes
+ * read back. */
+int cy_render_traces(const void *const *traces, const size_t *lens, int n, int engine, long long frame_pixels,
+                     unsigned char *out, const size_t *offsets, long long *stats);
+
 /* Deferred reads of a context, concatenated in call order (compact RGBA8
  * rectangles); -2 if cap is too small (*len holds the size). */
 int cy_ctx_take_reads(cy_ctx *ctx, unsigned char *out, size_t cap, size_t *len);

@@ -288,3 +288,39 @@ def test_tile_engine_strip_sizes(strip_pixels):
             assert_images_close(got, want, f"strip {strip_pixels}")
     finally:
         native.set_strip_config(4096, 256)
+
+
+def test_frame_views_match_copies():
+    """cy_frame_finish_views hands out the pinned read-back buffer itself;
+    its per-canvas ranges hold the same bytes as the copying collection."""
+    traces = [scenes.small_scene(cfg, 9) for cfg in ("c0_small", "c1_small", "c2_small", "mixed_small")]
+    traces += [scenes.c3_canvas(70 + s) for s in range(3)]
+    want = native.render_batch(traces, 0)
+    with native.Frame(traces, 0) as f:
+        views = f.finish(copy=False)
+        got = [bytes(v) for v in views]
+    assert got == want
+
+
+@pytest.mark.parametrize("frame_pixels", [0, 60000])
+def test_render_traces_pipelined_matches_frames(frame_pixels):
+    """cy_render_traces (frames pipelined: host replay of one under the
+    device work of the previous) writes every canvas's reads where the
+    caller's offsets say, equal to the single-frame path; small frames
+    force many frames in flight."""
+    traces = [scenes.c3_canvas(80 + s) for s in range(6)]
+    traces += [scenes.small_scene(cfg, 4) for cfg in ("c0_small", "c1_small", "c2_small", "mixed_small")]
+    want = native.render_batch(traces, 0)
+    views, stats = native.render_traces(traces, 0, frame_pixels)
+    assert [bytes(v) for v in views] == want
+    assert stats["read_bytes"] == sum(len(w) for w in want)
+    if frame_pixels:
+        assert stats["frames"] > 1
+
+
+def test_render_traces_rejects_wrong_sizes():
+    traces = [scenes.small_scene("c0_small", 1), scenes.small_scene("c1_small", 1)]
+    sizes = [T.read_bytes(t) for t in traces]
+    offsets = np.array([0, sizes[0] + 4, sizes[0] + sizes[1] + 4], np.uint64)
+    with pytest.raises(RuntimeError, match="status -1"):
+        native.render_traces(traces, 0, 0, np.zeros(int(offsets[-1]), np.uint8), offsets)
