@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -264,6 +267,11 @@ int cy_render_traces(const void *const *traces, const size_t *lens, int n, int e
     }
     starts.push_back(n);
     struct job { cy_frame *f = nullptr; std::vector<cy_canvas *> cv; int first = 0; };
+    // CY_DEBUG: per-frame host timings on stderr
+    const bool trace_timing = std::getenv("CY_DEBUG") != nullptr;
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+        return std::chrono::duration<double, std::milli>(b - a).count();
+    };
     const int nf = static_cast<int>(starts.size()) - 1;
     std::vector<job> slots(static_cast<size_t>(nf));
     std::vector<char> ready(static_cast<size_t>(nf), 0);
@@ -298,11 +306,16 @@ int cy_render_traces(const void *const *traces, const size_t *lens, int n, int e
             j.first = starts[fi];
             const int k = starts[fi + 1] - j.first;
             j.cv.assign(static_cast<size_t>(k), nullptr);
+            auto t0 = std::chrono::steady_clock::now();
             int rc = cy_canvases_from_traces(traces + j.first, lens + j.first, k, engine, 0, j.cv.data());
+            auto t1 = std::chrono::steady_clock::now();
             if (rc == CY_OK) {
                 std::vector<cy_ctx *> ctx(static_cast<size_t>(k));
                 for (int i = 0; i < k; ++i) ctx[i] = static_cast<cy_ctx *>(cy_canvas_ctx(j.cv[i]));
                 rc = cy_frame_create(ctx.data(), k, engine, &j.f);
+                if (trace_timing)
+                    std::fprintf(stderr, "render_traces frame %d: %d canvases, replay %.1f ms, create %.1f ms\n", fi, k,
+                                 ms(t0, t1), ms(t1, std::chrono::steady_clock::now()));
                 if (rc == CY_OK) {
                     long long st[10] = {};
                     if (cy_frame_stats(j.f, st, 10) >= 10) up += st[9];
@@ -333,7 +346,9 @@ int cy_render_traces(const void *const *traces, const size_t *lens, int n, int e
             if (j.f && failure.load() == 0) {
                 std::vector<size_t> offs(static_cast<size_t>(k) + 1);
                 const unsigned char *data = nullptr;
+                auto t0 = std::chrono::steady_clock::now();
                 int rc = cy_frame_finish_views(j.f, &data, offs.data());
+                auto t1 = std::chrono::steady_clock::now();
                 if (rc) fail(rc);
                 for (int i = 0; rc == 0 && i < k; ++i)
                     if (offs[i + 1] - offs[i] != offsets[j.first + i + 1] - offsets[j.first + i]) {
@@ -353,6 +368,9 @@ int cy_render_traces(const void *const *traces, const size_t *lens, int n, int e
                             }
                         });
                     for (std::thread &th : pool) th.join();
+                    if (trace_timing)
+                        std::fprintf(stderr, "render_traces frame %d: finish %.1f ms, copy out %.1f ms\n", fi, ms(t0, t1),
+                                     ms(t1, std::chrono::steady_clock::now()));
                 }
             }
             if (j.f) cy_frame_destroy(j.f);

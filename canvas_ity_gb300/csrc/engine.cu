@@ -27,6 +27,7 @@
 #include <mutex>
 #include <thread>
 #include <atomic>
+#include <chrono>
 #include <vector>
 
 #include "../../include/cy_gpu.h"
@@ -828,6 +829,11 @@ int frame::stroke_passes(bool sizing) {
 
 int frame::prepare() {
     if (int rc = ensure_srgb_table()) return fail(rc);
+    const bool timing = std::getenv("CY_DEBUG") != nullptr;
+    auto t_begin = std::chrono::steady_clock::now();
+    auto since = [&](std::chrono::steady_clock::time_point a) {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+    };
     gather();
     std::vector<command> &cmds = all.cmds;
     for (cy_ctx *c : cvs) {
@@ -861,6 +867,7 @@ int frame::prepare() {
     if (!lut_dev.ensure(256 * sizeof(float))) return fail(CY_ENOMEM, __LINE__);
     if (!ok(cudaMemcpyAsync(lut_dev.p, linear_lut_host(), 256 * sizeof(float), cudaMemcpyHostToDevice, stream)))
         return status;
+    double t_staged = timing ? since(t_begin) : 0.0;
     // Flattening counts size the polyline store (one read-back).
     int n_items = static_cast<int>(n_items_all);
     const int32_t *offs_h = nullptr;
@@ -1025,8 +1032,13 @@ int frame::prepare() {
         !get_host.ensure(static_cast<size_t>(std::max<int64_t>(get_total, 16))))
         return fail(CY_ENOMEM, __LINE__);
     if (!ok(cudaFuncSetAttribute(k_rows_long, cudaFuncAttributeMaxDynamicSharedMemorySize, kLongSmem))) return status;
+    double t_sized = timing ? since(t_begin) : 0.0;
     // The first run also sizes the run store and the clip masks.
-    return run();
+    int rc = run();
+    if (timing)
+        std::fprintf(stderr, "frame prepare: staged %.1f ms, geometry sized %.1f ms, first run queued %.1f ms\n",
+                     t_staged, t_sized, since(t_begin));
+    return rc;
 }
 
 int frame::run() {
