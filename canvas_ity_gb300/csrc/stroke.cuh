@@ -23,7 +23,6 @@
 namespace cyg {
 
 static constexpr int kDashCap = 1 << 22;     // dashed points one subpath may produce
-static constexpr int kStrokeCap = 1 << 26;   // outline points one subpath may produce
 
 __device__ __forceinline__ float2 xform(const float *m, float2 p) {
     return f2(m[0] * p.x + m[2] * p.y + m[4], m[1] * p.x + m[3] * p.y + m[5]);
