@@ -313,6 +313,8 @@ int cy_render_traces(const void *const *traces, const size_t *lens, int n, int e
                 std::vector<cy_ctx *> ctx(static_cast<size_t>(k));
                 for (int i = 0; i < k; ++i) ctx[i] = static_cast<cy_ctx *>(cy_canvas_ctx(j.cv[i]));
                 rc = cy_frame_create(ctx.data(), k, engine, &j.f);
+                // A canvas wider than a tile-engine strip renders on the plain engine.
+                if (rc == CY_EINVAL && engine == 0) rc = cy_frame_create(ctx.data(), k, 1, &j.f);
                 if (trace_timing)
                     std::fprintf(stderr, "render_traces frame %d: %d canvases, replay %.1f ms, create %.1f ms\n", fi, k,
                                  ms(t0, t1), ms(t1, std::chrono::steady_clock::now()));

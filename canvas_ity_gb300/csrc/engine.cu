@@ -64,6 +64,24 @@ struct dbuf {
         cap = n;
         return true;
     }
+    // Grow to at least `bytes`, keeping the first `keep` bytes (copied on
+    // stream s, which is waited for before the old buffer is freed).
+    bool grow_keep(size_t bytes, size_t keep, cudaStream_t s) {
+        if (bytes <= cap && p) return true;
+        size_t n = std::max(std::max(bytes, static_cast<size_t>(256)), cap + cap / 2);
+        void *q = nullptr;
+        if (cudaMalloc(&q, n) != cudaSuccess) { cudaGetLastError(); return false; }
+        if (p && keep && (cudaMemcpyAsync(q, p, std::min(keep, cap), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+                          cudaStreamSynchronize(s) != cudaSuccess)) {
+            cudaGetLastError();
+            cudaFree(q);
+            return false;
+        }
+        if (p) cudaFree(p);
+        p = q;
+        cap = n;
+        return true;
+    }
     template <class T> T *as() const { return static_cast<T *>(p); }
     void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
 };
@@ -326,6 +344,11 @@ struct frame {
     // nflat), the outlines follow at nflat; dashed centre lines are apart.
     int64_t nflat = 0, n_outline = 0, n_dashed = 0, n_pieces = 0, n_chunks = 0;
     bool any_dash = false;
+    // The sizing in prepare() flattened the centre lines and ran every stroke
+    // pass up to the outline counts; the first run then only writes the
+    // outlines (later runs redo everything).
+    bool geometry_ready = false;
+    int stroke_write();
     std::vector<int32_t> cmd_cv;
     int64_t get_total = 0;
     std::vector<scan_job> jobs;
@@ -399,6 +422,7 @@ struct frame {
         n_groups = n_styles = n_dash = 0;
         nflat = n_outline = n_dashed = n_pieces = n_chunks = 0;
         any_dash = false;
+        geometry_ready = false;
         cmd_cv.clear();
         get_total = 0;
         jobs.clear();
@@ -812,12 +836,22 @@ int frame::stroke_passes(bool sizing) {
         n_outline = g64[ng];
         if (err != 0 || n_outline < 0 || nflat + n_outline > (static_cast<int64_t>(1) << 30))
             return fail(CY_ENOMEM, __LINE__);
-        // the outlines go after the centre lines; every run writes both again
-        if (!flat_pts.ensure(static_cast<size_t>(nflat + n_outline + 1) * sizeof(float2)) ||
-            !flat_prev.ensure(static_cast<size_t>(nflat + n_outline + 1) * 4))
+        // the outlines go after the centre lines, which are kept
+        if (!flat_pts.grow_keep(static_cast<size_t>(nflat + n_outline + 1) * sizeof(float2),
+                                static_cast<size_t>(nflat) * sizeof(float2), stream) ||
+            !flat_prev.grow_keep(static_cast<size_t>(nflat + n_outline + 1) * 4, static_cast<size_t>(nflat) * 4,
+                                 stream))
             return fail(CY_ENOMEM, __LINE__);
+        geometry_ready = true;
         return ok(cudaGetLastError()) ? CY_OK : status;
     }
+    return stroke_write();
+}
+
+// The outlines from the counted joins (k_join's write pass).
+int frame::stroke_write() {
+    const int nch = static_cast<int>(n_chunks);
+    const int jgrid = std::max(1, (nch + kStrokeWarps - 1) / kStrokeWarps);
     k_join<true><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(), nch,
                                                           jn_cnt.as<int32_t>(), jn_alpha.as<float>(), nullptr,
                                                           jn_off.as<int64_t>(),
@@ -1065,7 +1099,9 @@ int frame::run() {
         src.texels = pat_f4.as<float4>();
     }
     int n_items_flat = static_cast<int>(n_items_all);
-    if (n_items_flat > 0) {
+    const bool reuse = geometry_ready;   // first run after the sizing: centre lines and counts are in place
+    geometry_ready = false;
+    if (n_items_flat > 0 && !reuse) {
         // flattening counts and offsets, then the points (the first run's
         // read-back only sized the store)
         k_flat_count<<<(n_items_flat + 255) / 256, 256, 0, stream>>>(d_bez, d_items, n_items_flat,
@@ -1079,7 +1115,7 @@ int frame::run() {
     }
     if (n_tex > 0) ++launches;
     if (n_groups > 0 && n_outline > 0) {
-        if (int rc = stroke_passes(false)) return rc;
+        if (int rc = reuse ? stroke_write() : stroke_passes(false)) return rc;
     }
     mark();   // 1: patterns and flattening done
     size_t nr = static_cast<size_t>(total_rows);

@@ -324,3 +324,17 @@ def test_render_traces_rejects_wrong_sizes():
     offsets = np.array([0, sizes[0] + 4, sizes[0] + sizes[1] + 4], np.uint64)
     with pytest.raises(RuntimeError, match="status -1"):
         native.render_traces(traces, 0, 0, np.zeros(int(offsets[-1]), np.uint8), offsets)
+
+
+def test_render_traces_wide_canvas_falls_back():
+    """A canvas wider than a tile-engine strip renders on the per-draw engine
+    inside cy_render_traces, with the same reads as alone."""
+    t = T.TraceWriter(4500, 12)
+    t.set_color(T.FILL_STYLE, 0.3, 0.6, 0.9, 0.8)
+    t.begin_path(); t.move_to(3.5, 1.25); t.line_to(4490.0, 6.0); t.line_to(10.0, 11.0); t.fill()
+    t.get_image_data(4500, 12, 0, 0)
+    wide = t.finish(read_back=False)
+    traces = [scenes.small_scene("c0_small", 2), wide]
+    views, _ = native.render_traces(traces, 0)
+    assert bytes(views[1]) == native.replay(wide)[0]
+    assert bytes(views[0]) == native.replay(traces[0])[0]
