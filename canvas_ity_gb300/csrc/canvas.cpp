@@ -1066,6 +1066,15 @@ bool canvas::is_point_in_path(float x, float y) {
     return s.even_odd ? (winding & 2) != 0 : winding != 0;   // each crossing edge counts +-1 on each side: twice the winding number
 }
 void canvas::set_fill_rule(fill_rule_style rule) { self->even_odd = rule == even_odd; }
+int canvas::points_in_path(float const *xy, int n, unsigned char *inside) {
+    // is_point_in_path (hpp:3101-3132) for many points: the path's
+    // device-space cubics go to the GPU, flattened there as for a fill
+    detail::canvas_state &s = *self;
+    s.counts.resize(s.path.subs.size());
+    for (size_t i = 0; i < s.path.subs.size(); ++i) s.counts[i] = static_cast<int>(s.path.subs[i].count);
+    return cy_points_in_path(reinterpret_cast<const float *>(s.path.pts.data()), s.counts.data(),
+                             static_cast<int>(s.counts.size()), xy, n, s.even_odd ? 1 : 0, inside);
+}
 
 static void rect_lines(detail::canvas_state &s, float x, float y, float w, float h, bool closing_point) {
     s.lines.pts.clear();

@@ -148,6 +148,11 @@ void cy_canvas_set_fill_rule(cy_canvas *c, int rule) {
     c->get().set_fill_rule(rule == 1 ? canvas_ity::even_odd : canvas_ity::nonzero);
 }
 
+int cy_canvas_points_in_path(cy_canvas *c, const float *xy, int n, unsigned char *inside) {
+    if (!c) return CY_EINVAL;
+    return c->get().points_in_path(xy, n, inside);
+}
+
 int cy_take_thread_status(void);
 
 int cy_replay(const void *trace, size_t trace_len, void *images, size_t images_cap, size_t *images_len,

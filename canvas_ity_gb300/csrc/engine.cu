@@ -1992,6 +1992,99 @@ int cy_fill_lines(cy_ctx *c, const float *points, const int *counts, int n_sub, 
     return queue_draw(c, points, counts, n_sub, false, paint, state);
 }
 
+int cy_points_in_path(const float *points, const int *counts, int n_sub, const float *queries, int n_queries,
+                      int fill_rule, unsigned char *inside) {
+    if (n_sub < 0 || n_queries < 0 || (n_sub > 0 && (!points || !counts)) ||
+        (n_queries > 0 && (!queries || !inside)))
+        return CY_EINVAL;
+    size_t total = 0;
+    if (!valid_counts(counts, n_sub, total)) return CY_EINVAL;
+    for (int s = 0; s < n_sub; ++s)
+        if (counts[s] != 0 && (counts[s] - 1) % 3 != 0) return CY_EINVAL;
+    if (n_queries == 0) return CY_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return CY_ENODEV;
+    }
+    // flattening items as for a fill, every subpath kept (path_to_lines(false))
+    std::vector<flat_item> items;
+    size_t at = 0;
+    for (int s = 0; s < n_sub; ++s) {
+        int n = counts[s];
+        if (n == 0) continue;
+        int32_t head = static_cast<int32_t>(items.size());
+        items.push_back(flat_item{static_cast<int32_t>(at), 0, -1.0f});
+        for (int k = 1; k < n; k += 3) items.push_back(flat_item{static_cast<int32_t>(at + k - 1), -1, -1.0f});
+        items[head].sub_end = static_cast<int32_t>(items.size());
+        at += static_cast<size_t>(n);
+    }
+    if (items.empty()) {
+        std::memset(inside, 0, static_cast<size_t>(n_queries));
+        return CY_OK;
+    }
+    const int ni = static_cast<int>(items.size());
+    cudaStream_t st = nullptr;
+    void *d_bez = nullptr, *d_items = nullptr, *d_cnt = nullptr, *d_off = nullptr, *d_pts = nullptr, *d_prev = nullptr,
+         *d_q = nullptr, *d_in = nullptr;
+    int rc = CY_OK;
+    auto check = [&](cudaError_t e) {
+        if (e == cudaSuccess || rc != CY_OK) return rc == CY_OK;
+        cudaGetLastError();
+        rc = e == cudaErrorMemoryAllocation ? CY_ENOMEM : CY_ECUDA;
+        return false;
+    };
+    std::vector<int32_t> off(static_cast<size_t>(ni) + 1);
+    if (check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) &&
+        check(cudaMalloc(&d_bez, total * sizeof(float2))) && check(cudaMalloc(&d_items, items.size() * sizeof(flat_item))) &&
+        check(cudaMalloc(&d_cnt, off.size() * 4)) && check(cudaMalloc(&d_off, off.size() * 4)) &&
+        check(cudaMemcpyAsync(d_bez, points, total * sizeof(float2), cudaMemcpyHostToDevice, st)) &&
+        check(cudaMemcpyAsync(d_items, items.data(), items.size() * sizeof(flat_item), cudaMemcpyHostToDevice, st))) {
+        k_flat_count<<<(ni + 255) / 256, 256, 0, st>>>(static_cast<const float2 *>(d_bez),
+                                                      static_cast<const flat_item *>(d_items), ni,
+                                                      static_cast<int32_t *>(d_cnt));
+        if (check(cudaGetLastError()) &&
+            check(cudaMemcpyAsync(off.data(), d_cnt, static_cast<size_t>(ni) * 4, cudaMemcpyDeviceToHost, st)) &&
+            check(cudaStreamSynchronize(st))) {
+            // exclusive scan of the point counts on the host
+            int64_t sum = 0;
+            for (int i = 0; i < ni; ++i) {
+                int32_t c = off[i];
+                off[i] = static_cast<int32_t>(sum);
+                sum += c;
+            }
+            if (sum <= 0 || sum > (static_cast<int64_t>(1) << 30)) rc = CY_ENOMEM;
+            off[ni] = static_cast<int32_t>(sum);
+            const size_t np = static_cast<size_t>(sum);
+            if (rc == CY_OK && check(cudaMalloc(&d_pts, np * sizeof(float2))) && check(cudaMalloc(&d_prev, np * 4)) &&
+                check(cudaMalloc(&d_q, static_cast<size_t>(n_queries) * sizeof(float2))) &&
+                check(cudaMalloc(&d_in, static_cast<size_t>(n_queries))) &&
+                check(cudaMemcpyAsync(d_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, st)) &&
+                check(cudaMemcpyAsync(d_q, queries, static_cast<size_t>(n_queries) * sizeof(float2),
+                                      cudaMemcpyHostToDevice, st))) {
+                k_flat_emit<<<(ni + 255) / 256, 256, 0, st>>>(static_cast<const float2 *>(d_bez),
+                                                             static_cast<const flat_item *>(d_items), ni,
+                                                             static_cast<const int32_t *>(d_off),
+                                                             static_cast<float2 *>(d_pts), static_cast<int32_t *>(d_prev),
+                                                             static_cast<int64_t>(np));
+                k_points_in_path<<<(n_queries + 255) / 256, 256, 0, st>>>(
+                    static_cast<const float2 *>(d_pts), static_cast<const int32_t *>(d_prev), static_cast<int>(np),
+                    static_cast<const float2 *>(d_q), n_queries, fill_rule == 1 ? 1 : 0,
+                    static_cast<unsigned char *>(d_in));
+                if (check(cudaGetLastError()) &&
+                    check(cudaMemcpyAsync(inside, d_in, static_cast<size_t>(n_queries), cudaMemcpyDeviceToHost, st)))
+                    check(cudaStreamSynchronize(st));
+            }
+        }
+    }
+    if (st) cudaStreamSynchronize(st);
+    for (void *p : {d_bez, d_items, d_cnt, d_off, d_pts, d_prev, d_q, d_in})
+        if (p) cudaFree(p);
+    if (st) cudaStreamDestroy(st);
+    cudaGetLastError();
+    return rc;
+}
+
 int cy_stroke_path(cy_ctx *c, const float *points, const int *counts, const int *closed, int n_sub,
                    const cy_stroke_style *style, const cy_paint *paint, const cy_draw_state *state) {
     return queue_stroke(c, points, counts, closed, n_sub, style, paint, state);

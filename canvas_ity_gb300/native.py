@@ -286,6 +286,29 @@ class Frame:
         self.close()
 
 
+def points_in_path(trace: bytes, queries) -> np.ndarray:
+    """Replay a call list into a canvas, then test (x, y) query points
+    against its current path on the GPU (cy_canvas_points_in_path, the
+    batched is_point_in_path).  Returns a uint8 array of 0/1."""
+    lib = _batch_lib()
+    q = np.ascontiguousarray(queries, np.float32).reshape(-1, 2)
+    st = ctypes.c_int(0)
+    c = lib.cy_canvas_from_trace(ctypes.cast(ctypes.c_char_p(trace), ctypes.c_void_p), len(trace), ctypes.byref(st))
+    if not c:
+        raise RuntimeError(f"replay failed with status {st.value}")
+    try:
+        fn = lib.cy_canvas_points_in_path
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        out = np.zeros(len(q), np.uint8)
+        rc = fn(c, q.ctypes.data, len(q), out.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"cy_canvas_points_in_path failed with status {rc}")
+        return out
+    finally:
+        lib.cy_canvas_delete(c)
+
+
 def render_traces(traces, engine: int = 0, frame_pixels: int = 0, out=None, offsets=None):
     """End to end through cy_render_traces: call lists in host memory to
     RGBA8 reads in host memory, frames pipelined (host work of one frame

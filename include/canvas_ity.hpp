@@ -143,6 +143,11 @@ public:
     // reference).  Strokes, text and rectangles always fill nonzero.
     void set_fill_rule( fill_rule_style rule );
 
+    // Extension, no reference counterpart: is_point_in_path() for n points
+    // (x, y pairs in xy) at once, tested on the GPU; inside[i] receives 0 or
+    // 1.  Returns 0 or a negative status (see cy_gpu.h).
+    int points_in_path( float const *xy, int n, unsigned char *inside );
+
     // Extension, no reference counterpart: 0 if every GPU operation so far
     // succeeded, else the first negative status (see cy_gpu.h).  The
     // reference API has no error channel; this lets callers detect device

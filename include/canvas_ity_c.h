@@ -81,6 +81,10 @@ void cy_canvas_restore(cy_canvas *c);                                           
 /* Extension, no reference counterpart: 0 nonzero (default), 1 even-odd for
  * fill(), clip() and is_point_in_path(). */
 void cy_canvas_set_fill_rule(cy_canvas *c, int rule);
+/* Extension, no reference counterpart: is_point_in_path for n points (x, y
+ * pairs) at once on the GPU; inside[i] receives 0 or 1.  Returns 0 or a
+ * negative status (cy_gpu.h). */
+int cy_canvas_points_in_path(cy_canvas *c, const float *xy, int n, unsigned char *inside);
 
 /* Replay a recorded call list (cy_trace.h) through canvas_ity::canvas.
  * Every non-null get_image_data appends its compact RGBA8 rectangle to

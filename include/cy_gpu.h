@@ -113,6 +113,16 @@ int cy_stroke_path(cy_ctx *ctx, const float *points, const int *subpath_counts, 
                    int n_subpaths, const cy_stroke_style *style, const cy_paint *paint,
                    const cy_draw_state *state);
 
+/* is_point_in_path (hpp:3101-3132) for many points at once: the path is
+ * laid out as for cy_fill_path (device-space Bezier points, 1 + 3k per
+ * subpath); queries holds n_queries x,y pairs in device space, as the
+ * reference takes them; inside[i] receives 1 when query i is inside (on
+ * the boundary counts as inside) under fill_rule (0 nonzero, 1 even-odd).
+ * The path is flattened and tested on the GPU; returns after the results
+ * are written.  No counterpart in the reference (one point per call). */
+int cy_points_in_path(const float *points, const int *subpath_counts, int n_subpaths, const float *queries,
+                      int n_queries, int fill_rule, unsigned char *inside);
+
 /* Where canvas_ity::canvas::stroke() expands strokes, for every canvas of
  * the process: 1 (the default) on the GPU through cy_stroke_path, 0 on the
  * host (the reference's own acosf/tanf) through cy_fill_lines. */
