@@ -35,6 +35,7 @@
 #include "kernels.cuh"
 #include "strips.cuh"
 #include "stroke.cuh"
+#include "encode.hpp"
 
 using namespace cyg;
 
@@ -2203,6 +2204,49 @@ int cy_get_image(cy_ctx *c, unsigned char *image, int w, int h, int stride, int 
     q.get_stride.push_back(stride);
     if (c->deferred) return CY_OK;
     return flush_ctx(c);
+}
+
+int cy_encode_image(cy_ctx *c, int format, int x, int y, int w, int h, unsigned char *out, size_t cap,
+                    size_t *len) {
+    if (!c || (format != encode::TGA && format != encode::PNG) || w <= 0 || h <= 0 || w > 65535 || h > 65535)
+        return CY_EINVAL;
+    if (format == encode::PNG && (w > 16383 || encode::png_size(w, h) > static_cast<size_t>(INT32_MAX)))
+        return CY_EINVAL;   // one stored block per row, and the writer's int sizes
+    const bool png = format == encode::PNG;
+    const size_t size = png ? encode::png_size(w, h) : encode::tga_size(w, h);
+    if (len) *len = size;
+    if (!out || cap < size) return CY_ENOMEM;
+    if (c->status) return c->status;
+    if (int rc = flush_ctx(c)) return rc;
+    if (int rc = ensure_srgb_table()) return rc;
+    unsigned char *d_out = nullptr;
+    uint32_t *d_sums = nullptr;
+    std::vector<uint32_t> sums(png ? static_cast<size_t>(h) * 3 : 0);
+    auto okc = [&](cudaError_t e) {
+        if (e == cudaSuccess) return true;
+        cudaGetLastError();
+        return false;
+    };
+    int rc = CY_OK;
+    if (!okc(cudaMalloc(&d_out, size)) || (png && !okc(cudaMalloc(&d_sums, sums.size() * 4)))) {
+        rc = CY_ENOMEM;
+    } else {
+        dim3 blk(32, 8), grd((w + 31) / 32, (h + 7) / 8);
+        k_encode<<<grd, blk, 0, c->stream>>>(c->bitmap, c->W, c->H, c->has_content ? 0 : 1, w, h, x, y, png ? 1 : 0,
+                                             d_out);
+        if (png)
+            k_png_rows<<<(h + 127) / 128, 128, 0, c->stream>>>(d_out, w, h, d_sums, d_sums + h, d_sums + 2 * h);
+        if (!okc(cudaGetLastError()) || !okc(cudaMemcpyAsync(out, d_out, size, cudaMemcpyDeviceToHost, c->stream)) ||
+            (png && !okc(cudaMemcpyAsync(sums.data(), d_sums, sums.size() * 4, cudaMemcpyDeviceToHost, c->stream))) ||
+            !okc(cudaStreamSynchronize(c->stream)))
+            rc = c->fail(CY_ECUDA);
+    }
+    if (d_out) cudaFree(d_out);
+    if (d_sums) cudaFree(d_sums);
+    if (rc) return rc;
+    if (png) encode::png_frame(out, w, h, sums.data(), sums.data() + h, sums.data() + 2 * static_cast<size_t>(h));
+    else encode::tga_header(out, w, h);
+    return CY_OK;
 }
 
 int cy_read_linear(cy_ctx *c, float *out) {

@@ -309,6 +309,34 @@ def points_in_path(trace: bytes, queries) -> np.ndarray:
         lib.cy_canvas_delete(c)
 
 
+TGA, PNG = 0, 1
+
+
+def encode_image(trace: bytes, fmt: int, x: int, y: int, w: int, h: int) -> bytes:
+    """Replay a call list into a canvas, then pack the w x h rectangle at
+    (x, y) into a TGA or PNG file on the GPU (cy_encode_image)."""
+    lib = _batch_lib()
+    st = ctypes.c_int(0)
+    c = lib.cy_canvas_from_trace(ctypes.cast(ctypes.c_char_p(trace), ctypes.c_void_p), len(trace), ctypes.byref(st))
+    if not c:
+        raise RuntimeError(f"replay failed with status {st.value}")
+    try:
+        fn = lib.cy_encode_image
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                       ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        size = ctypes.c_size_t(0)
+        ctx = lib.cy_canvas_ctx(c)
+        fn(ctx, int(fmt), int(x), int(y), int(w), int(h), None, 0, ctypes.byref(size))
+        buf = ctypes.create_string_buffer(max(size.value, 1))
+        rc = fn(ctx, int(fmt), int(x), int(y), int(w), int(h), buf, size.value, ctypes.byref(size))
+        if rc != 0:
+            raise RuntimeError(f"cy_encode_image failed with status {rc}")
+        return buf.raw[: size.value]
+    finally:
+        lib.cy_canvas_delete(c)
+
+
 def render_traces(traces, engine: int = 0, frame_pixels: int = 0, out=None, offsets=None):
     """End to end through cy_render_traces: call lists in host memory to
     RGBA8 reads in host memory, frames pipelined (host work of one frame

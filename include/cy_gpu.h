@@ -153,6 +153,17 @@ int cy_put_image(cy_ctx *ctx, const unsigned char *image, int width, int height,
  * `bitmap`, hpp:1171) into out[W*H*4].  Used to check coverage exactly. */
 int cy_read_linear(cy_ctx *ctx, float *out);
 
+/* No counterpart in the reference's library: get_image_data of a rectangle
+ * written as an image file, packed on the GPU.  format 0: TGA as the
+ * reference's tiger demo writes it (demos/tiger/tiger.cpp:4336-4343,
+ * BGRA, top-left origin, w and h up to 65535); format 1: PNG as the
+ * reference's test harness writes it (test/test.cpp:2415-2511, RGBA8, one
+ * stored deflate block per row, w up to 16383).  Runs queued work first.
+ * *len receives the file size; CY_ENOMEM (nothing written) when out is
+ * NULL or cap is smaller. */
+int cy_encode_image(cy_ctx *ctx, int format, int x, int y, int width, int height, unsigned char *out, size_t cap,
+                    size_t *len);
+
 /* Run all queued work and wait for it. */
 int cy_flush(cy_ctx *ctx);
 
