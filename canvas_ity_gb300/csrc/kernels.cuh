@@ -16,6 +16,9 @@
 #include <stdint.h>
 
 #include "device.cuh"
+#include "flatten.cuh"
+#include "hit.cuh"
+#include "pack.cuh"
 
 namespace cyg {
 
@@ -42,62 +45,6 @@ __global__ void k_pattern_prep(const uchar4 *__restrict__ src, float4 *__restric
     uchar4 c = src[i];
     float a = static_cast<float>(c.w) / 255.0f;
     dst[i] = make_float4(lut[c.x] * a, lut[c.y] * a, lut[c.z] * a, a);
-}
-
-// ------------------------------------------------------------- flattening
-__global__ void k_flat_count(const float2 *__restrict__ bez, const flat_item *__restrict__ items, int n,
-                             int32_t *__restrict__ counts) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    flat_item it = items[i];
-    if (it.sub_end >= 0) { counts[i] = 1; return; }
-    counts[i] = flatten_cubic<false>(bez[it.pt], bez[it.pt + 1], bez[it.pt + 2], bez[it.pt + 3], it.angular, nullptr, 0);
-}
-
-__global__ void k_flat_emit(const float2 *__restrict__ bez, const flat_item *__restrict__ items, int n,
-                            const int32_t *__restrict__ offs, float2 *__restrict__ pts,
-                            int32_t *__restrict__ prev, int64_t cap) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    flat_item it = items[i];
-    int o = offs[i];
-    int cnt = offs[i + 1] - o;
-    if (o < 0 || static_cast<int64_t>(o) + cnt > cap) return;
-    if (it.sub_end >= 0) {
-        pts[o] = bez[it.pt];
-        prev[o] = offs[it.sub_end] - 1;   // closing segment from the subpath's last point
-        return;
-    }
-    flatten_cubic<true>(bez[it.pt], bez[it.pt + 1], bez[it.pt + 2], bez[it.pt + 3], it.angular, pts + o, cnt);
-    for (int k = 0; k < cnt; ++k) prev[o + k] = o + k - 1;
-}
-
-// ------------------------------------------------------------ hit testing
-// is_point_in_path (hpp:3101-3132) for many query points, one thread per
-// point, over the fill-mode polyline of one path.  Each point k with its
-// previous-point link is the reference's segment from pts[prev[k]] to
-// pts[k] (the last point of a subpath links back to its first).  The
-// crossing count is an integer sum and a point on the boundary is inside
-// whichever segment finds it, so the segment order does not matter.
-__global__ void k_points_in_path(const float2 *__restrict__ pts, const int32_t *__restrict__ prev, int n_pts,
-                                 const float2 *__restrict__ queries, int n_queries, int even_odd,
-                                 unsigned char *__restrict__ inside) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n_queries) return;
-    const float x = queries[q].x, y = queries[q].y;
-    int winding = 0;
-    bool boundary = false;
-    for (int k = 0; k < n_pts && !boundary; ++k) {
-        float2 from = pts[prev[k]], to = pts[k];
-        if ((from.y < y && y <= to.y) || (to.y < y && y <= from.y)) {
-            float side = dot2(perp2(sub2(to, from)), sub2(f2(x, y), from));
-            if (side == 0.0f) boundary = true;
-            else winding += side > 0.0f ? 1 : -1;
-        } else if (from.y == y && y == to.y && ((from.x <= x && x <= to.x) || (to.x <= x && x <= from.x))) {
-            boundary = true;
-        }
-    }
-    inside[q] = boundary || (even_odd ? (winding & 2) != 0 : winding != 0) ? 1 : 0;
 }
 
 // ------------------------------------------------------------------- scan
@@ -1144,78 +1091,6 @@ __global__ void k_get(const float4 *__restrict__ bitmap, int W, int H, uchar4 *_
     float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (0 <= cx && cx < W && 0 <= cy && cy < H) c = bitmap[static_cast<size_t>(cy) * W + cx];
     out[static_cast<size_t>(iy) * w + ix] = to_srgb8(c, cx, cy);
-}
-
-// ---------------------------------------------------------- file packing
-// get_image_data's conversion (as k_get) written straight into an image
-// file's layout (encode.hpp): TGA pixels as BGRA after an 18-byte header;
-// PNG pixels after each row's 6-byte stored-block prefix (final flag, LEN,
-// NLEN, filter byte 0) at 56 + y * (6 + 4w).  `blank`: the canvas was never
-// painted (its buffer is not cleared), so every pixel is transparent black.
-__global__ void k_encode(const float4 *__restrict__ bitmap, int W, int H, int blank, int w, int h, int x0, int y0,
-                         int png, unsigned char *__restrict__ out) {
-    int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    int iy = blockIdx.y * blockDim.y + threadIdx.y;
-    if (ix >= w || iy >= h) return;
-    int cx = x0 + ix, cy = y0 + iy;
-    float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (!blank && 0 <= cx && cx < W && 0 <= cy && cy < H) c = bitmap[static_cast<size_t>(cy) * W + cx];
-    uchar4 p = to_srgb8(c, cx, cy);
-    if (!png) {
-        unsigned char *d = out + 18 + (static_cast<size_t>(iy) * w + ix) * 4;
-        d[0] = p.z;
-        d[1] = p.y;
-        d[2] = p.x;
-        d[3] = p.w;
-        return;
-    }
-    const size_t row = 56 + static_cast<size_t>(iy) * (6 + static_cast<size_t>(w) * 4);
-    unsigned char *d = out + row + 6 + static_cast<size_t>(ix) * 4;
-    d[0] = p.x;
-    d[1] = p.y;
-    d[2] = p.z;
-    d[3] = p.w;
-    if (ix == 0) {
-        const unsigned size = 1 + static_cast<unsigned>(w) * 4;
-        unsigned char *r = out + row;
-        r[0] = iy + 1 == h ? 1 : 0;
-        r[1] = static_cast<unsigned char>(size);
-        r[2] = static_cast<unsigned char>(size >> 8);
-        r[3] = static_cast<unsigned char>(~size);
-        r[4] = static_cast<unsigned char>(~size >> 8);
-        r[5] = 0;
-    }
-}
-
-// Per PNG row (one thread each): the CRC-32 of its 6 + 4w bytes from a zero
-// register, and the Adler-32 partials of its 1 + 4w zlib data bytes (filter
-// byte and pixels): a = sum of bytes, b = sum of byte * (distance to the
-// row's end), both mod 65521.
-__global__ void k_png_rows(const unsigned char *__restrict__ out, int w, int h, uint32_t *__restrict__ row_crc,
-                           uint32_t *__restrict__ row_a, uint32_t *__restrict__ row_b) {
-    __shared__ uint32_t tab[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
-        uint32_t v = static_cast<uint32_t>(i);
-        for (int k = 0; k < 8; ++k) v = (v & 1 ? 0xedb88320u : 0u) ^ (v >> 1);
-        tab[i] = v;
-    }
-    __syncthreads();
-    int y = blockIdx.x * blockDim.x + threadIdx.x;
-    if (y >= h) return;
-    const size_t n = 6 + static_cast<size_t>(w) * 4;
-    const unsigned char *r = out + 56 + static_cast<size_t>(y) * n;
-    uint32_t c = 0;
-    for (size_t k = 0; k < n; ++k) c = tab[(c ^ r[k]) & 0xff] ^ (c >> 8);
-    const uint64_t nd = n - 5;   // filter byte + pixels
-    uint64_t a = 0, b = 0;
-    for (uint64_t j = 0; j < nd; ++j) {
-        uint64_t v = r[5 + j];
-        a += v;
-        b += (nd - j) * v;
-    }
-    row_crc[y] = c;
-    row_a[y] = static_cast<uint32_t>(a % 65521);
-    row_b[y] = static_cast<uint32_t>(b % 65521);
 }
 
 }  // namespace cyg
