@@ -11,6 +11,10 @@
 // The float arithmetic mirrors the reference operation for operation (this
 // file is compiled with -ffp-contract=off) so that host-produced geometry is
 // identical to the reference's.  Citations: hpp = src/canvas_ity.hpp.
+//
+// Derived from canvas_ity (src/canvas_ity.hpp), Copyright (c) 2022 Andrew
+// Kensler, under the ISC license; its copyright and permission notice is
+// reproduced in LICENSES/canvas_ity-ISC.txt and applies to this file.
 
 #include "../../include/canvas_ity.hpp"
 #include "../../include/cy_gpu.h"

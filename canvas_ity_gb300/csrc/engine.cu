@@ -305,6 +305,7 @@ struct queue {
 
 struct cy_ctx {
     int W = 0, H = 0;
+    int device = 0;             // the device the canvas and its stream live on
     int status = 0;
     int engine = 0;
     bool deferred = false;
@@ -1944,6 +1945,11 @@ int cy_ctx_create(int width, int height, cy_ctx **out) {
     // Canvases wider than a strip use the per-draw engine.
     if (width > g_strip_pixels) c->engine = 1;
     c->masks.resize(1);
+    if (cudaGetDevice(&c->device) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return CY_ENODEV;
+    }
     size_t npx = static_cast<size_t>(width) * static_cast<size_t>(height);
     auto okc = [&](cudaError_t e) {
         if (e == cudaSuccess) return true;
@@ -2142,8 +2148,12 @@ int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, i
         return false;
     };
     if (!okc(cudaMalloc(&m.vis, static_cast<size_t>(c->W) * c->H * sizeof(float))) ||
-        !okc(cudaMalloc(&m.off, H1 * 4)) || !okc(cudaMalloc(&m.len, H1 * 4)) || !okc(cudaMalloc(&m.last_row, 4)))
+        !okc(cudaMalloc(&m.off, H1 * 4)) || !okc(cudaMalloc(&m.len, H1 * 4)) || !okc(cudaMalloc(&m.last_row, 4))) {
+        // Give back what was allocated, so the slot can be taken again.
+        m.free_all();
+        m = mask_slot();
         return c->status;
+    }
     m.refs = 2;   // the caller's reference plus the queued command's
     q.rows += c->H;
     q.cmds.push_back(cmd);
@@ -2295,6 +2305,9 @@ extern "C" int cy_get_image_noalloc(cy_ctx *c, unsigned char *image, int w, int 
         cudaGetLastError();
         return CY_ENODEV;
     }
+    // The array used is the current device's: it must be the canvas's own
+    // (a caller's mistake, answered without marking the context failed).
+    if (dev != c->device) return CY_EINVAL;
     std::lock_guard<std::mutex> hold(g_noalloc_lock);
     if (!g_noalloc_addr[dev]) {
         // Set-up, once per device, with that device current: host code must

@@ -179,7 +179,8 @@ int cy_flush(cy_ctx *ctx);
  * synchronises.  Converts the canvas as of its last flush exactly like
  * cy_get_image, staging in one fixed device array instead of allocated
  * memory, and calls no allocating routine.
- *   - Call with the context's device current.  The first call on a device
+ *   - Call with the context's device current (CY_EINVAL otherwise; the
+ *     context stays usable).  The first call on a device
  *     looks up the array's device address (cudaGetSymbolAddress) and, if no
  *     frame has run on the device yet, copies the 16 KiB colour-conversion
  *     table into its fixed device array; make that first call before any
@@ -188,6 +189,9 @@ int cy_flush(cy_ctx *ctx);
  *     CY_GET_IMAGE_NOALLOC_MAX_PIXELS, when stride < 4*width, or when the
  *     context still holds queued commands (run cy_flush first: a flush may
  *     allocate).  Returns when the pixels are in `image`.
+ *   - No batched frame (include/cy_batch.h) that holds the context may be
+ *     running: after cy_frame_run, call cy_frame_sync or cy_frame_finish
+ *     first, since the frame's stream writes the canvas.
  *   - All calls share the array.  Each call writes every pixel it copies
  *     back, so no part of the array has to start at zero.  Calls from the
  *     threads of one process are serialised by a lock and each waits for

@@ -1,6 +1,6 @@
 """Standalone workloads for the bandwidth-bound kernels, for profiling.
 
-    python -m canvas_ity_gb300.kernel_bench io [--side 4096] [--reps 3]
+    python kernel_bench.py io [--side 4096] [--reps 3]
 
 `io` replays, on the plain engine, a call list that puts a random RGBA8
 image over a whole side x side canvas and reads the canvas back: k_put
@@ -14,11 +14,16 @@ import argparse
 import json
 import time
 
+import os
+import sys
+
 import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 
 
 def io_trace(side: int, seed: int = 0) -> bytes:
-    from . import trace as T
+    from canvas_ity_gb300 import trace as T
     rng = np.random.default_rng(seed)
     img = rng.integers(0, 256, size=(side, side, 4), dtype=np.uint8)
     t = T.TraceWriter(side, side)
@@ -33,7 +38,7 @@ def main(argv=None) -> None:
     ap.add_argument("--side", type=int, default=4096)
     ap.add_argument("--reps", type=int, default=3)
     args = ap.parse_args(argv)
-    from . import build, native
+    from canvas_ity_gb300 import build, native
     build.build()
     native.set_engine(1)
     tb = io_trace(args.side)

@@ -26,7 +26,9 @@ ORACLE_SO = os.path.join(BUILD_DIR, "libcy_oracle.so")
 ORACLE_SIGN_SO = os.path.join(BUILD_DIR, "libcy_oracle_sign.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libcy_ref.so")
-REFERENCE_ROOT = os.environ.get("CY_REFERENCE_ROOT", "/root/reference")
+# Where the reference sources lie: CY_REFERENCE_ROOT, or the root passed to
+# build_reference().  Unset (as on a machine without them): no reference tools.
+REFERENCE_ROOT = os.environ.get("CY_REFERENCE_ROOT")
 
 _FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
 
@@ -59,15 +61,18 @@ def build(force: bool = False, ties: str = "reference", trig: str = "libm") -> s
     return out
 
 
-def build_reference(force: bool = False) -> Optional[str]:
-    """Build the reference tools from the read-only sources, if present."""
-    if not os.path.isfile(os.path.join(REFERENCE_ROOT, "src", "canvas_ity.hpp")):
-        return None
+def build_reference(force: bool = False, root: Optional[str] = None) -> Optional[str]:
+    """Build the reference tools from the read-only sources under `root` (or
+    CY_REFERENCE_ROOT), if they are there; returns the library path or None.
+    Tools built earlier are reused when no sources are named."""
+    root = root or REFERENCE_ROOT
+    if not root or not os.path.isfile(os.path.join(root, "src", "canvas_ity.hpp")):
+        return REF_SO if os.path.exists(REF_SO) and not force else None
     ours = [os.path.join(HERE, "ref", f) for f in os.listdir(os.path.join(HERE, "ref"))]
     ours += [os.path.join(HERE, "..", "include", h) for h in ("cy_trace.h", "cy_replay.hpp")]
     stale = not os.path.exists(REF_SO) or os.path.getmtime(REF_SO) < max(os.path.getmtime(p) for p in ours)
     if force or stale:
-        subprocess.check_call(["sh", os.path.join(HERE, "ref", "build_ref.sh"), REFERENCE_ROOT])
+        subprocess.check_call(["sh", os.path.join(HERE, "ref", "build_ref.sh"), root])
     return REF_SO
 
 

@@ -17,6 +17,10 @@
 // fused multiply-add.
 //
 // Every function cites the reference lines it restates (hpp = src/canvas_ity.hpp).
+//
+// Derived from canvas_ity (src/canvas_ity.hpp), Copyright (c) 2022 Andrew
+// Kensler, under the ISC license; its copyright and permission notice is
+// reproduced in LICENSES/canvas_ity-ISC.txt and applies to this file.
 
 #include <algorithm>
 #include <cmath>

@@ -4,9 +4,13 @@
 #   libcy_ref.so   reference canvas + call-list replay (cyr_replay)
 #   ref_recorder   the reference's own test/test.cpp compiled against the
 #                  recording canvas (oracle/ref/recorder.hpp)
-# Usage: oracle/ref/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/ref/build_ref.sh REFERENCE_ROOT   (or CY_REFERENCE_ROOT in the environment)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-$CY_REFERENCE_ROOT}
+if [ -z "$REF" ]; then
+    echo "usage: $0 REFERENCE_ROOT (or set CY_REFERENCE_ROOT)" >&2
+    exit 2
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$HERE/../_ref
 if [ ! -f "$REF/src/canvas_ity.hpp" ]; then

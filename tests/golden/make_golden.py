@@ -10,7 +10,7 @@ Runs only where the reference sources are present.  Steps:
      reference's table (test/test.cpp:2185-2261), and the hash the
      reference produced here.
 
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT   (or CY_REFERENCE_ROOT set)
 """
 import glob
 import json
@@ -26,7 +26,9 @@ REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CY_REFERENCE_ROOT")
+    if not ref:
+        raise SystemExit(__doc__)
     subprocess.check_call(["sh", os.path.join(REPO, "oracle", "ref", "build_ref.sh"), ref])
     table = {}
     with open(os.path.join(ref, "test", "test.cpp")) as f:

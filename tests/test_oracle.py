@@ -82,12 +82,21 @@ def test_sign_ordered_ties_match_reference_fixture(entry):
 @pytest.mark.parametrize("index", range(8))
 def test_sign_ordered_ties_bounded_on_workload(index):
     """On canvases of the many-canvas workload the two tie orders differ by
-    float rounding only: within 1 LSB wherever alpha is above 2/255 (an
-    unpremultiply of a smaller alpha magnifies the last bit of the float)."""
+    float rounding only.  What holds at every pixel:
+      * the alpha byte is within 1 LSB;
+      * the colour bytes are within 1 LSB wherever alpha is above 2/255;
+      * where alpha is 2/255 or less, get_image_data divides the colour by
+        alpha (hpp:3348-3381), which magnifies the last bit of the float by
+        up to 255x at alpha 1/255: the colour bytes there are bounded by
+        2 LSB, the largest difference seen on 256 workload canvases, and
+        such pixels are at most 2/255 opaque.
+    And at least 99.5% of the pixels are identical."""
     tb = scenes.c3_canvas(index * 37)
     a = np.frombuffer(oracle.replay(tb, ties="sign")[0], np.uint8).reshape(-1, 4).astype(np.int16)
     b = np.frombuffer(oracle.replay(tb)[0], np.uint8).reshape(-1, 4).astype(np.int16)
-    d = np.abs(a - b).max(axis=1)
+    d = np.abs(a - b)
+    assert d[:, 3].max(initial=0) <= 1
     opaque = np.minimum(a[:, 3], b[:, 3]) > 2
     assert d[opaque].max(initial=0) <= 1
-    assert (d != 0).mean() <= 0.005
+    assert d[~opaque].max(initial=0) <= 2
+    assert (d.max(axis=1) != 0).mean() <= 0.005
