@@ -46,6 +46,17 @@ thread_local int g_deferred = 0;        // contexts created now queue their read
 thread_local int g_thread_status = 0;   // first failure in this thread since the last take
 int g_strip_pixels = 4096;              // strip size of the tile engine (autotuned)
 int g_strip_threads = 256;
+// Coverage of the tile engine's draws: 0 binned (fixed-point accumulation in
+// shared memory, within the parity tolerance), 1 exact (row-sorted runs, the
+// reference's float sums bit for bit).  Read when a frame is prepared.
+std::atomic<int> g_coverage{0};
+// Binned strips keep 20 B per pixel in shared memory (float4 pixels and an
+// int32 accumulation image): at most this many pixels per strip.
+constexpr int kBinnedMaxStrip = 9216;
+constexpr size_t kMaxStripSmem = 226 * 1024;   // dynamic shared memory of one strip block (of 227 KiB)
+constexpr int kBinnedMaxRows = 256;             // rows of a binned strip
+// Rows per bin band of a binned canvas W pixels wide: about 2048 pixels.
+inline int band_rows(int W) { return std::max(1, 2048 / std::max(1, W)); }
 
 void note_thread_status(int rc) {
     if (rc && g_thread_status == 0) g_thread_status = rc;
@@ -371,14 +382,18 @@ struct frame {
     int64_t pass_n[5] = {};    // clip pass sizes (input of pass 0 .. output of pass 3)
     int n_items = 0;
     int strip_pixels = 4096;
+    // Binned coverage (tile engine): draws' segments go to row-band bins.
+    bool binned = false;
+    int64_t n_bins = 0, n_bin_entries = 0;
     // device
     dbuf arena, flat_pts, flat_prev, item_cnt, item_off, pat_f4, jobs_dev, boxes;
     dbuf row_cnt, row_off, row_cur, row_len, row_meta, long_rows, n_long, runs, sums;
+    dbuf bin_cnt, bin_cur, bin_off, bin_seg;
     dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
     dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, st_err, pc_cnt, pc_base, pc_list, wk_cnt, wk_base,
         wk_chunks, jn_cnt, jn_alpha, jn_sum, jn_off, st_goff;
-    hbuf staging, offs_host, rowoff_host, get_host, stoff_host;
+    hbuf staging, offs_host, rowoff_host, get_host, stoff_host, binoff_host;
     char *d = nullptr;
     size_t o_cmd = 0, o_hpts = 0, o_hprev = 0, o_bez = 0, o_items = 0, o_soff = 0, o_scol = 0, o_tex = 0, o_put = 0;
     size_t o_groups = 0, o_styles = 0, o_dash = 0;
@@ -406,6 +421,24 @@ struct frame {
     const float *last_lut = nullptr;
     int launch_strips();
     int build_strips();
+    // The strip kernel instance for the frame's coverage and block size, and
+    // its shared memory: 16 B per pixel, 24 B when binned.
+    using strip_fn = void (*)(strip_params);
+    strip_fn strip_kernel() const {
+        if (binned)
+            return strip_threads == 128 ? k_strips<128, true> : strip_threads == 512 ? k_strips<512, true>
+                                                                                      : k_strips<256, true>;
+        return strip_threads == 128 ? k_strips<128, false> : strip_threads == 512 ? k_strips<512, false>
+                                                                                   : k_strips<256, false>;
+    }
+    // Shared memory of a strip: 16 B per pixel; binned adds an int32 per
+    // pixel and a chunk mask per row.
+    int strip_cap = 0, strip_rows = 0;   // pixels and rows of the largest strip
+    size_t strip_smem() const {
+        if (!binned) return static_cast<size_t>(strip_cap) * sizeof(float4);
+        return static_cast<size_t>(strip_cap) * (sizeof(float4) + sizeof(int32_t)) +
+               static_cast<size_t>(strip_rows) * sizeof(uint32_t);
+    }
     void drop_graph() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
@@ -443,6 +476,8 @@ struct frame {
         nc_segs = cl_points = 0;
         for (int64_t &v : pass_n) v = 0;
         n_items = 0;
+        binned = false;
+        n_bins = n_bin_entries = 0;
         sized = ext_built = strips_built = false;
         n_runs = main_runs = main_rows = h2d_bytes = 0;
     }
@@ -455,10 +490,11 @@ struct frame {
                      &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev, &dash_cnt, &dash_off, &dash_pts,
                      &dash_subs, &dash_nsub, &st_err, &pc_cnt, &pc_base, &pc_list, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt,
-                     &jn_alpha, &jn_sum, &jn_off, &st_goff};
+                     &jn_alpha, &jn_sum, &jn_off, &st_goff, &bin_cnt, &bin_cur, &bin_off, &bin_seg};
         for (dbuf *x : b) x->release();
         staging.release();
         stoff_host.release();
+        binoff_host.release();
         offs_host.release();
         rowoff_host.release();
         get_host.release();
@@ -872,6 +908,9 @@ int frame::prepare() {
     };
     gather();
     std::vector<command> &cmds = all.cmds;
+    binned = engine == 0 && g_coverage.load() == 0;
+    for (cy_ctx *c : cvs)
+        if (c->W > kBinnedMaxStrip) binned = false;   // its strips would not fit in shared memory
     for (cy_ctx *c : cvs) {
         for (auto &m : c->dead) m.free_all();
         c->dead.clear();
@@ -963,21 +1002,31 @@ int frame::prepare() {
     }
     // Scan-conversion jobs: shadow pass (padded canvas) and main pass of each
     // draw, and the path of each clip.
-    auto add_job = [&](const command &c, int rows_n, int cols_n, float wd, float ht, float ox, float oy) {
+    // A binned job (a draw's own coverage on the tile engine) gets row-band
+    // bins instead of rows of runs.
+    auto add_job = [&](const command &c, int rows_n, int cols_n, float wd, float ht, float ox, float oy,
+                       bool to_bins = false) {
         scan_job j;
         std::memset(&j, 0, sizeof(j));
         j.geom = c.geom;
         j.line_first = c.line_first;
         j.seg_count = c.line_count;
         j.clip = needs_clip(c, wd, ht, ox, oy) ? 1 : 0;
-        j.row_base = static_cast<int32_t>(total_rows);
         j.rows = rows_n;
         j.cols = cols_n;
         j.width = wd;
         j.height = ht;
         j.offx = ox;
         j.offy = oy;
-        total_rows += rows_n;
+        if (to_bins) {
+            j.binned = 1;
+            j.band_h = band_rows(cols_n - 2);
+            j.bin_base = static_cast<int32_t>(n_bins);
+            n_bins += (rows_n + j.band_h - 1) / j.band_h;
+        } else {
+            j.row_base = static_cast<int32_t>(total_rows);
+            total_rows += rows_n;
+        }
         total_segs += c.line_count;
         jobs.push_back(j);
         return static_cast<int>(jobs.size()) - 1;
@@ -1011,7 +1060,8 @@ int frame::prepare() {
             sjobs.push_back(s);
         }
         if (c.kind == CMD_FILL || c.kind == CMD_CLIP)
-            main_job[i] = add_job(c, H, W + 2, static_cast<float>(W), static_cast<float>(H), 0.0f, 0.0f);
+            main_job[i] = add_job(c, H, W + 2, static_cast<float>(W), static_cast<float>(H), 0.0f, 0.0f,
+                                  binned && c.kind == CMD_FILL);
         if (c.kind == CMD_CLIP) jobs[main_job[i]].need_box = 1;
         if (c.kind == CMD_CLIP) {
             int lv = level_of_cv[cmd_cv[i]]++;
@@ -1019,7 +1069,8 @@ int frame::prepare() {
             max_level = std::max(max_level, lv);
         }
     }
-    if (total_rows > INT32_MAX / 2 || total_segs > INT32_MAX / 2) return fail(CY_ENOMEM, __LINE__);
+    if (total_rows > INT32_MAX / 2 || total_segs > INT32_MAX / 2 || n_bins > INT32_MAX / 2)
+        return fail(CY_ENOMEM, __LINE__);
     for (size_t ji = 0; ji < jobs.size(); ++ji) {
         const scan_job &j = jobs[ji];
         if (j.seg_count <= 0) continue;
@@ -1053,6 +1104,12 @@ int frame::prepare() {
             !ok(cudaMemsetAsync(row_cnt.p, 0, (nr + 1) * 4, stream)) ||
             !ok(cudaMemsetAsync(row_cur.p, 0, (nr + 1) * 4, stream)))
             return status;
+    }
+    if (n_bins > 0) {
+        size_t nb = static_cast<size_t>(n_bins);
+        if (!bin_cnt.ensure((nb + 1) * 4) || !bin_cur.ensure((nb + 1) * 4) || !bin_off.ensure((nb + 2) * 8) ||
+            !binoff_host.ensure(8))
+            return fail(CY_ENOMEM, __LINE__);
     }
     if (!sjobs.empty()) {
         if (!sj_dev.ensure(sjobs.size() * sizeof(cyg::shadow_job)) ||
@@ -1162,18 +1219,44 @@ int frame::run() {
         if (segs_cl > 0) k_runs<false, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl, spw_cl);
         rc = scan64(row_cnt.as<int32_t>(), row_off.as<int64_t>(), static_cast<int>(nr) + 1);
         if (rc) return rc;
+        // Binned draws: count each bin's segments, then place the bins.
+        bin_tables bt;
+        std::memset(&bt, 0, sizeof(bt));
+        const size_t nb = static_cast<size_t>(n_bins);
+        auto bin_grid = [](int segs) { return std::max(1, std::min((segs + 255) / 256, 152 * 8)); };
+        if (nb > 0) {
+            bt.cnt = bin_cnt.as<int32_t>();
+            bt.cur = bin_cur.as<int32_t>();
+            bt.off = bin_off.as<int64_t>();
+            if (!ok(cudaMemsetAsync(bin_cnt.p, 0, (nb + 1) * 4, stream)) ||
+                !ok(cudaMemsetAsync(bin_cur.p, 0, (nb + 1) * 4, stream)))
+                return status;
+            if (segs_nc > 0) k_bin<false, false><<<bin_grid(segs_nc), 256, 0, stream>>>(t, bt, segs_nc);
+            if (segs_cl > 0) k_bin<false, true><<<bin_grid(segs_cl), 256, 0, stream>>>(t, bt, segs_cl);
+            rc = scan64(bin_cnt.as<int32_t>(), bin_off.as<int64_t>(), static_cast<int>(nb) + 1);
+            if (rc) return rc;
+            launches += 2 + (segs_nc > 0 ? 2 : 0) + (segs_cl > 0 ? 2 : 0) + scan_launch_count(static_cast<int64_t>(nb) + 1);
+        }
         if (!sized) {
             sized = true;
-            // First run: size the run store and the new clip masks from the counts.
+            // First run: size the run store, the bins and the new clip masks from the counts.
             if (!ok(cudaMemcpyAsync(rowoff_host.p, row_off.p, (nr + 1) * 8, cudaMemcpyDeviceToHost, stream)) ||
+                (nb > 0 && !ok(cudaMemcpyAsync(binoff_host.p, bin_off.as<int64_t>() + nb, 8, cudaMemcpyDeviceToHost,
+                                               stream))) ||
                 !ok(cudaStreamSynchronize(stream)))
                 return status;
+            if (nb > 0) {
+                n_bin_entries = *static_cast<const int64_t *>(binoff_host.p);
+                if (n_bin_entries < 0) return fail(CY_ENOMEM, __LINE__);
+                if (!bin_seg.ensure(static_cast<size_t>(n_bin_entries + 1) * sizeof(float4)))
+                    return fail(CY_ENOMEM, __LINE__);
+            }
             const int64_t *rowoff_h = static_cast<const int64_t *>(rowoff_host.p);
             int64_t nruns = rowoff_h[nr];
             if (nruns < 0) return fail(CY_ENOMEM, __LINE__);
             n_runs = nruns;
             for (size_t i = 0; i < cmds.size(); ++i) {
-                if (cmds[i].kind != CMD_FILL || main_job[i] < 0) continue;
+                if (cmds[i].kind != CMD_FILL || main_job[i] < 0 || jobs[main_job[i]].binned) continue;
                 const scan_job &mj = jobs[main_job[i]];
                 main_runs += rowoff_h[mj.row_base + mj.rows] - rowoff_h[mj.row_base];
                 main_rows += mj.rows;
@@ -1200,6 +1283,11 @@ int frame::run() {
         t.runs = runs.as<cyg::run>();
         if (segs_nc > 0) k_runs<true, false><<<grid_nc, kRunsWarps * 32, 0, stream>>>(t, segs_nc, spw_nc);
         if (segs_cl > 0) k_runs<true, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl, spw_cl);
+        if (nb > 0) {
+            bt.seg = bin_seg.as<float4>();
+            if (segs_nc > 0) k_bin<true, false><<<bin_grid(segs_nc), 256, 0, stream>>>(t, bt, segs_nc);
+            if (segs_cl > 0) k_bin<true, true><<<bin_grid(segs_cl), 256, 0, stream>>>(t, bt, segs_cl);
+        }
         int rgrid = static_cast<int>(std::min<size_t>((nr + kRowsWarps - 1) / kRowsWarps, 152 * 32));
         if (!ok(cudaMemsetAsync(n_long.p, 0, 4, stream))) return status;
         k_rows<<<std::max(rgrid, 1), kRowsWarps * 32, 0, stream>>>(
@@ -1292,6 +1380,8 @@ int frame::run() {
             const command &c = cmds[i];
             cy_ctx *cv = cvs[cmd_cv[i]];
             e.main_row_base = main_job[i] >= 0 ? jobs[main_job[i]].row_base : 0;
+            e.bin_base = main_job[i] >= 0 ? jobs[main_job[i]].bin_base : 0;
+            e.band_h = main_job[i] >= 0 && jobs[main_job[i]].band_h > 0 ? jobs[main_job[i]].band_h : 1;
             e.has_shadow = shadow_job[i] >= 0;
             e.shadow_img = 0;
             if (e.has_shadow)
@@ -1383,8 +1473,11 @@ int frame::run() {
 int frame::build_strips() {
     strips_built = true;
     strip_pixels = g_strip_pixels;
+    if (binned) strip_pixels = std::min(strip_pixels, kBinnedMaxStrip);
     strip_threads = g_strip_threads;
-    size_t smem = static_cast<size_t>(strip_pixels) * sizeof(float4);
+    const int nwarps = (strip_threads == 128 || strip_threads == 512 ? strip_threads : 256) / 32;
+    strip_cap = 0;
+    strip_rows = 0;
     scv.resize(cvs.size());
     std::vector<std::pair<int64_t, int2>> work;
     int cursor = 0;
@@ -1395,6 +1488,16 @@ int frame::build_strips() {
         s.W = cv->W;
         s.H = cv->H;
         s.TH = std::max(1, std::min(cv->H, strip_pixels / std::max(1, cv->W)));
+        if (binned) {
+            // Binned warps own whole rows: at least one row per warp, and a
+            // multiple of the warps, while the strip fits in shared memory.
+            int th = std::min(std::max(s.TH, nwarps), kBinnedMaxRows);
+            if (th > nwarps) th -= th % nwarps;
+            const int fit = static_cast<int>((kMaxStripSmem - kBinnedMaxRows * 4) / (static_cast<size_t>(cv->W) * 20));
+            s.TH = std::max(1, std::min({th, cv->H, fit}));
+        }
+        strip_cap = std::max(strip_cap, s.TH * s.W);
+        strip_rows = std::max(strip_rows, s.TH);
         s.cmd_first = cursor;
         s.cmd_count = static_cast<int32_t>(cv->q.cmds.size());
         cursor += s.cmd_count;
@@ -1423,9 +1526,11 @@ int frame::build_strips() {
     if (!ext.empty() && !ok(cudaMemcpyAsync(ext_dev.p, ext.data(), ext.size() * sizeof(strip_cmd),
                                             cudaMemcpyHostToDevice, stream)))
         return status;
-    if (!ok(cudaFuncSetAttribute(k_strips<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))) ||
-        !ok(cudaFuncSetAttribute(k_strips<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))) ||
-        !ok(cudaFuncSetAttribute(k_strips<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))))
+    // The attribute is per kernel, shared by every frame in every thread:
+    // always the largest strip any frame may launch (a launch uses its own).
+    if (strip_smem() > kMaxStripSmem) return fail(CY_EINVAL, __LINE__);
+    if (!ok(cudaFuncSetAttribute(strip_kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(kMaxStripSmem))))
         return status;
     return CY_OK;
 }
@@ -1434,7 +1539,7 @@ int frame::build_strips() {
 // inputs of the last run.
 int frame::launch_strips() {
     if (n_items == 0) return CY_OK;
-    size_t smem = static_cast<size_t>(strip_pixels) * sizeof(float4);
+    size_t smem = strip_smem();
     if (!ok(cudaMemsetAsync(counter.p, 0, 4, stream))) return status;
     strip_params P;
     P.canvases = scv_dev.as<strip_canvas>();
@@ -1450,9 +1555,12 @@ int frame::launch_strips() {
     P.put_px = last_put;
     P.lut = last_lut;
     P.get_buf = get_dev.as<uint8_t>();
-    P.strip_pixels = strip_pixels;
+    P.strip_pixels = strip_cap;
+    P.strip_rows = strip_rows;
+    P.bin_off = bin_off.p ? bin_off.as<int64_t>() : nullptr;
+    P.bin_seg = bin_seg.p ? bin_seg.as<float4>() : nullptr;
     int per_sm = 0, dev = 0, sms = 152;
-    auto kern = strip_threads == 128 ? k_strips<128> : strip_threads == 512 ? k_strips<512> : k_strips<256>;
+    auto kern = strip_kernel();
     int threads = strip_threads == 128 || strip_threads == 512 ? strip_threads : 256;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     cudaGetDevice(&dev);
@@ -1914,6 +2022,8 @@ int queue_stroke(cy_ctx *c, const float *points, const int *counts, const int *c
 extern "C" {
 
 void cy_set_engine(int engine) { g_engine = engine; }
+void cy_set_coverage(int exact) { g_coverage.store(exact ? 1 : 0); }
+int cy_get_coverage(void) { return g_coverage.load(); }
 void cy_set_deferred(int deferred) { g_deferred = deferred; }
 void cy_set_strip_config(int pixels, int threads) {
     if (pixels >= 256 && pixels <= 12288) g_strip_pixels = pixels;
@@ -2473,7 +2583,7 @@ int cy_frame_autotune(cy_frame *fr, int *best_pixels, int *best_threads, float *
     f.drop_graph();
     int rc = CY_OK;
     for (int px : pixels) {
-        if (px < max_w) continue;
+        if (px < max_w || (f.binned && px > kBinnedMaxStrip)) continue;
         for (int th : threads) {
             g_strip_pixels = px;
             g_strip_threads = th;
@@ -2598,7 +2708,8 @@ int cy_frame_stats(cy_frame *fr, long long *stats, int n) {
     for (cy_ctx *c : f.cvs) pixels += static_cast<long long>(c->W) * c->H;
     long long v[] = {pixels, static_cast<long long>(f.all.cmds.size()), f.nc_segs + f.pass_n[4], f.n_runs, f.total_rows,
                      f.main_runs, f.main_rows, f.shadow_floats, f.get_total, f.h2d_bytes, f.launches,
-                     static_cast<long long>(f.sjobs.size()), static_cast<long long>(f.clips.size())};
+                     static_cast<long long>(f.sjobs.size()), static_cast<long long>(f.clips.size()),
+                     f.n_bin_entries, f.binned ? 1LL : 0LL};
     int m = static_cast<int>(sizeof(v) / sizeof(v[0]));
     for (int i = 0; i < n && i < m; ++i) stats[i] = v[i];
     return m;

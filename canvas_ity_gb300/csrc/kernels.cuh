@@ -162,7 +162,9 @@ struct scan_job {
     float width, height;   // clip rectangle [0,width] x [0,height]
     float offx, offy;      // added to every point first (shadow offset)
     int32_t need_box;      // 1: track the exact bounds of nonzero cells
-    int32_t pad;
+    int32_t binned;        // 1: segments go to row-band bins (k_bin) instead of runs
+    int32_t bin_base;      // binned: first bin of this job
+    int32_t band_h;        // binned: rows per band
 };
 
 // Segment ranges of a list of jobs: entry i = (first segment, job index),
@@ -322,6 +324,81 @@ struct job_tables {
     run *runs;
 };
 
+// Segment s of the scan (its end points moved by the job's offset, as scan
+// does with add(offset, point), hpp:2205) clamped to the job's rectangle as
+// scan does before add_runs (hpp:2236-2238).  Returns the job index.
+template <bool CLIPPED>
+__device__ __forceinline__ int segment_of(const job_tables &t, int s, float2 &a, float2 &b) {
+    int ji;
+    if (CLIPPED) {
+        ji = t.cl_job[s];
+        a = t.cl_pts[t.cl_prev[s]];
+        b = t.cl_pts[s];
+    } else {
+        int c = table_find(t.tab, t.n_tab, s);
+        ji = t.tab[c].y;
+        const scan_job &jj = t.jobs[ji];
+        int k = jj.line_first + (s - t.tab[c].x);
+        int g = jj.geom ? 1 : 0;
+        float2 pb = t.pts[g][k];
+        float2 pa = t.pts[g][t.prev[g][k]];
+        a = f2(jj.offx + pa.x, jj.offy + pa.y);
+        b = f2(jj.offx + pb.x, jj.offy + pb.y);
+    }
+    const scan_job &j = t.jobs[ji];
+    a = f2(lo(hi(a.x, 0.0f), j.width), lo(hi(a.y, 0.0f), j.height));
+    b = f2(lo(hi(b.x, 0.0f), j.width), lo(hi(b.y, 0.0f), j.height));
+    return ji;
+}
+
+// Rows of the job that a segment's cell walk touches: [r0, r1] (empty when
+// r0 > r1).  Row k of the walk is dda_row_index(p, k), k < nrows, and rows
+// outside [0, rows) contribute nothing (as in k_runs).
+__device__ __forceinline__ void dda_rows(const dda_piece &p, int rows, int &r0, int &r1) {
+    int n = p.nrows < rows + 2 ? p.nrows : rows + 2;
+    int a = dda_row_index(p, 0), b = dda_row_index(p, n - 1);
+    r0 = max(min(a, b), 0);
+    r1 = min(max(a, b), rows - 1);
+}
+
+// ------------------------------------------------------ row-band binning
+// The sort-free coverage path: instead of runs, every segment of a binned
+// job is listed in each band of rows it crosses (band_h rows per band, bins
+// of one job consecutive), as its clamped end points.  The tile kernel then
+// accumulates the signed areas of one strip's bands in shared memory.
+// Pass 1 counts entries per bin, pass 2 (after a scan) writes them.
+struct bin_tables {
+    int32_t *cnt;          // per bin: entries (count pass)
+    int32_t *cur;          // per bin: write cursor (emit pass)
+    const int64_t *off;    // per bin: first entry (exclusive scan of cnt)
+    float4 *seg;           // entries: (a.x, a.y, b.x, b.y)
+};
+
+template <bool EMIT, bool CLIPPED>
+__global__ void k_bin(job_tables t, bin_tables bt, int total_segments) {
+    int stride = gridDim.x * blockDim.x;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < total_segments; s += stride) {
+        float2 a, b;
+        int ji = segment_of<CLIPPED>(t, s, a, b);
+        const scan_job &j = t.jobs[ji];
+        if (!j.binned) continue;
+        dda_piece p;
+        if (!dda_setup(a, b, p)) continue;
+        int r0, r1;
+        dda_rows(p, j.rows, r0, r1);
+        if (r0 > r1) continue;
+        for (int band = r0 / j.band_h; band <= r1 / j.band_h; ++band) {
+            int bin = j.bin_base + band;
+            if (!EMIT) {
+                atomicAdd(bt.cnt + bin, 1);
+            } else {
+                int64_t at = bt.off[bin] + atomicAdd(bt.cur + bin, 1);
+                if (at < bt.off[bin + 1]) bt.seg[at] = make_float4(a.x, a.y, b.x, b.y);
+            }
+        }
+    }
+}
+
 // Segments go to warps 32 at a time: each lane prepares one segment
 // (clamped to its job's rectangle as scan does before add_runs,
 // hpp:2236-2238), then the warp deals all rows of the 32 segments out to its
@@ -345,25 +422,9 @@ __global__ void __launch_bounds__(kRunsWarps * 32) k_runs(job_tables t, int tota
         p.nrows = 0;
         if (lane < seg_per_warp && s < total_segments) {
             float2 a, b;
-            if (CLIPPED) {
-                ji = t.cl_job[s];
-                a = t.cl_pts[t.cl_prev[s]];
-                b = t.cl_pts[s];
-            } else {
-                int c = table_find(t.tab, t.n_tab, s);
-                ji = t.tab[c].y;
-                const scan_job &jj = t.jobs[ji];
-                int k = jj.line_first + (s - t.tab[c].x);
-                int g = jj.geom ? 1 : 0;
-                float2 pb = t.pts[g][k];
-                float2 pa = t.pts[g][t.prev[g][k]];
-                a = f2(jj.offx + pa.x, jj.offy + pa.y);
-                b = f2(jj.offx + pb.x, jj.offy + pb.y);
-            }
+            ji = segment_of<CLIPPED>(t, s, a, b);
             const scan_job &j = t.jobs[ji];
-            a = f2(lo(hi(a.x, 0.0f), j.width), lo(hi(a.y, 0.0f), j.height));
-            b = f2(lo(hi(b.x, 0.0f), j.width), lo(hi(b.y, 0.0f), j.height));
-            if (dda_setup(a, b, p)) rows_here = p.nrows < j.rows + 2 ? p.nrows : j.rows + 2;
+            if (!j.binned && dda_setup(a, b, p)) rows_here = p.nrows < j.rows + 2 ? p.nrows : j.rows + 2;
         }
         int incl = rows_here;
 #pragma unroll
@@ -392,6 +453,9 @@ __global__ void __launch_bounds__(kRunsWarps * 32) k_runs(job_tables t, int tota
             dda_span(pp, k, entry, ex, ps, pe);
             int row = dda_row_index(pp, k);
             if (row < 0 || row >= j.rows) continue;
+            // cells of a clamped segment lie in [0, cols]; other spans come
+            // from non-finite input and are skipped
+            if (!(ps >= 0 && pe >= ps && pe <= j.cols)) continue;
             int n = pe - ps + 2;
             int grow = j.row_base + row;
             if (!EMIT) {

@@ -26,7 +26,9 @@ struct strip_canvas {
 };
 
 struct strip_cmd {            // per command extras resolved at the flush
-    int32_t main_row_base;    // rows of the command's main scan job
+    int32_t main_row_base;    // rows of the command's main scan job (sorted-run coverage)
+    int32_t bin_base;         // binned coverage: first row-band bin of the main job
+    int32_t band_h;           // binned coverage: rows per band
     int32_t has_shadow;
     int64_t shadow_img;       // float offset of the blurred shadow image
     const float *vis;         // clip visibility (null: whole canvas)
@@ -48,14 +50,172 @@ struct strip_params {
     const uint8_t *put_px;
     const float *lut;
     uint8_t *get_buf;
-    int strip_pixels;
+    int strip_pixels;         // pixels of the largest strip (shared memory per strip)
+    int strip_rows;           // binned: rows of the tallest strip (one chunk mask each)
+    const int64_t *bin_off;   // binned coverage: first entry of each bin (and the end)
+    const float4 *bin_seg;    // binned coverage: segment end points
 };
 
-template <int THREADS>
+// ------------------------------------------------- binned coverage (strips)
+// Signed areas are accumulated in shared memory as 32-bit fixed point with
+// kAccBits fractional bits.  A lane walks one row of one segment the way
+// add_runs does (hpp:2131-2169) and keeps the running total C of the deltas
+// it has produced (C after cell m = sign * (sum of strips up to m - area of
+// m)); it adds round(C * 2^kAccBits) minus what it added before, so the
+// integers of a segment row telescope to its rounded total and the prefix
+// sum of a pixel row is off by at most half a unit per segment row to its
+// left.  Integer adds commute, so the result does not depend on the order in
+// which lanes and warps get there.  Windings beyond +-2^(31-kAccBits) wrap:
+// coverage is only wrong where the winding is a nonzero multiple of
+// 2^(32-kAccBits) (1024 overlapping layers of one path).
+static constexpr int kAccBits = 22;
+static constexpr float kAccScale = 4194304.0f;          // 2^kAccBits
+static constexpr float kAccInv = 1.0f / 4194304.0f;
+
+// Accumulate row k of segment piece p into acc (row ly of the strip, W
+// cells), and widen the strip extents (row and column range touched).
+__device__ __forceinline__ void raster_row(const dda_piece &p, int k, int *row_acc, int W, int &xlo, int &xhi) {
+    float2 entry = k == 0 ? f2(p.fx, p.fy) : dda_exit(p, k - 1);
+    float2 ex = dda_exit(p, k);
+    int ps, pe;
+    dda_span(p, k, entry, ex, ps, pe);
+    // Segments are clamped to [0, W] x [0, H], so a row's cells lie in
+    // [0, W + 1]; anything else comes from non-finite input: skipped.
+    if (!(ps >= 0 && pe >= ps && pe <= W + 1)) return;
+    float2 now = entry;
+    float total = 0.0f;
+    int qprev = 0;
+    for (int m = ps; m <= pe + 1; ++m) {
+        float c;
+        if (m < pe) {
+            float2 X;
+            if (!p.vert) {
+                float cx = static_cast<float>(m + 1);
+                X = f2(cx, (cx - p.fx) * p.sy + p.fy);
+            } else {
+                X = f2(p.tx, p.ty);
+            }
+            float strip = lo(hi((X.y - now.y) * p.ystep, 0.0f), 1.0f);
+            float mid = (X.x + now.x) * 0.5f;
+            float area = (mid - static_cast<float>(m)) * strip;
+            total += strip;
+            c = (total - area) * p.sign;
+            now = X;
+        } else if (m == pe) {
+            float strip = lo(hi((ex.y - now.y) * p.ystep, 0.0f), 1.0f);
+            float mid = (ex.x + now.x) * 0.5f;
+            float area = (mid - static_cast<float>(pe)) * strip;
+            total += strip;
+            c = (total - area) * p.sign;
+        } else {
+            c = total * p.sign;
+        }
+        int q = __float2int_rn(c * kAccScale);
+        int dq = q - qprev;
+        qprev = q;
+        if (dq != 0 && m >= 0 && m < W) {
+            atomicAdd(row_acc + m, dq);
+            xlo = min(xlo, m);
+            xhi = max(xhi, m);
+        }
+    }
+}
+
+// One warp's share of a draw: the entries of the draw's bins whose bands
+// overlap the warp's own strip rows [r0, r1) (local); 32 entries at a time
+// each lane prepares one segment, the (segment, row) pairs inside the
+// warp's rows are dealt to the lanes, and each lane accumulates its row.
+// rmask[ly] gets a bit per group of g chunks (32 pixels each) that the row
+// touched.
+__device__ void raster_rows(const strip_params &P, const strip_cmd &e, int W, int H, int y0, int r0, int r1,
+                            int *acc, unsigned *rmask, int g, int lane) {
+    const int band_h = e.band_h;
+    const int ya = y0 + r0, yb = min(y0 + r1, H) - 1;   // canvas rows owned
+    if (ya > yb) return;
+    const int b0 = ya / band_h, b1 = yb / band_h;
+    const int64_t *off = P.bin_off + e.bin_base;
+    const int64_t first = off[b0], last = off[b1 + 1];
+    for (int64_t base = first; base < last; base += 32) {
+        const int64_t ei = base + lane;
+        int cnt = 0, klo = 0;
+        float4 sg = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (ei < last) {
+            sg = P.bin_seg[ei];
+            int band = b0;
+            while (band < b1 && ei >= off[band + 1]) ++band;
+            // owned rows inside the entry's band
+            int ylo = max(ya, band * band_h), yhi = min(yb, (band + 1) * band_h - 1);
+            dda_piece p;
+            if (ylo <= yhi && dda_setup(f2(sg.x, sg.y), f2(sg.z, sg.w), p)) {
+                int n = p.nrows < H + 2 ? p.nrows : H + 2;
+                int py0 = static_cast<int>(p.py0);
+                int k0 = p.up ? ylo - py0 : py0 - yhi;
+                int k1 = p.up ? yhi - py0 : py0 - ylo;
+                k0 = max(k0, 0);
+                k1 = min(k1, n - 1);
+                if (k0 <= k1) {
+                    cnt = k1 - k0 + 1;
+                    klo = k0;
+                }
+            }
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int q0 = 0; q0 < total; q0 += 32) {
+            const int q = q0 + lane;
+            // the lane whose inclusive end first exceeds q owns pair q
+            int lo_i = 0, hi_i = 31;
+#pragma unroll
+            for (int it = 0; it < 5; ++it) {
+                int mid = (lo_i + hi_i) >> 1;
+                int v = __shfl_sync(0xffffffffu, incl, mid);
+                if (v > q) hi_i = mid; else lo_i = mid + 1;
+            }
+            const int src = lo_i;
+            float ax = __shfl_sync(0xffffffffu, sg.x, src), ay = __shfl_sync(0xffffffffu, sg.y, src);
+            float bx = __shfl_sync(0xffffffffu, sg.z, src), by = __shfl_sync(0xffffffffu, sg.w, src);
+            int s_incl = __shfl_sync(0xffffffffu, incl, src), s_cnt = __shfl_sync(0xffffffffu, cnt, src);
+            int s_klo = __shfl_sync(0xffffffffu, klo, src);
+            if (q < total) {
+                dda_piece p;
+                dda_setup(f2(ax, ay), f2(bx, by), p);
+                int k = s_klo + (q - (s_incl - s_cnt));
+                int ly = dda_row_index(p, k) - y0;
+                int x0 = 0x7fffffff, x1 = -1;
+                raster_row(p, k, acc + ly * W, W, x0, x1);
+                if (x0 <= x1) {
+                    int g0 = (x0 >> 5) / g, g1 = (x1 >> 5) / g;
+                    unsigned bits = (g1 >= 31 ? 0xffffffffu : ((2u << g1) - 1u)) & ~((1u << g0) - 1u);
+                    atomicOr(rmask + ly, bits);
+                }
+            }
+        }
+    }
+}
+
+// BINNED selects the coverage of draws: false walks the row-sorted runs
+// (the float canvas is then the reference's bit for bit); true has each
+// warp accumulate the draw's binned segments over its own rows of the strip
+// in shared memory (raster_rows), then prefix-sum each row with shuffles
+// while it paints.  Binned warps own whole rows, so no barrier is needed
+// between draws.  Shared memory: the strip's float4 pixels, and for BINNED
+// an int32 accumulation image of the strip and one chunk mask per row.
+template <int THREADS, bool BINNED>
 __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
     extern __shared__ float4 px[];
     __shared__ int item_slot;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    int *acc = BINNED ? reinterpret_cast<int *>(px + P.strip_pixels) : nullptr;
+    unsigned *rmask = BINNED ? reinterpret_cast<unsigned *>(acc + P.strip_pixels) : nullptr;
+    if (BINNED) {   // zero once: each draw's paint clears what its raster wrote
+        for (int i = threadIdx.x; i < P.strip_pixels; i += blockDim.x) acc[i] = 0;
+        for (int i = threadIdx.x; i < P.strip_rows; i += blockDim.x) rmask[i] = 0;
+    }
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) item_slot = atomicAdd(P.counter, 1);
@@ -70,8 +230,10 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
         const int chunks = rows * cpr;
         // Each warp owns a contiguous range of chunks (row-major) for the
         // whole item, so every pixel is always touched by the same thread.
-        const int per = (chunks + nwarps - 1) / nwarps;
+        // Binned: whole rows per warp.
+        const int per = BINNED ? ((rows + nwarps - 1) / nwarps) * cpr : (chunks + nwarps - 1) / nwarps;
         const int cb = min(chunks, warp * per), ce = min(chunks, cb + per);
+        const int g = (cpr + 31) >> 5;           // binned: chunks per row-mask bit
         for (int ch = cb; ch < ce; ++ch) {
             int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
             if (x >= W) continue;
@@ -132,6 +294,63 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
                         px[ly * W + x] = blend(px[ly * W + x], fore, op, vis);
                     }
                 }
+            }
+            if (BINNED) {
+                if (cb >= ce || (!clearing && (c.gy1 < wy0 || c.gy0 > wy1))) continue;
+                const int r0 = cb / cpr, r1 = (ce - 1) / cpr + 1;
+                raster_rows(P, e, W, cv.H, y0, r0, r1, acc, rmask, g, lane);
+                __syncwarp();
+                for (int ly = r0; ly < r1; ++ly) {
+                    unsigned mask = 0;
+                    if (lane == 0) {
+                        mask = rmask[ly];
+                        rmask[ly] = 0;
+                    }
+                    mask = __shfl_sync(0xffffffffu, mask, 0);
+                    if (!clearing && !mask) continue;
+                    const int y = y0 + ly;
+                    int *arow = acc + ly * W;
+                    int carry = 0;
+                    // Chunks of a clear mask bit hold no accumulated area: the
+                    // sum there is the carry.  Where that is invisible the
+                    // walk jumps to the next marked chunk.
+                    for (int ch = 0; ch < cpr;) {
+                        const bool marked = (mask >> (ch / g)) & 1u;
+                        if (!marked && !clearing && cover_of(static_cast<float>(carry) * kAccInv, c.fill_rule) < kVisible) {
+                            unsigned rest = mask & ~((2u << (ch / g)) - 1u);
+                            if ((ch / g) >= 31 || !rest) break;
+                            ch = (__ffs(rest) - 1) * g;
+                            continue;
+                        }
+                        const int x = (ch << 5) + lane;
+                        int v = 0;
+                        if (marked && x < W) {
+                            v = arow[x];
+                            if (v) arow[x] = 0;
+                        }
+                        if (marked) {
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) {
+                                int t = __shfl_up_sync(0xffffffffu, v, o);
+                                if (lane >= o) v += t;
+                            }
+                        }
+                        const int sum = carry + v;
+                        if (marked) carry = __shfl_sync(0xffffffffu, sum, 31);
+                        ++ch;
+                        if (x >= W) continue;
+                        float cov = cover_of(static_cast<float>(sum) * kAccInv, c.fill_rule);
+                        float vis = e.vis ? e.vis[static_cast<size_t>(y) * W + x] : 1.0f;
+                        if ((cov >= kVisible || clearing) && vis >= kVisible) {
+                            float4 pp = paint_at(c, P.src, static_cast<float>(x) + 0.5f, static_cast<float>(y) + 0.5f);
+                            float kk = cov * c.alpha;
+                            float4 fore = make_float4(pp.x * kk, pp.y * kk, pp.z * kk, pp.w * kk);
+                            px[ly * W + x] = blend(px[ly * W + x], fore, op, vis);
+                        }
+                    }
+                }
+                __syncwarp();
+                continue;
             }
             // Rows [gy0, gy1] hold all of the draw's runs; elsewhere only a
             // clearing operation changes pixels.

@@ -49,6 +49,24 @@ def set_engine(engine: int) -> None:
     load().cy_set_engine(int(engine))
 
 
+def set_coverage(exact: bool) -> None:
+    """Coverage of the tile engine's draws for frames prepared afterwards:
+    binned fixed-point accumulation (False, the default; within the parity
+    tolerance) or the exact row-sorted runs (True; the float canvas is the
+    reference's bit for bit).  Applies to the whole process."""
+    lib = load()
+    lib.cy_set_coverage.restype = None
+    lib.cy_set_coverage.argtypes = [ctypes.c_int]
+    lib.cy_set_coverage(1 if exact else 0)
+
+
+def coverage_exact() -> bool:
+    lib = load()
+    lib.cy_get_coverage.restype = ctypes.c_int
+    lib.cy_get_coverage.argtypes = []
+    return bool(lib.cy_get_coverage())
+
+
 def set_device_stroke(on: bool) -> None:
     """Expand strokes on the GPU (True, the default) or on the host with the
     reference's own acosf/tanf (False); applies to the whole process."""
@@ -205,7 +223,8 @@ class Frame:
         return int(self.lib.cy_frame_stream(self.frame) or 0)
 
     STAT_NAMES = ("pixels", "commands", "segments", "runs", "rows", "draw_runs", "draw_rows",
-                  "shadow_floats", "read_bytes", "upload_bytes", "launches", "shadows", "clips")
+                  "shadow_floats", "read_bytes", "upload_bytes", "launches", "shadows", "clips",
+                  "bin_entries", "binned")
 
     def stats(self) -> dict:
         arr = (ctypes.c_longlong * len(self.STAT_NAMES))()

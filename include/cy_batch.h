@@ -28,8 +28,20 @@ struct cy_canvas;   /* canvas_ity_c.h */
 void cy_set_deferred(int deferred);
 
 /* Tile engine strip size in pixels (256..12288, shared memory is 16 B per
- * pixel) and threads per block (128, 256 or 512). */
+ * pixel, 24 B with binned coverage, which caps it at 9216) and threads per
+ * block (128, 256 or 512). */
 void cy_set_strip_config(int strip_pixels, int threads);
+
+/* Coverage of the tile engine's draws, for frames prepared afterwards in
+ * any thread.  0 (default), binned: each draw's segments are listed per band
+ * of rows and accumulated per strip in shared memory as fixed-point signed
+ * areas (add_runs' cell areas, hpp:2109-2170, with no sorted runs in
+ * memory); coverage is within 1e-5 of the reference's and RGBA8 within
+ * +-1 LSB.  1, exact: row-sorted runs summed in the reference's order
+ * (lines_to_runs and render_main, hpp:2193-2253, 2551-2605), so the float
+ * canvas is the reference's bit for bit.  The plain engine is always exact. */
+void cy_set_coverage(int exact);
+int cy_get_coverage(void);
 
 /* Build a frame over the queued work of n contexts, upload it and run it
  * once.  engine: 0 tile, 1 plain.  The contexts' queues are consumed by
@@ -81,7 +93,8 @@ int cy_frame_profile(cy_frame *frame, float *phase_ms, int n);
 
 /* Frame statistics (first n of): pixels, commands, segments, runs, rows,
  * runs of draws, rows of draws, shadow image floats, read-back bytes,
- * uploaded bytes, kernel launches per run, shadows, clips. */
+ * uploaded bytes, kernel launches per run, shadows, clips, binned segment
+ * entries, binned (1) or exact (0) coverage. */
 int cy_frame_stats(cy_frame *frame, long long *stats, int n);
 
 /* Replay n call lists (cy_trace.h) into n new canvases whose reads are

@@ -33,23 +33,28 @@ REFERENCE_ROOT = os.environ.get("CY_REFERENCE_ROOT")
 _FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
 
 
-def _variant(ties: str, trig: str) -> Tuple[str, list]:
+def _variant(ties: str, trig: str, coverage: str = "runs") -> Tuple[str, list]:
     name, extra = "libcy_oracle", []
     if ties == "sign":
         name, extra = name + "_sign", extra + ["-DCYO_TIES_BY_SIGN"]
     if trig == "cr":
         name, extra = name + "_cr", extra + ["-DCYO_CR_TRIG"]
+    if coverage == "binned":
+        name, extra = name + "_binned", extra + ["-DCYO_BINNED"]
     return os.path.join(BUILD_DIR, name + ".so"), extra
 
 
-def build(force: bool = False, ties: str = "reference", trig: str = "libm") -> str:
+def build(force: bool = False, ties: str = "reference", trig: str = "libm", coverage: str = "runs") -> str:
     """Compile the oracle restatement (fast: one translation unit).
 
     ties="sign" builds the variant whose sort orders equal-magnitude,
     opposite-sign runs of one cell negative first; trig="cr" the variant
-    whose round joins use correctly rounded acos/tan."""
+    whose round joins use correctly rounded acos/tan; coverage="binned" the
+    variant whose draws take the library's sort-free fixed-point coverage
+    instead of the reference's sorted runs (its distance from the reference
+    is what the tests bound)."""
     src = os.path.join(HERE, "cy_oracle.cpp")
-    out, extra = _variant(ties, trig)
+    out, extra = _variant(ties, trig, coverage)
     hdrs = [os.path.join(HERE, "..", "include", h) for h in ("cy_trace.h", "cy_replay.hpp")]
     newest = max(os.path.getmtime(p) for p in [src] + hdrs)
     if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
@@ -104,21 +109,24 @@ _oracles: dict = {}
 _ref: Optional[_Lib] = None
 
 
-def _get(ties: str, trig: str = "libm") -> _Lib:
-    if (ties, trig) not in _oracles:
-        _oracles[(ties, trig)] = _Lib(build(ties=ties, trig=trig), "cyo_replay")
-    return _oracles[(ties, trig)]
+def _get(ties: str, trig: str = "libm", coverage: str = "runs") -> _Lib:
+    key = (ties, trig, coverage)
+    if key not in _oracles:
+        _oracles[key] = _Lib(build(ties=ties, trig=trig, coverage=coverage), "cyo_replay")
+    return _oracles[key]
 
 
-def replay(trace: bytes, ties: str = "reference", trig: str = "libm") -> Tuple[bytes, List[float]]:
+def replay(trace: bytes, ties: str = "reference", trig: str = "libm",
+           coverage: str = "runs") -> Tuple[bytes, List[float]]:
     """Replay through the oracle: (concatenated get_image_data bytes, results)."""
-    return _get(ties, trig).replay(trace)
+    return _get(ties, trig, coverage).replay(trace)
 
 
-def replay_linear(trace: bytes, width: int, height: int, ties: str = "reference", trig: str = "libm"):
+def replay_linear(trace: bytes, width: int, height: int, ties: str = "reference", trig: str = "libm",
+                  coverage: str = "runs"):
     """Replay through the oracle; return the final float canvas (H, W, 4)."""
     import numpy as np
-    fn = _get(ties, trig).lib.cyo_replay_linear
+    fn = _get(ties, trig, coverage).lib.cyo_replay_linear
     fn.restype = ctypes.c_int
     fn.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t,
                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]

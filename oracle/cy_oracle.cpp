@@ -276,6 +276,12 @@ private:
     void stroke_outline();
     void scan_segment(vec2 from, vec2 to);
     void scan(vec2 offset, int padding);
+    // Binned coverage (built with CYO_BINNED): the library's sort-free
+    // coverage of a draw, restated -- fixed-point cell areas summed per
+    // pixel row instead of sorted runs.
+    std::vector<int32_t> acc;
+    void scan_segment_binned(vec2 from, vec2 to);
+    void scan_binned();
     col paint(vec2 p, const brush &br, bool clamp_edges);
     void render_shadow(const brush &br, bool clamp_edges);
     void render(const brush &br, bool clamp_edges);
@@ -1069,6 +1075,102 @@ void canvas::scan(vec2 offset, int padding) {
     runs.erase(runs.begin() + static_cast<ptrdiff_t>(to) + 1, runs.end());
 }
 
+// ---- binned coverage (the library's sort-free variant, CYO_BINNED) ----
+// The same cell walk as scan_segment (add_runs, hpp:2109-2170), but each
+// row keeps the running total C of the deltas it produced (C after cell m =
+// sign * (strips so far - area of m)) and adds round(C * 2^22) minus what
+// it added before, as 32-bit integers, into a per-pixel accumulation image.
+// Cells at x >= W or rows outside [0, H) are dropped.
+static const float kAccScale = 4194304.0f;   // 2^22
+static const float kAccInv = 1.0f / 4194304.0f;
+
+void canvas::scan_segment_binned(vec2 from, vec2 to) {
+    const float eps = 2.0e-5f;
+    if (fabsf(to.y - from.y) < eps) return;
+    float sign = to.y > from.y ? 1.0f : -1.0f;
+    if (from.x > to.x) std::swap(from, to);
+    vec2 now = from;
+    vec2 pixel = mk(floorf(now.x), floorf(now.y));
+    vec2 corner = add(pixel, mk(1.0f, to.y > from.y ? 1.0f : 0.0f));
+    vec2 slope = mk((to.x - from.x) / (to.y - from.y), (to.y - from.y) / (to.x - from.x));
+    vec2 nx = (to.x - from.x < eps) ? to : mk(corner.x, now.y + (corner.x - now.x) * slope.y);
+    vec2 ny = mk(now.x + (corner.y - now.y) * slope.x, corner.y);
+    if ((from.y < to.y && to.y < ny.y) || (from.y > to.y && to.y > ny.y)) ny = to;
+    float ystep = to.y > from.y ? 1.0f : -1.0f;
+    auto put = [&](float x, float y, int dq) {
+        int ix = static_cast<int>(x), iy = static_cast<int>(y);
+        if (dq != 0 && ix >= 0 && ix < W && iy >= 0 && iy < H)
+            acc[static_cast<size_t>(iy) * W + ix] = static_cast<int32_t>(
+                static_cast<uint32_t>(acc[static_cast<size_t>(iy) * W + ix]) + static_cast<uint32_t>(dq));
+    };
+    do {
+        float total = 0.0f;
+        int qprev = 0;
+        while (nx.x < ny.x) {
+            float strip = lo(hi((nx.y - now.y) * ystep, 0.0f), 1.0f);
+            float mid = (nx.x + now.x) * 0.5f;
+            float area = (mid - pixel.x) * strip;
+            total += strip;
+            int q = static_cast<int>(rintf((total - area) * sign * kAccScale));
+            put(pixel.x, pixel.y, q - qprev);
+            qprev = q;
+            now = nx;
+            nx.x += 1.0f;
+            nx.y = (nx.x - from.x) * slope.y + from.y;
+            pixel.x += 1.0f;
+        }
+        float strip = lo(hi((ny.y - now.y) * ystep, 0.0f), 1.0f);
+        float mid = (ny.x + now.x) * 0.5f;
+        float area = (mid - pixel.x) * strip;
+        total += strip;
+        int q = static_cast<int>(rintf((total - area) * sign * kAccScale));
+        put(pixel.x, pixel.y, q - qprev);
+        int q2 = static_cast<int>(rintf(total * sign * kAccScale));
+        put(pixel.x + 1.0f, pixel.y, q2 - q);
+        now = ny;
+        ny.y += ystep;
+        ny.x = (ny.y - from.y) * slope.x + from.x;
+        pixel.y += ystep;
+        if ((from.y < to.y && to.y < ny.y) || (from.y > to.y && to.y > ny.y)) ny = to;
+    } while (now.y != to.y);
+}
+
+// scan() of the draw itself (no offset, no padding) into `acc`: the same
+// Sutherland-Hodgman clip and clamp, then the binned cell walk.
+void canvas::scan_binned() {
+    acc.assign(static_cast<size_t>(W) * static_cast<size_t>(H), 0);
+    float width = static_cast<float>(W), height = static_cast<float>(H);
+    size_t end = 0;
+    for (size_t s = 0; s < lines.subs.size(); ++s) {
+        size_t begin = end;
+        end += lines.subs[s].count;
+        scratch.pts.clear();
+        for (size_t i = begin; i < end; ++i) scratch.pts.push_back(add(mk(0.0f, 0.0f), lines.pts[i]));
+        for (int edge = 0; edge < 4; ++edge) {
+            vec2 normal = mk(edge == 0 ? 1.0f : edge == 2 ? -1.0f : 0.0f,
+                             edge == 1 ? 1.0f : edge == 3 ? -1.0f : 0.0f);
+            float place = edge == 2 ? width : edge == 3 ? height : 0.0f;
+            size_t first = scratch.pts.size();
+            for (size_t i = 0; i < first; ++i) {
+                vec2 from = scratch.pts[(i ? i : first) - 1];
+                vec2 to = scratch.pts[i];
+                float fs = dot(from, normal) + place;
+                float ts = dot(to, normal) + place;
+                if (fs * ts < 0.0f) scratch.pts.push_back(mix(from, to, fs / (fs - ts)));
+                if (ts >= 0.0f) scratch.pts.push_back(to);
+            }
+            scratch.pts.erase(scratch.pts.begin(), scratch.pts.begin() + static_cast<ptrdiff_t>(first));
+        }
+        size_t last = scratch.pts.size();
+        for (size_t i = 0; i < last; ++i) {
+            vec2 from = scratch.pts[(i ? i : last) - 1];
+            vec2 to = scratch.pts[i];
+            scan_segment_binned(mk(lo(hi(from.x, 0.0f), width), lo(hi(from.y, 0.0f), height)),
+                                mk(lo(hi(to.x, 0.0f), width), lo(hi(to.y, 0.0f), height)));
+        }
+    }
+}
+
 // ---- paint (hpp:2265-2377) ----
 static inline float keys_weight(float t) {
     return t < 1.0f ? (1.5f * t - 2.5f) * t * t + 1.0f : ((-0.5f * t + 2.5f) * t - 4.0f) * t + 2.0f;
@@ -1258,6 +1360,45 @@ void canvas::render_shadow(const brush &br, bool clamp_edges) {
 void canvas::render(const brush &br, bool clamp_edges) {
     if (fwd.a * fwd.d - fwd.b * fwd.c == 0.0f) return;
     render_shadow(br, clamp_edges);
+#ifdef CYO_BINNED
+    // Every pixel the reference's walk visits gets the coverage of the
+    // row's accumulated area up to it and the clip visibility of the walk:
+    // min(|mask sum|, 1) from the row's first to its last mask run, else 0.
+    {
+        scan_binned();
+        int op = global_composite_operation;
+        std::vector<float> vis(static_cast<size_t>(W));
+        size_t ci = 0;
+        for (int y = 0; y < H; ++y) {
+            std::fill(vis.begin(), vis.end(), 0.0f);
+            while (ci < mask.size() && mask[ci].y < y) ++ci;
+            size_t c0 = ci;
+            while (ci < mask.size() && mask[ci].y == y) ++ci;
+            if (ci > c0) {
+                float csum = 0.0f;
+                for (size_t k = c0; k < ci; ++k) {
+                    csum += mask[k].delta;
+                    int xa = mask[k].x, xb = k + 1 < ci ? mask[k + 1].x : mask[k].x + 1;
+                    float v = lo(fabsf(csum), 1.0f);
+                    for (int x = xa; x < xb && x < W; ++x) vis[static_cast<size_t>(x)] = v;
+                }
+            }
+            uint32_t s = 0;
+            for (int x = 0; x < W; ++x) {
+                s += static_cast<uint32_t>(acc[static_cast<size_t>(y) * W + x]);
+                float coverage = cover(static_cast<float>(static_cast<int32_t>(s)) * kAccInv);
+                float v = vis[static_cast<size_t>(x)];
+                if ((coverage >= kVisible || ~op & 8) && v >= kVisible) {
+                    col &back = bitmap[static_cast<size_t>(y * W + x)];
+                    col fore = cscl(coverage * g_alpha, paint(mk(static_cast<float>(x) + 0.5f, static_cast<float>(y) + 0.5f),
+                                                             br, clamp_edges));
+                    blend_into(back, fore, op, v);
+                }
+            }
+        }
+        return;
+    }
+#endif
     scan(mk(0.0f, 0.0f), 0);
     int op = global_composite_operation;
     int x = -1, y = -1;

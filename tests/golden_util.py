@@ -37,3 +37,56 @@ def compare(a: np.ndarray, b: np.ndarray) -> Tuple[int, float]:
     """(max per-channel difference, fraction of pixels that differ at all)."""
     d = np.abs(a.astype(np.int16) - b.astype(np.int16))
     return int(d.max(initial=0)), float(np.any(d != 0, axis=-1).mean()) if d.size else 0.0
+
+
+# ---------------------------------------------------------------- tolerance
+# The parity contract for RGBA8 reads against the reference (or its
+# restatement): at least MIN_IDENTICAL of the pixels identical; the alpha
+# byte within MAX_LSB everywhere; the colour bytes within MAX_LSB wherever
+# alpha is above LOW_ALPHA / 255.  Below that, get_image_data divides the
+# colour by alpha (hpp:3348-3381): a difference in the last bit of a
+# premultiplied float is magnified up to 8160x, so those colour bytes of a
+# nearly transparent pixel are not bounded.  `strict` additionally bounds
+# every colour byte by MAX_LSB (what the exact coverage path meets).
+MAX_LSB = 1
+MIN_IDENTICAL = 0.995
+LOW_ALPHA = 2
+
+
+def contract_stats(a: np.ndarray, b: np.ndarray) -> dict:
+    d = np.abs(a.astype(np.int16) - b.astype(np.int16)).reshape(-1, 4)
+    if d.size == 0:
+        return {"max": 0, "alpha": 0, "colour_opaque": 0, "frac": 0.0}
+    low = np.minimum(a.reshape(-1, 4)[:, 3], b.reshape(-1, 4)[:, 3]) <= LOW_ALPHA
+    return {"max": int(d.max()), "alpha": int(d[:, 3].max()),
+            "colour_opaque": int(d[~low, :3].max(initial=0)), "frac": float(np.any(d != 0, axis=1).mean())}
+
+
+def assert_within_contract(got: np.ndarray, want: np.ndarray, what: str, strict: bool = False) -> None:
+    assert got.shape == want.shape, what
+    s = contract_stats(got, want)
+    assert s["alpha"] <= MAX_LSB, f"{what}: alpha differs by {s['alpha']}"
+    assert s["colour_opaque"] <= MAX_LSB, f"{what}: colour differs by {s['colour_opaque']} where alpha > {LOW_ALPHA}"
+    if strict:
+        assert s["max"] <= MAX_LSB, f"{what}: max channel difference {s['max']}"
+    assert s["frac"] <= 1.0 - MIN_IDENTICAL, f"{what}: {s['frac']:.4%} of pixels differ"
+
+
+# -------------------------------------------------------------- render modes
+# The GPU path's modes, and the oracle variant each equals bit for bit:
+#   tile        tile engine, binned coverage (the default): the oracle's
+#               coverage="binned" restatement of the same fixed-point sums;
+#   tile_exact  tile engine, sorted-run coverage: the oracle itself;
+#   plain       per-draw engine (always sorted runs): the oracle itself.
+MODES = {"tile": (0, False), "tile_exact": (0, True), "plain": (1, True)}
+
+
+def use_mode(mode: str) -> None:
+    from canvas_ity_gb300 import native
+    engine, exact = MODES[mode]
+    native.set_engine(engine)
+    native.set_coverage(exact)
+
+
+def oracle_coverage(mode: str) -> str:
+    return "binned" if mode == "tile" else "runs"

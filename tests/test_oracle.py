@@ -100,3 +100,61 @@ def test_sign_ordered_ties_bounded_on_workload(index):
     assert d[opaque].max(initial=0) <= 1
     assert d[~opaque].max(initial=0) <= 2
     assert (d.max(axis=1) != 0).mean() <= 0.005
+
+
+# ------------------------------------------- the binned coverage restatement
+# The GPU's default coverage (fixed-point areas accumulated per strip, no
+# sorted runs) is restated in the oracle (coverage="binned"); the GPU tests
+# hold the GPU to it bit for bit.  Here, on the CPU and at scale, that
+# restatement is held to the reference's own outputs and to the oracle.
+
+@pytest.mark.parametrize("entry", MANIFEST, ids=[e["name"] for e in MANIFEST])
+def test_binned_coverage_within_contract_on_reference_suite(entry):
+    tb = G.load_fixture(entry)
+    got = G.split_images(tb, oracle.replay(tb, coverage="binned")[0])
+    want = [img for _, _, img in T.parse(tb).expected_images()]
+    for i, (g, w) in enumerate(zip(got, want)):
+        G.assert_within_contract(g, w, f"{entry['name']} read {i}")
+    assert cy_hash.hamming(cy_hash.hash_image(got[-1]), entry["golden_hash"]) <= 5
+
+
+@pytest.mark.parametrize("index", range(16))
+def test_binned_coverage_within_contract_on_workload(index):
+    tb = scenes.c3_canvas(index * 17 + 5)
+    got = G.split_images(tb, oracle.replay(tb, coverage="binned")[0])
+    want = G.split_images(tb, oracle.replay(tb)[0])
+    for g, w in zip(got, want):
+        G.assert_within_contract(g, w, f"c3 canvas {index * 17 + 5}")
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_binned_coverage_within_tolerance(seed):
+    """One opaque white fill on a blank canvas (its float alpha is its
+    coverage): within 1e-5 of the sorted-run coverage wherever both paint;
+    where only one side paints, its coverage is within 1e-5 of the
+    1/8160 painting threshold (hpp:2571)."""
+    rng = np.random.default_rng(1000 + seed)
+    w, h = 160, 128
+    t = T.TraceWriter(w, h)
+    t.set_color(T.FILL_STYLE, 1.0, 1.0, 1.0, 1.0)
+    if seed % 3 == 2:
+        t.set_fill_rule(T.EVEN_ODD)
+    t.begin_path()
+    n = int(rng.integers(3, 40))
+    pts = rng.uniform((-30, -30), (w + 30, h + 30), size=(n, 2))
+    t.move_to(*pts[0])
+    for i in range(1, n):
+        if i % 3 == 0:
+            c = rng.uniform((-30, -30), (w + 30, h + 30), size=(2, 2))
+            t.bezier_curve_to(c[0, 0], c[0, 1], c[1, 0], c[1, 1], *pts[i])
+        else:
+            t.line_to(*pts[i])
+    t.close_path()
+    t.fill()
+    tb = t.finish()
+    a = oracle.replay_linear(tb, w, h, coverage="binned")[..., 3]
+    b = oracle.replay_linear(tb, w, h)[..., 3]
+    both = (a > 0) & (b > 0)
+    assert np.abs(a - b)[both].max(initial=0.0) <= 1e-5
+    one = (a > 0) != (b > 0)
+    assert (np.maximum(a, b)[one] <= 1.0 / 8160.0 + 1e-5).all()

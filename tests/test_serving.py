@@ -35,8 +35,7 @@ def test_each_result_same_alone_and_in_the_mix():
     # and within the parity tolerance of the oracle
     for tb, r in list(zip(reqs, res["results"]))[::8]:
         for g, w in zip(G.split_images(tb, r.images), G.split_images(tb, oracle.replay(tb)[0])):
-            maxd, frac = G.compare(g, w)
-            assert maxd <= 1 and frac <= 0.005
+            G.assert_within_contract(g, w, "served request")
 
 
 def test_admission_budget_limits_what_runs_at_once():

@@ -114,16 +114,19 @@ def test_cr_trig_close_to_libm_on_stroke_scenes(seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("engine_id", [0, 1], ids=["tile", "plain"])
+@pytest.mark.parametrize("mode", sorted(G.MODES))
 @pytest.mark.parametrize("seed", range(10))
-def test_device_stroke_float_canvas_bit_exact(engine_id, seed):
+def test_device_stroke_float_canvas_bit_exact(mode, seed):
     from canvas_ity_gb300 import native
-    native.set_engine(engine_id)
+    G.use_mode(mode)
     native.set_device_stroke(True)
-    tb = stroke_scene(seed)
-    w, h = T.canvas_size(tb)
-    got = native.replay_linear(tb, w, h)
-    want = oracle.replay_linear(tb, w, h, ties="sign", trig="cr")
+    try:
+        tb = stroke_scene(seed)
+        w, h = T.canvas_size(tb)
+        got = native.replay_linear(tb, w, h)
+    finally:
+        G.use_mode("tile")
+    want = oracle.replay_linear(tb, w, h, ties="sign", trig="cr", coverage=G.oracle_coverage(mode))
     bad = np.argwhere(got != want)
     assert bad.size == 0, f"{len(bad)} float values differ, first at {bad[0].tolist()}"
 
@@ -139,8 +142,7 @@ def test_device_stroke_rgba8_vs_reference_trig(seed):
     tb = stroke_scene(seed)
     got = G.split_images(tb, native.replay(tb)[0])[-1]
     want = G.split_images(tb, oracle.replay(tb, ties="sign")[0])[-1]
-    maxd, frac = G.compare(got, want)
-    assert maxd <= 1 and frac <= 0.005
+    G.assert_within_contract(got, want, f"stroke scene {seed}")
 
 
 @pytest.mark.gpu
