@@ -154,6 +154,7 @@ int cy_canvas_points_in_path(cy_canvas *c, const float *xy, int n, unsigned char
 }
 
 int cy_take_thread_status(void);
+void cy_ctx_set_transient(cy_ctx *ctx, int transient);
 
 int cy_replay(const void *trace, size_t trace_len, void *images, size_t images_cap, size_t *images_len,
               float *results, int results_cap, int *results_len) {
@@ -316,7 +317,10 @@ int cy_render_traces(const void *const *traces, const size_t *lens, int n, int e
             auto t1 = std::chrono::steady_clock::now();
             if (rc == CY_OK) {
                 std::vector<cy_ctx *> ctx(static_cast<size_t>(k));
-                for (int i = 0; i < k; ++i) ctx[i] = static_cast<cy_ctx *>(cy_canvas_ctx(j.cv[i]));
+                for (int i = 0; i < k; ++i) {
+                    ctx[i] = static_cast<cy_ctx *>(cy_canvas_ctx(j.cv[i]));
+                    cy_ctx_set_transient(ctx[i], 1);   // deleted once its reads are out
+                }
                 rc = cy_frame_create(ctx.data(), k, engine, &j.f);
                 // A canvas wider than a tile-engine strip renders on the plain engine.
                 if (rc == CY_EINVAL && engine == 0) rc = cy_frame_create(ctx.data(), k, 1, &j.f);

@@ -54,9 +54,8 @@ std::atomic<int> g_coverage{0};
 // int32 accumulation image): at most this many pixels per strip.
 constexpr int kBinnedMaxStrip = 9216;
 constexpr size_t kMaxStripSmem = 226 * 1024;   // dynamic shared memory of one strip block (of 227 KiB)
-constexpr int kBinnedMaxRows = 256;             // rows of a binned strip
-// Rows per bin band of a binned canvas W pixels wide: about 2048 pixels.
-inline int band_rows(int W) { return std::max(1, 2048 / std::max(1, W)); }
+// Rows per bin band of a binned canvas W pixels wide: about 1024 pixels.
+inline int band_rows(int W) { return std::max(1, 1024 / std::max(1, W)); }
 
 void note_thread_status(int rc) {
     if (rc && g_thread_status == 0) g_thread_status = rc;
@@ -321,6 +320,7 @@ struct cy_ctx {
     int engine = 0;
     bool deferred = false;
     bool has_content = false;   // bitmap holds more than transparent black
+    bool transient = false;     // destroyed right after its frame: the tile engine keeps no float pixels
     cudaStream_t stream = nullptr;
     float4 *bitmap = nullptr;
     size_t bitmap_bytes = 0;        // size class of the pooled buffer
@@ -433,11 +433,11 @@ struct frame {
     }
     // Shared memory of a strip: 16 B per pixel; binned adds an int32 per
     // pixel and a chunk mask per row.
-    int strip_cap = 0, strip_rows = 0;   // pixels and rows of the largest strip
+    int strip_cap = 0, strip_words = 0;   // pixels of the largest strip, words of its chunk marks
     size_t strip_smem() const {
         if (!binned) return static_cast<size_t>(strip_cap) * sizeof(float4);
         return static_cast<size_t>(strip_cap) * (sizeof(float4) + sizeof(int32_t)) +
-               static_cast<size_t>(strip_rows) * sizeof(uint32_t);
+               static_cast<size_t>(strip_words) * sizeof(uint32_t);
     }
     void drop_graph() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -1475,9 +1475,8 @@ int frame::build_strips() {
     strip_pixels = g_strip_pixels;
     if (binned) strip_pixels = std::min(strip_pixels, kBinnedMaxStrip);
     strip_threads = g_strip_threads;
-    const int nwarps = (strip_threads == 128 || strip_threads == 512 ? strip_threads : 256) / 32;
     strip_cap = 0;
-    strip_rows = 0;
+    strip_words = 0;
     scv.resize(cvs.size());
     std::vector<std::pair<int64_t, int2>> work;
     int cursor = 0;
@@ -1488,20 +1487,14 @@ int frame::build_strips() {
         s.W = cv->W;
         s.H = cv->H;
         s.TH = std::max(1, std::min(cv->H, strip_pixels / std::max(1, cv->W)));
-        if (binned) {
-            // Binned warps own whole rows: at least one row per warp, and a
-            // multiple of the warps, while the strip fits in shared memory.
-            int th = std::min(std::max(s.TH, nwarps), kBinnedMaxRows);
-            if (th > nwarps) th -= th % nwarps;
-            const int fit = static_cast<int>((kMaxStripSmem - kBinnedMaxRows * 4) / (static_cast<size_t>(cv->W) * 20));
-            s.TH = std::max(1, std::min({th, cv->H, fit}));
-        }
         strip_cap = std::max(strip_cap, s.TH * s.W);
-        strip_rows = std::max(strip_rows, s.TH);
+        strip_words = std::max(strip_words, (s.TH * ((s.W + 31) / 32) + 31) / 32);
         s.cmd_first = cursor;
         s.cmd_count = static_cast<int32_t>(cv->q.cmds.size());
         cursor += s.cmd_count;
-        s.flags = (cv->has_content ? 1 : 0) | 2;   // every canvas keeps its pixels for later frames
+        // canvases keep their pixels for later frames, unless their owner
+        // destroys them after this one
+        s.flags = (cv->has_content ? 1 : 0) | (cv->transient ? 0 : 2);
         s.bitmap = cv->bitmap;
         int64_t cost = static_cast<int64_t>(s.TH) * s.W * (s.cmd_count + 1);
         for (int y = 0; y < s.H; y += s.TH) work.push_back({cost, make_int2(static_cast<int>(ci), y)});
@@ -1556,7 +1549,7 @@ int frame::launch_strips() {
     P.lut = last_lut;
     P.get_buf = get_dev.as<uint8_t>();
     P.strip_pixels = strip_cap;
-    P.strip_rows = strip_rows;
+    P.strip_words = strip_words;
     P.bin_off = bin_off.p ? bin_off.as<int64_t>() : nullptr;
     P.bin_seg = bin_seg.p ? bin_seg.as<float4>() : nullptr;
     int per_sm = 0, dev = 0, sms = 152;
@@ -2022,6 +2015,12 @@ int queue_stroke(cy_ctx *c, const float *points, const int *counts, const int *c
 extern "C" {
 
 void cy_set_engine(int engine) { g_engine = engine; }
+// Internal (the batch and serving paths): the context will be destroyed
+// right after its next frame finishes, so the tile engine need not store
+// its float pixels back (its reads are still written).
+void cy_ctx_set_transient(cy_ctx *c, int transient) {
+    if (c) c->transient = transient != 0;
+}
 void cy_set_coverage(int exact) { g_coverage.store(exact ? 1 : 0); }
 int cy_get_coverage(void) { return g_coverage.load(); }
 void cy_set_deferred(int deferred) { g_deferred = deferred; }

@@ -25,6 +25,8 @@
 #include "../../include/cy_batch.h"
 #include "../../include/cy_serve.h"
 
+extern "C" void cy_ctx_set_transient(cy_ctx *ctx, int transient);   // engine.cu
+
 namespace {
 
 double now_s() {
@@ -135,7 +137,10 @@ void cy_server::worker() {
         cy_frame *fr = nullptr;
         if (rc == 0) {
             std::vector<cy_ctx *> ctxs(n);
-            for (int i = 0; i < n; ++i) ctxs[i] = static_cast<cy_ctx *>(cy_canvas_ctx(canvases[i]));
+            for (int i = 0; i < n; ++i) {
+                ctxs[i] = static_cast<cy_ctx *>(cy_canvas_ctx(canvases[i]));
+                cy_ctx_set_transient(ctxs[i], 1);   // deleted once its reads are out
+            }
             rc = cy_frame_create(ctxs.data(), n, engine, &fr);
             // A canvas wider than a tile-engine strip renders on the plain engine.
             if (rc == CY_EINVAL && engine == 0) rc = cy_frame_create(ctxs.data(), n, 1, &fr);

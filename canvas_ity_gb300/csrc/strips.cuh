@@ -51,87 +51,113 @@ struct strip_params {
     const float *lut;
     uint8_t *get_buf;
     int strip_pixels;         // pixels of the largest strip (shared memory per strip)
-    int strip_rows;           // binned: rows of the tallest strip (one chunk mask each)
+    int strip_words;          // binned: 32-bit words of the largest strip's chunk marks
     const int64_t *bin_off;   // binned coverage: first entry of each bin (and the end)
     const float4 *bin_seg;    // binned coverage: segment end points
 };
 
 // ------------------------------------------------- binned coverage (strips)
 // Signed areas are accumulated in shared memory as 32-bit fixed point with
-// kAccBits fractional bits.  A lane walks one row of one segment the way
-// add_runs does (hpp:2131-2169) and keeps the running total C of the deltas
-// it has produced (C after cell m = sign * (sum of strips up to m - area of
-// m)); it adds round(C * 2^kAccBits) minus what it added before, so the
-// integers of a segment row telescope to its rounded total and the prefix
-// sum of a pixel row is off by at most half a unit per segment row to its
-// left.  Integer adds commute, so the result does not depend on the order in
-// which lanes and warps get there.  Windings beyond +-2^(31-kAccBits) wrap:
-// coverage is only wrong where the winding is a nonzero multiple of
-// 2^(32-kAccBits) (1024 overlapping layers of one path).
+// kAccBits fractional bits.  A row of a segment is walked cell by cell as
+// add_runs walks it (hpp:2131-2169); the value C_m that its cells up to m
+// add to every pixel from m on is sign * (S_m - area_m), where S_m is the
+// row's vertical extent from its entry point to the cell's right crossing
+// and area_m the cell's own trapezoid, and cell pe + 1 (past the exit)
+// completes the row with sign * S_pe.  Each cell adds round(C_m * 2^kAccBits)
+// minus the same for the cell before, so a row's integers telescope and the
+// prefix sum of a pixel row is off by at most half a unit per segment row to
+// its left.  Every C_m has this closed form, so the part of a row left of a
+// column is known without walking it.  Integer adds commute, so the result
+// does not depend on which lane or warp gets where first.  Windings beyond
+// +-2^(31-kAccBits) wrap: coverage is only wrong where the winding is a
+// nonzero multiple of 2^(32-kAccBits) (1024 overlapping layers of one path).
 static constexpr int kAccBits = 22;
 static constexpr float kAccScale = 4194304.0f;          // 2^kAccBits
 static constexpr float kAccInv = 1.0f / 4194304.0f;
 
-// Accumulate row k of segment piece p into acc (row ly of the strip, W
-// cells), and widen the strip extents (row and column range touched).
-__device__ __forceinline__ void raster_row(const dda_piece &p, int k, int *row_acc, int W, int &xlo, int &xhi) {
-    float2 entry = k == 0 ? f2(p.fx, p.fy) : dda_exit(p, k - 1);
-    float2 ex = dda_exit(p, k);
-    int ps, pe;
-    dda_span(p, k, entry, ex, ps, pe);
-    // Segments are clamped to [0, W] x [0, H], so a row's cells lie in
-    // [0, W + 1]; anything else comes from non-finite input: skipped.
-    if (!(ps >= 0 && pe >= ps && pe <= W + 1)) return;
-    float2 now = entry;
-    float total = 0.0f;
-    int qprev = 0;
-    for (int m = ps; m <= pe + 1; ++m) {
-        float c;
-        if (m < pe) {
-            float2 X;
-            if (!p.vert) {
-                float cx = static_cast<float>(m + 1);
-                X = f2(cx, (cx - p.fx) * p.sy + p.fy);
-            } else {
-                X = f2(p.tx, p.ty);
-            }
-            float strip = lo(hi((X.y - now.y) * p.ystep, 0.0f), 1.0f);
-            float mid = (X.x + now.x) * 0.5f;
-            float area = (mid - static_cast<float>(m)) * strip;
-            total += strip;
-            c = (total - area) * p.sign;
-            now = X;
-        } else if (m == pe) {
-            float strip = lo(hi((ex.y - now.y) * p.ystep, 0.0f), 1.0f);
-            float mid = (ex.x + now.x) * 0.5f;
-            float area = (mid - static_cast<float>(pe)) * strip;
-            total += strip;
-            c = (total - area) * p.sign;
-        } else {
-            c = total * p.sign;
-        }
-        int q = __float2int_rn(c * kAccScale);
-        int dq = q - qprev;
-        qprev = q;
-        if (dq != 0 && m >= 0 && m < W) {
-            atomicAdd(row_acc + m, dq);
-            xlo = min(xlo, m);
-            xhi = max(xhi, m);
-        }
-    }
+// Where the walk of row k enters cell m > ps: the crossing of x = m.
+__device__ __forceinline__ float2 dda_cross(const dda_piece &p, int m) {
+    if (p.vert) return f2(p.tx, p.ty);
+    float cx = static_cast<float>(m);
+    return f2(cx, (cx - p.fx) * p.sy + p.fy);
 }
 
-// One warp's share of a draw: the entries of the draw's bins whose bands
-// overlap the warp's own strip rows [r0, r1) (local); 32 entries at a time
-// each lane prepares one segment, the (segment, row) pairs inside the
-// warp's rows are dealt to the lanes, and each lane accumulates its row.
-// rmask[ly] gets a bit per group of g chunks (32 pixels each) that the row
-// touched.
-__device__ void raster_rows(const strip_params &P, const strip_cmd &e, int W, int H, int y0, int r0, int r1,
-                            int *acc, unsigned *rmask, int g, int lane) {
+// The fixed-point C_m of cell m in [ps, pe] from its left point L and right
+// point R, the row's entry point E.
+__device__ __forceinline__ int acc_q(const dda_piece &p, int m, float2 E, float2 L, float2 R) {
+    float strip = lo(hi((R.y - L.y) * p.ystep, 0.0f), 1.0f);
+    float mid = (R.x + L.x) * 0.5f;
+    float area = (mid - static_cast<float>(m)) * strip;
+    float S = lo(hi((R.y - E.y) * p.ystep, 0.0f), 1.0f);
+    return __float2int_rn((S - area) * p.sign * kAccScale);
+}
+
+// Accumulate the cells of row k of piece p that lie in columns [xa, xb)
+// into row_acc; returns the row's integer total over the columns left of xa
+// (0 when xa == 0).  [x0, x1] receives the columns of the cells written.
+__device__ __forceinline__ int raster_row(const dda_piece &p, int k, int *row_acc, int W, int xa, int xb, int &x0,
+                                          int &x1) {
+    float2 E = k == 0 ? f2(p.fx, p.fy) : dda_exit(p, k - 1);
+    float2 X = dda_exit(p, k);
+    int ps, pe;
+    dda_span(p, k, E, X, ps, pe);
+    // Segments are clamped to [0, W] x [0, H], so a row's cells lie in
+    // [0, W + 1]; anything else comes from non-finite input: skipped.
+    if (!(ps >= 0 && pe >= ps && pe <= W + 1)) return 0;
+    if (ps >= xb) return 0;
+    int m = ps, qprev = 0, left = 0;
+    float2 L = E;
+    if (xa > ps) {
+        // cells ps .. xa-1 belong to columns left of this range
+        const int ms = min(pe + 1, xa - 1);
+        if (ms == pe + 1) {
+            float S = lo(hi((X.y - E.y) * p.ystep, 0.0f), 1.0f);
+            return __float2int_rn(S * p.sign * kAccScale);
+        }
+        float2 Lm = ms == ps ? E : dda_cross(p, ms);
+        float2 Rm = ms < pe ? dda_cross(p, ms + 1) : X;
+        qprev = left = acc_q(p, ms, E, Lm, Rm);
+        m = ms + 1;
+        L = Rm;
+    }
+    for (; m <= pe + 1 && m < xb; ++m) {
+        int q;
+        if (m <= pe) {
+            float2 R = m < pe ? dda_cross(p, m + 1) : X;
+            q = acc_q(p, m, E, L, R);
+            L = R;
+        } else {
+            float S = lo(hi((X.y - E.y) * p.ystep, 0.0f), 1.0f);
+            q = __float2int_rn(S * p.sign * kAccScale);
+        }
+        int dq = q - qprev;
+        qprev = q;
+        if (dq != 0 && m < W) {
+            atomicAdd(row_acc + m, dq);
+            x0 = min(x0, m);
+            x1 = max(x1, m);
+        }
+    }
+    return left;
+}
+
+// One warp's share of a draw over its own chunks [cb, ce) of the strip
+// (row-major, cpr chunks of 32 pixels per row): the entries of the draw's
+// bins whose bands overlap the warp's rows; 32 entries at a time each lane
+// prepares one segment, the (segment, row) pairs inside the warp's rows are
+// dealt to the lanes, and each lane accumulates the row's cells inside the
+// warp's columns of that row.  Touched chunks are marked in cmask (one bit
+// per chunk of the strip).  Returns, in every lane, what the columns left of
+// the warp's first chunk add to its first row.
+__device__ int raster_chunks(const strip_params &P, const strip_cmd &e, int W, int H, int y0, int cb, int ce,
+                             int cpr, int *acc, unsigned *cmask, int lane) {
     const int band_h = e.band_h;
-    const int ya = y0 + r0, yb = min(y0 + r1, H) - 1;   // canvas rows owned
-    if (ya > yb) return;
+    const int rA = cb / cpr, rB = (ce - 1) / cpr;          // local rows of the range
+    const int xa0 = (cb - rA * cpr) << 5;                  // first column of the first row
+    const int xb1 = min(W, (ce - rB * cpr) << 5);          // end column of the last row
+    const int ya = y0 + rA, yb = min(y0 + rB, H - 1);
+    int carry = 0;
+    if (ya > yb) return 0;
     const int b0 = ya / band_h, b1 = yb / band_h;
     const int64_t *off = P.bin_off + e.bin_base;
     const int64_t first = off[b0], last = off[b1 + 1];
@@ -143,7 +169,7 @@ __device__ void raster_rows(const strip_params &P, const strip_cmd &e, int W, in
             sg = P.bin_seg[ei];
             int band = b0;
             while (band < b1 && ei >= off[band + 1]) ++band;
-            // owned rows inside the entry's band
+            // the warp's rows inside the entry's band
             int ylo = max(ya, band * band_h), yhi = min(yb, (band + 1) * band_h - 1);
             dda_piece p;
             if (ylo <= yhi && dda_setup(f2(sg.x, sg.y), f2(sg.z, sg.w), p)) {
@@ -186,35 +212,55 @@ __device__ void raster_rows(const strip_params &P, const strip_cmd &e, int W, in
                 dda_setup(f2(ax, ay), f2(bx, by), p);
                 int k = s_klo + (q - (s_incl - s_cnt));
                 int ly = dda_row_index(p, k) - y0;
+                int xa = ly == rA ? xa0 : 0, xb = ly == rB ? xb1 : W;
                 int x0 = 0x7fffffff, x1 = -1;
-                raster_row(p, k, acc + ly * W, W, x0, x1);
+                int left = raster_row(p, k, acc + ly * W, W, xa, xb, x0, x1);
+                if (ly == rA) carry += left;
                 if (x0 <= x1) {
-                    int g0 = (x0 >> 5) / g, g1 = (x1 >> 5) / g;
-                    unsigned bits = (g1 >= 31 ? 0xffffffffu : ((2u << g1) - 1u)) & ~((1u << g0) - 1u);
-                    atomicOr(rmask + ly, bits);
+                    int c0 = ly * cpr + (x0 >> 5), c1 = ly * cpr + (x1 >> 5);
+                    for (int w = c0 >> 5; w <= (c1 >> 5); ++w) {
+                        int lo_b = max(c0, w << 5) - (w << 5), hi_b = min(c1, (w << 5) + 31) - (w << 5);
+                        unsigned bits = (hi_b >= 31 ? 0xffffffffu : ((2u << hi_b) - 1u)) & ~((1u << lo_b) - 1u);
+                        atomicOr(cmask + w, bits);
+                    }
                 }
             }
         }
     }
+    return static_cast<int>(__reduce_add_sync(0xffffffffu, static_cast<unsigned>(carry)));
+}
+
+// First marked chunk in [c, c_end), or c_end.
+__device__ __forceinline__ int next_marked(const unsigned *cmask, int c, int c_end) {
+    while (c < c_end) {
+        unsigned w = cmask[c >> 5] & (0xffffffffu << (c & 31));
+        if (w) {
+            int f = ((c >> 5) << 5) + __ffs(w) - 1;
+            return f < c_end ? f : c_end;
+        }
+        c = ((c >> 5) + 1) << 5;
+    }
+    return c_end;
 }
 
 // BINNED selects the coverage of draws: false walks the row-sorted runs
 // (the float canvas is then the reference's bit for bit); true has each
-// warp accumulate the draw's binned segments over its own rows of the strip
-// in shared memory (raster_rows), then prefix-sum each row with shuffles
-// while it paints.  Binned warps own whole rows, so no barrier is needed
-// between draws.  Shared memory: the strip's float4 pixels, and for BINNED
-// an int32 accumulation image of the strip and one chunk mask per row.
+// warp accumulate the draw's binned segments over its own chunks of the
+// strip in shared memory (raster_chunks), then prefix-sum its rows with
+// shuffles while it paints.  A warp only ever touches its own chunks, so no
+// barrier is needed between draws.  Shared memory: the strip's float4
+// pixels, and for BINNED an int32 accumulation image of the strip and one
+// bit per chunk.
 template <int THREADS, bool BINNED>
 __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
     extern __shared__ float4 px[];
     __shared__ int item_slot;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     int *acc = BINNED ? reinterpret_cast<int *>(px + P.strip_pixels) : nullptr;
-    unsigned *rmask = BINNED ? reinterpret_cast<unsigned *>(acc + P.strip_pixels) : nullptr;
+    unsigned *cmask = BINNED ? reinterpret_cast<unsigned *>(acc + P.strip_pixels) : nullptr;
     if (BINNED) {   // zero once: each draw's paint clears what its raster wrote
         for (int i = threadIdx.x; i < P.strip_pixels; i += blockDim.x) acc[i] = 0;
-        for (int i = threadIdx.x; i < P.strip_rows; i += blockDim.x) rmask[i] = 0;
+        for (int i = threadIdx.x; i < P.strip_words; i += blockDim.x) cmask[i] = 0;
     }
     for (;;) {
         __syncthreads();
@@ -230,10 +276,8 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
         const int chunks = rows * cpr;
         // Each warp owns a contiguous range of chunks (row-major) for the
         // whole item, so every pixel is always touched by the same thread.
-        // Binned: whole rows per warp.
-        const int per = BINNED ? ((rows + nwarps - 1) / nwarps) * cpr : (chunks + nwarps - 1) / nwarps;
+        const int per = (chunks + nwarps - 1) / nwarps;
         const int cb = min(chunks, warp * per), ce = min(chunks, cb + per);
-        const int g = (cpr + 31) >> 5;           // binned: chunks per row-mask bit
         for (int ch = cb; ch < ce; ++ch) {
             int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;
             if (x >= W) continue;
@@ -297,38 +341,30 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
             }
             if (BINNED) {
                 if (cb >= ce || (!clearing && (c.gy1 < wy0 || c.gy0 > wy1))) continue;
-                const int r0 = cb / cpr, r1 = (ce - 1) / cpr + 1;
-                raster_rows(P, e, W, cv.H, y0, r0, r1, acc, rmask, g, lane);
+                const int carry0 = raster_chunks(P, e, W, cv.H, y0, cb, ce, cpr, acc, cmask, lane);
                 __syncwarp();
-                for (int ly = r0; ly < r1; ++ly) {
-                    unsigned mask = 0;
-                    if (lane == 0) {
-                        mask = rmask[ly];
-                        rmask[ly] = 0;
-                    }
-                    mask = __shfl_sync(0xffffffffu, mask, 0);
-                    if (!clearing && !mask) continue;
-                    const int y = y0 + ly;
+                const int rA = cb / cpr, rB = (ce - 1) / cpr;
+                for (int ly = rA; ly <= rB; ++ly) {
+                    const int row0 = ly * cpr, y = y0 + ly;
+                    const int c_hi = min(ce, row0 + cpr);
+                    int ch = max(cb, row0);
+                    int carry = ly == rA ? carry0 : 0;
                     int *arow = acc + ly * W;
-                    int carry = 0;
-                    // Chunks of a clear mask bit hold no accumulated area: the
-                    // sum there is the carry.  Where that is invisible the
-                    // walk jumps to the next marked chunk.
-                    for (int ch = 0; ch < cpr;) {
-                        const bool marked = (mask >> (ch / g)) & 1u;
+                    while (ch < c_hi) {
+                        const bool marked = (cmask[ch >> 5] >> (ch & 31)) & 1u;
                         if (!marked && !clearing && cover_of(static_cast<float>(carry) * kAccInv, c.fill_rule) < kVisible) {
-                            unsigned rest = mask & ~((2u << (ch / g)) - 1u);
-                            if ((ch / g) >= 31 || !rest) break;
-                            ch = (__ffs(rest) - 1) * g;
+                            // no area here and the sum so far is invisible:
+                            // on to the next chunk that holds area
+                            ch = next_marked(cmask, ch + 1, c_hi);
                             continue;
                         }
-                        const int x = (ch << 5) + lane;
+                        const int x = ((ch - row0) << 5) + lane;
                         int v = 0;
-                        if (marked && x < W) {
-                            v = arow[x];
-                            if (v) arow[x] = 0;
-                        }
                         if (marked) {
+                            if (x < W) {
+                                v = arow[x];
+                                if (v) arow[x] = 0;
+                            }
 #pragma unroll
                             for (int o = 1; o < 32; o <<= 1) {
                                 int t = __shfl_up_sync(0xffffffffu, v, o);
@@ -348,6 +384,14 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
                             px[ly * W + x] = blend(px[ly * W + x], fore, op, vis);
                         }
                     }
+                }
+                // clear the marks of the warp's chunks (other warps' bits in
+                // the same words are left alone)
+                __syncwarp();
+                for (int w = (cb >> 5) + lane; w <= ((ce - 1) >> 5); w += 32) {
+                    int lo_b = max(cb, w << 5) - (w << 5), hi_b = min(ce - 1, (w << 5) + 31) - (w << 5);
+                    unsigned bits = (hi_b >= 31 ? 0xffffffffu : ((2u << hi_b) - 1u)) & ~((1u << lo_b) - 1u);
+                    atomicAnd(cmask + w, ~bits);
                 }
                 __syncwarp();
                 continue;

@@ -159,3 +159,76 @@ def run_poisson(server: Server, traces: Sequence[bytes], rate: float, seed: int 
     if keep_results:
         out["results"] = [results[i] for i in order]
     return out
+
+
+def run_steady(server: Server, pool: Sequence[bytes], rate: float, duration_s: float = 5.0, seed: int = 0,
+               max_backlog: int = 2000) -> dict:
+    """Offer requests (cycling through `pool`) with exponential inter-arrival
+    times of mean 1/rate for `duration_s` seconds of arrivals, and measure
+    the server at that load: latency percentiles (ms, submission to
+    completion) of every request, and the rate it actually completed them
+    at.  A server that cannot keep up builds a backlog; once `max_backlog`
+    requests wait unanswered, arrivals stop early (the run is then marked
+    saturated, and its completion rate is the server's capacity)."""
+    from . import trace as T
+    rng = np.random.default_rng(seed)
+    n_max = max(1, int(rate * duration_s))
+    gaps = rng.exponential(1.0 / rate, size=n_max)
+    picks = rng.integers(0, len(pool), size=n_max)
+    px_of = [T.canvas_size(tb)[0] * T.canvas_size(tb)[1] for tb in pool]
+    submitted = [0]
+    stopped_early = [False]
+    done_count = [0]
+    lock = threading.Lock()
+    t0 = [0.0]
+
+    def drive():
+        t = time.perf_counter()
+        t0[0] = t
+        due = t
+        for i in range(n_max):
+            due += gaps[i]
+            while time.perf_counter() < due:
+                pass
+            with lock:
+                if submitted[0] - done_count[0] >= max_backlog:
+                    stopped_early[0] = True
+                    break
+            server.submit(pool[picks[i]])
+            with lock:
+                submitted[0] += 1
+
+    driver = threading.Thread(target=drive)
+    driver.start()
+    lat, failed, px = [], 0, 0
+    t_last = 0.0
+    while True:
+        with lock:
+            finished_all = not driver.is_alive() and done_count[0] >= submitted[0]
+        if finished_all:
+            break
+        r = server.poll(200)
+        if r is None:
+            continue
+        lat.append(r.latency_ms)
+        failed += r.status != 0
+        t_last = time.perf_counter()
+        with lock:
+            done_count[0] += 1
+    driver.join()
+    n = len(lat)
+    lat_a = np.asarray(lat) if n else np.zeros(1)
+    span = max(t_last - t0[0], 1e-9)
+    mean_px = float(np.mean([px_of[i] for i in picks[:n]])) if n else 0.0
+    return {
+        "offered_req_s": rate,
+        "requests": n,
+        "offered_for_s": round(float(gaps[:n].sum()), 3),
+        "achieved_req_s": round(n / span, 1),
+        "saturated": bool(stopped_early[0]),
+        "p50_ms": round(float(np.percentile(lat_a, 50)), 3),
+        "p99_ms": round(float(np.percentile(lat_a, 99)), 3),
+        "mean_ms": round(float(lat_a.mean()), 3),
+        "mpix_s": round(n * mean_px / span / 1e6, 2),
+        "failed": failed,
+    }

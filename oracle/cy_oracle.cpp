@@ -1076,11 +1076,13 @@ void canvas::scan(vec2 offset, int padding) {
 }
 
 // ---- binned coverage (the library's sort-free variant, CYO_BINNED) ----
-// The same cell walk as scan_segment (add_runs, hpp:2109-2170), but each
-// row keeps the running total C of the deltas it produced (C after cell m =
-// sign * (strips so far - area of m)) and adds round(C * 2^22) minus what
-// it added before, as 32-bit integers, into a per-pixel accumulation image.
-// Cells at x >= W or rows outside [0, H) are dropped.
+// The same cell walk as scan_segment (add_runs, hpp:2109-2170), but a row
+// adds to a per-pixel 32-bit integer accumulation image: cell m adds
+// round(C_m * 2^22) minus the same for the cell before, where C_m = sign *
+// (S_m - area_m), S_m the row's vertical extent from its entry point to
+// the cell's right crossing and area_m the cell's trapezoid; the cell past
+// the exit adds what completes sign * S of the whole row.  Cells at x >= W or
+// rows outside [0, H) are dropped.
 static const float kAccScale = 4194304.0f;   // 2^22
 static const float kAccInv = 1.0f / 4194304.0f;
 
@@ -1103,15 +1105,18 @@ void canvas::scan_segment_binned(vec2 from, vec2 to) {
             acc[static_cast<size_t>(iy) * W + ix] = static_cast<int32_t>(
                 static_cast<uint32_t>(acc[static_cast<size_t>(iy) * W + ix]) + static_cast<uint32_t>(dq));
     };
+    auto q_of = [&](vec2 entry, vec2 left, vec2 right, float px) {
+        float strip = lo(hi((right.y - left.y) * ystep, 0.0f), 1.0f);
+        float mid = (right.x + left.x) * 0.5f;
+        float area = (mid - px) * strip;
+        float S = lo(hi((right.y - entry.y) * ystep, 0.0f), 1.0f);
+        return static_cast<int>(rintf((S - area) * sign * kAccScale));
+    };
     do {
-        float total = 0.0f;
+        const vec2 entry = now;
         int qprev = 0;
         while (nx.x < ny.x) {
-            float strip = lo(hi((nx.y - now.y) * ystep, 0.0f), 1.0f);
-            float mid = (nx.x + now.x) * 0.5f;
-            float area = (mid - pixel.x) * strip;
-            total += strip;
-            int q = static_cast<int>(rintf((total - area) * sign * kAccScale));
+            int q = q_of(entry, now, nx, pixel.x);
             put(pixel.x, pixel.y, q - qprev);
             qprev = q;
             now = nx;
@@ -1119,13 +1124,10 @@ void canvas::scan_segment_binned(vec2 from, vec2 to) {
             nx.y = (nx.x - from.x) * slope.y + from.y;
             pixel.x += 1.0f;
         }
-        float strip = lo(hi((ny.y - now.y) * ystep, 0.0f), 1.0f);
-        float mid = (ny.x + now.x) * 0.5f;
-        float area = (mid - pixel.x) * strip;
-        total += strip;
-        int q = static_cast<int>(rintf((total - area) * sign * kAccScale));
+        int q = q_of(entry, now, ny, pixel.x);
         put(pixel.x, pixel.y, q - qprev);
-        int q2 = static_cast<int>(rintf(total * sign * kAccScale));
+        float S = lo(hi((ny.y - entry.y) * ystep, 0.0f), 1.0f);
+        int q2 = static_cast<int>(rintf(S * sign * kAccScale));
         put(pixel.x + 1.0f, pixel.y, q2 - q);
         now = ny;
         ny.y += ystep;

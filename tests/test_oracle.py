@@ -158,3 +158,26 @@ def test_binned_coverage_within_tolerance(seed):
     assert np.abs(a - b)[both].max(initial=0.0) <= 1e-5
     one = (a > 0) != (b > 0)
     assert (np.maximum(a, b)[one] <= 1.0 / 8160.0 + 1e-5).all()
+
+
+@pytest.mark.reference
+def test_port_runs_at_the_reference_speed():
+    """The CPU baseline on the GPU host is this restatement (the reference's
+    sources do not travel there): on the same canvases, one thread, it must
+    run at the speed of the reference header compiled here, so that a
+    baseline measured with it stands for the reference's own."""
+    import time
+    if not oracle.reference_available():
+        pytest.skip("reference sources are not present here")
+    traces = [scenes.c3_canvas(i) for i in range(24)]
+    oracle.replay(traces[0])
+    oracle.reference_replay(traces[0])
+    best = {}
+    for name, fn in (("port", oracle.replay), ("reference", oracle.reference_replay)) * 2:
+        t0 = time.perf_counter()
+        for tb in traces:
+            fn(tb)
+        best[name] = min(best.get(name, 1e9), time.perf_counter() - t0)
+    ratio = best["reference"] / best["port"]
+    print(f"port {best['port']:.3f} s, reference {best['reference']:.3f} s, port speed / reference speed {ratio:.3f}")
+    assert 0.67 <= ratio <= 1.5
