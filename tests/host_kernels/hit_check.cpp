@@ -53,6 +53,7 @@ int cy_flush(cy_ctx *) { return 0; }
 int cy_ctx_status(const cy_ctx *) { return 0; }
 void cy_set_engine(int) {}
 int cy_take_thread_status(void) { return 0; }
+void cy_ctx_set_transient(cy_ctx *, int) {}
 void cy_set_deferred(int) {}
 }
 int main() {

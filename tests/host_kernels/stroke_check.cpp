@@ -212,6 +212,7 @@ int cy_ctx_status(const cy_ctx *) { return 0; }
 void cy_set_engine(int) {}
 void cy_set_deferred(int) {}
 int cy_take_thread_status(void) { return 0; }
+void cy_ctx_set_transient(cy_ctx *, int) {}
 int cy_frame_create(cy_ctx *const *, int, int, cy_frame **) { return CY_ENODEV; }
 int cy_frame_stats(cy_frame *, long long *, int) { return 0; }
 int cy_frame_finish_views(cy_frame *, const unsigned char **, size_t *) { return CY_ENODEV; }
