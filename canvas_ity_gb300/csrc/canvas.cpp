@@ -130,6 +130,10 @@ struct canvas_state {
     void half_stroke(size_t begin, size_t end, bool closed);
     void stroke_outline();
     void glyph_outline(int glyph, float angular);
+    // Glyph outlines into `path` as cubic control points (lines as
+    // degenerate cubics) instead of flattening them into `lines`: what the
+    // device stroke expansion takes (set while stroke_text builds them).
+    bool outline_cubics = false;
     int glyph_of(const char *text, int &index);
     void text_outline(const char *text, v2 at, float maxw, bool stroking);
     float measure(const char *text);
@@ -519,7 +523,32 @@ void canvas_state::glyph_outline(int glyph, float angular) {
         int end = u16at(d, offset + 10 + ct * 2);
         v2 bp = mk(0, 0), ep = mk(0, 0);
         bool bon = false, eon = false;
-        size_t first = lines.pts.size();
+        // Each contour is emitted as points and cubics: flattened into
+        // `lines` (add_glyph, hpp:1533-1846), or kept as cubic control points
+        // in `path` (outline_cubics), where the device flattens them alike.
+        polyline &out = outline_cubics ? path : lines;
+        size_t first = out.pts.size();
+        auto put_point = [&](v2 p) {
+            if (!outline_cubics) {
+                lines.pts.push_back(p);
+            } else if (out.pts.size() == first) {
+                path.pts.push_back(p);
+            } else {
+                v2 p1 = path.pts.back();
+                path.pts.push_back(p1);
+                path.pts.push_back(p);
+                path.pts.push_back(p);
+            }
+        };
+        auto put_curve = [&](v2 p1, v2 c1, v2 c2, v2 p2) {
+            if (!outline_cubics) {
+                bezier(p1, c1, c2, p2, angular);
+            } else {
+                path.pts.push_back(c1);
+                path.pts.push_back(c2);
+                path.pts.push_back(p2);
+            }
+        };
         for (; idx <= end; ++idx) {
             if (rep) --rep;
             else {
@@ -537,33 +566,36 @@ void canvas_state::glyph_outline(int glyph, float angular) {
             if (idx == begin) {
                 bp = pt;
                 bon = on;
-                if (on) lines.pts.push_back(pt);
+                if (on) put_point(pt);
             } else {
                 v2 p2 = on ? pt : mix(ep, pt, 0.5f);
-                if (lines.pts.size() == first || (eon && on)) {
-                    lines.pts.push_back(p2);
+                if (out.pts.size() == first || (eon && on)) {
+                    put_point(p2);
                 } else if (!eon || on) {
-                    v2 p1 = lines.pts.back();
-                    bezier(p1, mix(p1, ep, 2.0f / 3.0f), mix(p2, ep, 2.0f / 3.0f), p2, angular);
+                    v2 p1 = out.pts.back();
+                    put_curve(p1, mix(p1, ep, 2.0f / 3.0f), mix(p2, ep, 2.0f / 3.0f), p2);
                 }
             }
             ep = pt;
             eon = on;
         }
+        // a contour of one off-curve point has nothing to close (the host
+        // walk below follows the reference even there)
+        if (outline_cubics && out.pts.size() == first) continue;
         if (bon ^ eon) {
-            v2 p1 = lines.pts.back(), p2 = lines.pts[first];
+            v2 p1 = out.pts.back(), p2 = out.pts[first];
             v2 ctl = eon ? bp : ep;
-            bezier(p1, mix(p1, ctl, 2.0f / 3.0f), mix(p2, ctl, 2.0f / 3.0f), p2, angular);
+            put_curve(p1, mix(p1, ctl, 2.0f / 3.0f), mix(p2, ctl, 2.0f / 3.0f), p2);
         } else if (!bon && !eon) {
-            v2 p1 = lines.pts.back();
+            v2 p1 = out.pts.back();
             v2 split = mix(bp, ep, 0.5f);
-            v2 p2 = lines.pts[first];
-            bezier(p1, mix(p1, ep, 2.0f / 3.0f), mix(split, ep, 2.0f / 3.0f), split, angular);
-            bezier(split, mix(split, bp, 2.0f / 3.0f), mix(p2, bp, 2.0f / 3.0f), p2, angular);
+            v2 p2 = out.pts[first];
+            put_curve(p1, mix(p1, ep, 2.0f / 3.0f), mix(split, ep, 2.0f / 3.0f), split);
+            put_curve(split, mix(split, bp, 2.0f / 3.0f), mix(p2, bp, 2.0f / 3.0f), p2);
         }
-        lines.pts.push_back(lines.pts[first]);
-        subpath e = {lines.pts.size() - first, true};
-        lines.subs.push_back(e);
+        put_point(out.pts[first]);
+        subpath e = {out.pts.size() - first, true};
+        out.subs.push_back(e);
     }
 }
 
@@ -1118,6 +1150,37 @@ void canvas::stroke_rectangle(float x, float y, float w, float h) {
     sync_public_state();
     detail::canvas_state &s = *self;
     if (w == 0.0f && h == 0.0f) return;
+    if (cy_device_stroke()) {
+        // The rectangle's lines as a path of degenerate cubics, which the
+        // device flattens to the same points, stroked on the device; the
+        // current path is left as it was.
+        detail::polyline saved;
+        saved.pts.swap(s.path.pts);
+        saved.subs.swap(s.path.subs);
+        v2 a = apply(s.fwd, mk(x, y));
+        s.path.pts.push_back(a);
+        auto line = [&](v2 p) {
+            v2 p1 = s.path.pts.back();
+            s.path.pts.push_back(p1);
+            s.path.pts.push_back(p);
+            s.path.pts.push_back(p);
+        };
+        bool flat = w == 0.0f || h == 0.0f;
+        if (flat) {
+            line(apply(s.fwd, mk(x + w, y + h)));
+        } else {
+            line(apply(s.fwd, mk(x + w, y)));
+            line(apply(s.fwd, mk(x + w, y + h)));
+            line(apply(s.fwd, mk(x, y + h)));
+            line(a);
+        }
+        detail::subpath e = {s.path.pts.size(), !flat};
+        s.path.subs.push_back(e);
+        s.stroke_path(s.stroke);
+        s.path.pts.swap(saved.pts);
+        s.path.subs.swap(saved.subs);
+        return;
+    }
     if (w == 0.0f || h == 0.0f) {
         s.lines.pts.clear();
         s.lines.subs.clear();
@@ -1178,6 +1241,21 @@ void canvas::fill_text(char const *text, float x, float y, float maxw) {
 }
 void canvas::stroke_text(char const *text, float x, float y, float maxw) {
     sync_public_state();
+    detail::canvas_state &s = *self;
+    if (cy_device_stroke()) {
+        // The glyph outlines as cubics, flattened and stroked on the device;
+        // the current path is left as it was.
+        detail::polyline saved;
+        saved.pts.swap(s.path.pts);
+        saved.subs.swap(s.path.subs);
+        s.outline_cubics = true;
+        s.text_outline(text, mk(x, y), maxw, true);
+        s.outline_cubics = false;
+        if (!s.path.subs.empty()) s.stroke_path(s.stroke);
+        s.path.pts.swap(saved.pts);
+        s.path.subs.swap(saved.subs);
+        return;
+    }
     self->text_outline(text, mk(x, y), maxw, true);
     self->stroke_outline();
     self->draw_lines(self->stroke, false, false, true);

@@ -54,8 +54,8 @@ std::atomic<int> g_coverage{0};
 // int32 accumulation image): at most this many pixels per strip.
 constexpr int kBinnedMaxStrip = 9216;
 constexpr size_t kMaxStripSmem = 226 * 1024;   // dynamic shared memory of one strip block (of 227 KiB)
-// Rows per bin band of a binned canvas W pixels wide: about 1024 pixels.
-inline int band_rows(int W) { return std::max(1, 1024 / std::max(1, W)); }
+// Rows per bin band of a binned canvas W pixels wide: about 2048 pixels.
+inline int band_rows(int W) { return std::max(1, 2048 / std::max(1, W)); }
 
 void note_thread_status(int rc) {
     if (rc && g_thread_status == 0) g_thread_status = rc;
@@ -388,7 +388,7 @@ struct frame {
     // device
     dbuf arena, flat_pts, flat_prev, item_cnt, item_off, pat_f4, jobs_dev, boxes;
     dbuf row_cnt, row_off, row_cur, row_len, row_meta, long_rows, n_long, runs, sums;
-    dbuf bin_cnt, bin_cur, bin_off, bin_seg;
+    dbuf bin_cnt, bin_cur, bin_off, bin_seg, clip_dev;
     dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
     dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, st_err, pc_cnt, pc_base, pc_list, wk_cnt, wk_base,
@@ -410,6 +410,9 @@ struct frame {
     }
     bool ext_built = false;
     bool strips_built = false;
+    bool clips_built = false;                 // clip_dev holds the clip masks' arguments
+    std::vector<clip_args> clip_host;
+    std::vector<int> level_first, level_max_h;   // clips of each nesting level in clip_host
     int strip_threads = 256;
     cudaGraphExec_t graph_exec = nullptr;   // captured device-only run (after sizing)
     // inputs of the strip launch, kept by run() so the paint stage can be
@@ -478,7 +481,7 @@ struct frame {
         n_items = 0;
         binned = false;
         n_bins = n_bin_entries = 0;
-        sized = ext_built = strips_built = false;
+        sized = ext_built = strips_built = clips_built = false;
         n_runs = main_runs = main_rows = h2d_bytes = 0;
     }
 
@@ -490,7 +493,7 @@ struct frame {
                      &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev, &dash_cnt, &dash_off, &dash_pts,
                      &dash_subs, &dash_nsub, &st_err, &pc_cnt, &pc_base, &pc_list, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt,
-                     &jn_alpha, &jn_sum, &jn_off, &st_goff, &bin_cnt, &bin_cur, &bin_off, &bin_seg};
+                     &jn_alpha, &jn_sum, &jn_off, &st_goff, &bin_cnt, &bin_cur, &bin_off, &bin_seg, &clip_dev};
         for (dbuf *x : b) x->release();
         staging.release();
         stoff_host.release();
@@ -1302,44 +1305,61 @@ int frame::run() {
         launches += (segs_nc > 0 ? 2 : 0) + (segs_cl > 0 ? 2 : 0) + 2 + scan_launch_count(static_cast<int64_t>(nr) + 1);
     }
     mark();   // 2: scan conversion done
-    // Clip masks, level by level (a clip depends on the previous mask).
-    for (int lv = 0; lv <= max_level; ++lv) {
-        for (const clip_op &op : clips) {
-            if (op.level != lv) continue;
-            cy_ctx *cv = cvs[op.cv];
-            int W = cv->W, H = cv->H;
-            mask_slot &nm = cv->masks[op.out_id];
-            const mask_slot *om = op.in_id > 0 ? &cv->masks[op.in_id] : nullptr;
-            const scan_job &j = jobs[main_job[op.cmd]];
-            k_clip_caps<<<(H + 255) / 256, 256, 0, stream>>>(row_off.as<int64_t>() + j.row_base,
-                                                              om ? om->off : nullptr, H, nm.len);
-            if (!ok(cudaMemsetAsync(nm.len + H, 0, 4, stream))) return status;
-            int rc = scan(nm.len, nm.off, H + 1);
-            if (rc) return rc;
-            if (!ok(cudaMemsetAsync(nm.last_row, 0xff, 4, stream))) return status;
-            clip_args a;
-            a.p_off = row_off.as<int64_t>();
-            a.p_len = row_len.as<int32_t>();
-            a.p_runs = runs.as<cyg::run>();
-            a.p_base = j.row_base;
-            a.p_box = boxes.as<cover_box>() + main_job[op.cmd];
-            a.o_off = om ? om->off : nullptr;
-            a.o_len = om ? om->len : nullptr;
-            a.o_runs = om ? om->runs : nullptr;
-            a.o_last_row = om ? om->last_row : nullptr;
-            a.n_off = nm.off;
-            a.n_len = nm.len;
-            a.n_runs = nm.runs;
-            a.n_last_row = nm.last_row;
-            a.W = W;
-            a.H = H;
-            a.rule = cmds[op.cmd].fill_rule;
-            k_clip_rows<<<(H + 127) / 128, 128, 0, stream>>>(a);
-            k_mask_prefix<<<(H + 127) / 128, 128, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, H);
-            k_mask_fill<<<std::max(1, (H + 7) / 8), 256, 0, stream>>>(nm.off, nm.len, nm.runs, nm.sums, W, H,
-                                                                      nm.vis);
+    // Clip masks, level by level (a clip depends on the previous mask); all
+    // clips of a level together, four launches.
+    if (!clips.empty()) {
+        if (!clips_built) {
+            clips_built = true;
+            clip_host.clear();
+            level_first.assign(static_cast<size_t>(max_level) + 2, 0);
+            level_max_h.assign(static_cast<size_t>(max_level) + 1, 0);
+            for (int lv = 0; lv <= max_level; ++lv) {
+                level_first[lv] = static_cast<int>(clip_host.size());
+                for (const clip_op &op : clips) {
+                    if (op.level != lv) continue;
+                    cy_ctx *cv = cvs[op.cv];
+                    mask_slot &nm = cv->masks[op.out_id];
+                    const mask_slot *om = op.in_id > 0 ? &cv->masks[op.in_id] : nullptr;
+                    const scan_job &j = jobs[main_job[op.cmd]];
+                    clip_args a;
+                    a.p_off = row_off.as<int64_t>();
+                    a.p_len = row_len.as<int32_t>();
+                    a.p_runs = runs.as<cyg::run>();
+                    a.p_base = j.row_base;
+                    a.p_box = boxes.as<cover_box>() + main_job[op.cmd];
+                    a.o_off = om ? om->off : nullptr;
+                    a.o_len = om ? om->len : nullptr;
+                    a.o_runs = om ? om->runs : nullptr;
+                    a.o_last_row = om ? om->last_row : nullptr;
+                    a.n_off = nm.off;
+                    a.n_len = nm.len;
+                    a.n_runs = nm.runs;
+                    a.n_sums = nm.sums;
+                    a.n_vis = nm.vis;
+                    a.n_last_row = nm.last_row;
+                    a.W = cv->W;
+                    a.H = cv->H;
+                    a.rule = cmds[op.cmd].fill_rule;
+                    clip_host.push_back(a);
+                    level_max_h[lv] = std::max(level_max_h[lv], cv->H);
+                }
+            }
+            level_first[max_level + 1] = static_cast<int>(clip_host.size());
+            if (!clip_dev.ensure(clip_host.size() * sizeof(clip_args)) ||
+                !ok(cudaMemcpyAsync(clip_dev.p, clip_host.data(), clip_host.size() * sizeof(clip_args),
+                                    cudaMemcpyHostToDevice, stream)))
+                return status;
+        }
+        const clip_args *ca = clip_dev.as<clip_args>();
+        for (int lv = 0; lv <= max_level; ++lv) {
+            int first = level_first[lv], n = level_first[lv + 1] - first, H = level_max_h[lv];
+            if (n == 0) continue;
+            k_clip_caps_all<<<dim3((H + 1 + 255) / 256, n), 256, 0, stream>>>(ca, first);
+            k_clip_scan_all<<<dim3(1, n), 1024, 0, stream>>>(ca, first);
+            k_clip_rows_all<<<dim3((H + 127) / 128, n), 128, 0, stream>>>(ca, first);
+            k_mask_fill_all<<<dim3(std::max(1, std::min((H + 7) / 8, 64)), n), 256, 0, stream>>>(ca, first);
             if (!ok(cudaGetLastError())) return status;
-            launches += 5 + scan_launch_count(H + 1);
+            launches += 4;
         }
     }
     // Shadow images of every shadowed draw.
@@ -1477,6 +1497,7 @@ int frame::build_strips() {
     strip_threads = g_strip_threads;
     strip_cap = 0;
     strip_words = 0;
+    const int nwarps = (strip_threads == 128 || strip_threads == 512 ? strip_threads : 256) / 32;
     scv.resize(cvs.size());
     std::vector<std::pair<int64_t, int2>> work;
     int cursor = 0;
@@ -1487,6 +1508,12 @@ int frame::build_strips() {
         s.W = cv->W;
         s.H = cv->H;
         s.TH = std::max(1, std::min(cv->H, strip_pixels / std::max(1, cv->W)));
+        if (binned && s.TH > nwarps && s.TH < cv->H) {
+            // a multiple of the warps, so each warp owns whole rows (when that
+            // costs at most a quarter of the strip)
+            int th = s.TH - s.TH % nwarps;
+            if (4 * th >= 3 * s.TH) s.TH = th;
+        }
         strip_cap = std::max(strip_cap, s.TH * s.W);
         strip_words = std::max(strip_words, (s.TH * ((s.W + 31) / 32) + 31) / 32);
         s.cmd_first = cursor;

@@ -907,19 +907,82 @@ struct clip_args {
     const int *o_last_row;   // last row holding old-mask runs (null: H-1)
     const cover_box *p_box;  // bounds of the path runs
     // new mask
-    const int32_t *n_off;
-    int32_t *n_len;
+    int32_t *n_off;          // H+1 offsets (from the capacities)
+    int32_t *n_len;          // H+1: capacities, then run counts
     run *n_runs;
+    float *n_sums;           // running sum after each run
+    float *n_vis;            // W*H dense visibility
     int *n_last_row;
     int W, H;
     int rule;                // fill rule of the clip path
 };
 
+// All clip masks of one nesting level are made together: blockIdx.y picks
+// the clip (args[first + blockIdx.y]), so a level costs four launches
+// however many canvases hold a clip.
+
+// Run capacity of each row of a new clip mask: the path's raw runs plus the
+// old mask's runs (2 per row for the whole canvas).
+__global__ void k_clip_caps_all(const clip_args *args, int first) {
+    const clip_args &a = args[first + blockIdx.y];
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y > a.H) return;
+    if (y == 0) *a.n_last_row = -1;
+    if (y == a.H) {
+        a.n_len[y] = 0;
+        return;
+    }
+    int p = static_cast<int>(a.p_off[a.p_base + y + 1] - a.p_off[a.p_base + y]);
+    int o = a.o_off ? a.o_off[y + 1] - a.o_off[y] : 2;
+    a.n_len[y] = p + o;
+}
+
+// Exclusive scan of the H+1 capacities into the row offsets, one block (of
+// 1024 threads) per clip.
+__global__ void __launch_bounds__(1024) k_clip_scan_all(const clip_args *args, int first) {
+    __shared__ int32_t warp_sums[32];
+    __shared__ int32_t carry;
+    const clip_args &a = args[first + blockIdx.y];
+    const int n = a.H + 1, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 1024) {
+        int i = base + threadIdx.x;
+        int32_t v = i < n ? a.n_len[i] : 0;
+        int32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_sums[w] = incl;
+        __syncthreads();
+        if (w == 0) {
+            int32_t s = warp_sums[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int32_t t = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += t;
+            }
+            warp_sums[lane] = s;
+        }
+        __syncthreads();
+        int32_t before = carry + (w > 0 ? warp_sums[w - 1] : 0);
+        if (i < n) a.n_off[i] = before + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sums[31];
+        __syncthreads();
+    }
+}
+
 // clip() (hpp:3057-3099) for one row: merge the path runs with the old mask
 // runs in the reference's order and emit changes of the product coverage.
 // The reference stops its single merge loop when either list runs out, so
-// the row where that happens is cut short and later rows stay empty.
-__global__ void k_clip_rows(clip_args a) {
+// the row where that happens is cut short and later rows stay empty.  The
+// running sums of the new runs follow (the clip visibility in force from
+// each run on is min(|sum|, 1), hpp:2568-2570).
+__global__ void k_clip_rows_all(const clip_args *args, int first) {
+    const clip_args &a = args[first + blockIdx.y];
     int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= a.H) return;
     int o_last = a.o_last_row ? *a.o_last_row : a.H - 1;
@@ -959,47 +1022,29 @@ __global__ void k_clip_rows(clip_args a) {
     }
     a.n_len[y] = m;
     if (m > 0) atomicMax(a.n_last_row, y);
-}
-
-// Run capacity of each row of a new clip mask: the path's raw runs plus the
-// old mask's runs (2 per row for the whole canvas).
-__global__ void k_clip_caps(const int64_t *path_off, const int32_t *old_off, int H, int32_t *caps) {
-    int y = blockIdx.x * blockDim.x + threadIdx.x;
-    if (y >= H) return;
-    int p = static_cast<int>(path_off[y + 1] - path_off[y]);
-    int o = old_off ? old_off[y + 1] - old_off[y] : 2;
-    caps[y] = p + o;
-}
-
-// Running sums of a mask's runs (one thread per row): the clip visibility in
-// force from each run on is min(|sum|, 1) (hpp:2568-2570).
-__global__ void k_mask_prefix(const int32_t *off, const int32_t *len, const run *runs, float *sums, int H) {
-    int y = blockIdx.x * blockDim.x + threadIdx.x;
-    if (y >= H) return;
-    const run *r = runs + off[y];
-    float *sm = sums + off[y];
-    int n = len[y];
+    float *sm = a.n_sums + a.n_off[y];
     float sum = 0.0f;
-    for (int j = 0; j < n; ++j) {
-        sum += r[j].delta;
+    for (int j = 0; j < m; ++j) {
+        sum += out[j].delta;
         sm[j] = sum;
     }
 }
 
 // Dense visibility from the mask runs (warp per row).  Pixels outside the
 // row's first..last run are never visited by the reference's walks: 0.
-__global__ void k_mask_fill(const int32_t *off, const int32_t *len, const run *runs, const float *sums, int W,
-                            int H, float *vis) {
-    int lane = threadIdx.x & 31;
-    for (int y = warp_id_global(); y < H; y += warps_total()) {
-        const run *r = runs + off[y];
-        const float *sm = sums + off[y];
-        int n = len[y];
-        int first = n ? r[0].x : 0x7fffffff, last = n ? r[n - 1].x : -1;
-        for (int x = lane; x < W; x += 32) {
+__global__ void k_mask_fill_all(const clip_args *args, int first) {
+    const clip_args &a = args[first + blockIdx.y];
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int y = blockIdx.x * wpb + (threadIdx.x >> 5); y < a.H; y += gridDim.x * wpb) {
+        const run *r = a.n_runs + a.n_off[y];
+        const float *sm = a.n_sums + a.n_off[y];
+        int n = a.n_len[y];
+        int first_x = n ? r[0].x : 0x7fffffff, last_x = n ? r[n - 1].x : -1;
+        for (int x = lane; x < a.W; x += 32) {
             float v = 0.0f;
-            if (x >= first && x <= last) v = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
-            vis[static_cast<size_t>(y) * W + x] = v;
+            if (x >= first_x && x <= last_x) v = lo(fabsf(sum_at(r, sm, n, x)), 1.0f);
+            a.n_vis[static_cast<size_t>(y) * a.W + x] = v;
         }
     }
 }

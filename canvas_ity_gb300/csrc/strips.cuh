@@ -141,14 +141,36 @@ __device__ __forceinline__ int raster_row(const dda_piece &p, int k, int *row_ac
     return left;
 }
 
+// Accumulate pair (piece p, row k) for the warp owning chunks [cb, ce):
+// the row's cells inside the warp's columns of that row, the chunk marks,
+// and (first row only) what the columns left of the warp add.
+__device__ __forceinline__ void raster_pair(const dda_piece &p, int k, int y0, int W, int cpr, int rA, int rB,
+                                            int xa0, int xb1, int *acc, unsigned *cmask, int &carry) {
+    int ly = dda_row_index(p, k) - y0;
+    int xa = ly == rA ? xa0 : 0, xb = ly == rB ? xb1 : W;
+    int x0 = 0x7fffffff, x1 = -1;
+    int left = raster_row(p, k, acc + ly * W, W, xa, xb, x0, x1);
+    if (ly == rA) carry += left;
+    if (x0 <= x1) {
+        int c0 = ly * cpr + (x0 >> 5), c1 = ly * cpr + (x1 >> 5);
+        for (int w = c0 >> 5; w <= (c1 >> 5); ++w) {
+            int lo_b = max(c0, w << 5) - (w << 5), hi_b = min(c1, (w << 5) + 31) - (w << 5);
+            unsigned bits = (hi_b >= 31 ? 0xffffffffu : ((2u << hi_b) - 1u)) & ~((1u << lo_b) - 1u);
+            atomicOr(cmask + w, bits);
+        }
+    }
+}
+
 // One warp's share of a draw over its own chunks [cb, ce) of the strip
 // (row-major, cpr chunks of 32 pixels per row): the entries of the draw's
-// bins whose bands overlap the warp's rows; 32 entries at a time each lane
-// prepares one segment, the (segment, row) pairs inside the warp's rows are
-// dealt to the lanes, and each lane accumulates the row's cells inside the
-// warp's columns of that row.  Touched chunks are marked in cmask (one bit
-// per chunk of the strip).  Returns, in every lane, what the columns left of
-// the warp's first chunk add to its first row.
+// bins whose bands overlap the warp's rows.  32 entries at a time, each lane
+// prepares one segment and counts its rows inside the warp's rows; when no
+// lane has more than one, each does its own, else the (segment, row) pairs
+// are dealt out to the lanes (the prepared segment travels by shuffles).
+// Each pair accumulates the row's cells inside the warp's columns of that
+// row and marks the chunks it touched in cmask (one bit per chunk of the
+// strip).  Returns, in every lane, what the columns left of the warp's first
+// chunk add to its first row.
 __device__ int raster_chunks(const strip_params &P, const strip_cmd &e, int W, int H, int y0, int cb, int ce,
                              int cpr, int *acc, unsigned *cmask, int lane) {
     const int band_h = e.band_h;
@@ -164,14 +186,14 @@ __device__ int raster_chunks(const strip_params &P, const strip_cmd &e, int W, i
     for (int64_t base = first; base < last; base += 32) {
         const int64_t ei = base + lane;
         int cnt = 0, klo = 0;
-        float4 sg = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        dda_piece p;
+        p.nrows = 0;
         if (ei < last) {
-            sg = P.bin_seg[ei];
+            const float4 sg = P.bin_seg[ei];
             int band = b0;
             while (band < b1 && ei >= off[band + 1]) ++band;
             // the warp's rows inside the entry's band
             int ylo = max(ya, band * band_h), yhi = min(yb, (band + 1) * band_h - 1);
-            dda_piece p;
             if (ylo <= yhi && dda_setup(f2(sg.x, sg.y), f2(sg.z, sg.w), p)) {
                 int n = p.nrows < H + 2 ? p.nrows : H + 2;
                 int py0 = static_cast<int>(p.py0);
@@ -185,6 +207,10 @@ __device__ int raster_chunks(const strip_params &P, const strip_cmd &e, int W, i
                 }
             }
         }
+        if (__all_sync(0xffffffffu, cnt <= 1)) {
+            if (cnt == 1) raster_pair(p, klo, y0, W, cpr, rA, rB, xa0, xb1, acc, cmask, carry);
+            continue;
+        }
         int incl = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -192,6 +218,8 @@ __device__ int raster_chunks(const strip_params &P, const strip_cmd &e, int W, i
             if (lane >= o) incl += v;
         }
         const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int first_k = klo - (incl - cnt);   // k of pair q is first_k + q for the owning lane
+        const int vert = p.vert ? 1 : 0;
         for (int q0 = 0; q0 < total; q0 += 32) {
             const int q = q0 + lane;
             // the lane whose inclusive end first exceeds q owns pair q
@@ -203,28 +231,22 @@ __device__ int raster_chunks(const strip_params &P, const strip_cmd &e, int W, i
                 if (v > q) hi_i = mid; else lo_i = mid + 1;
             }
             const int src = lo_i;
-            float ax = __shfl_sync(0xffffffffu, sg.x, src), ay = __shfl_sync(0xffffffffu, sg.y, src);
-            float bx = __shfl_sync(0xffffffffu, sg.z, src), by = __shfl_sync(0xffffffffu, sg.w, src);
-            int s_incl = __shfl_sync(0xffffffffu, incl, src), s_cnt = __shfl_sync(0xffffffffu, cnt, src);
-            int s_klo = __shfl_sync(0xffffffffu, klo, src);
-            if (q < total) {
-                dda_piece p;
-                dda_setup(f2(ax, ay), f2(bx, by), p);
-                int k = s_klo + (q - (s_incl - s_cnt));
-                int ly = dda_row_index(p, k) - y0;
-                int xa = ly == rA ? xa0 : 0, xb = ly == rB ? xb1 : W;
-                int x0 = 0x7fffffff, x1 = -1;
-                int left = raster_row(p, k, acc + ly * W, W, xa, xb, x0, x1);
-                if (ly == rA) carry += left;
-                if (x0 <= x1) {
-                    int c0 = ly * cpr + (x0 >> 5), c1 = ly * cpr + (x1 >> 5);
-                    for (int w = c0 >> 5; w <= (c1 >> 5); ++w) {
-                        int lo_b = max(c0, w << 5) - (w << 5), hi_b = min(c1, (w << 5) + 31) - (w << 5);
-                        unsigned bits = (hi_b >= 31 ? 0xffffffffu : ((2u << hi_b) - 1u)) & ~((1u << lo_b) - 1u);
-                        atomicOr(cmask + w, bits);
-                    }
-                }
-            }
+            dda_piece r;
+            r.fx = __shfl_sync(0xffffffffu, p.fx, src);
+            r.fy = __shfl_sync(0xffffffffu, p.fy, src);
+            r.tx = __shfl_sync(0xffffffffu, p.tx, src);
+            r.ty = __shfl_sync(0xffffffffu, p.ty, src);
+            r.sx = __shfl_sync(0xffffffffu, p.sx, src);
+            r.sy = __shfl_sync(0xffffffffu, p.sy, src);
+            r.sign = __shfl_sync(0xffffffffu, p.sign, src);
+            r.ystep = __shfl_sync(0xffffffffu, p.ystep, src);
+            r.px0 = __shfl_sync(0xffffffffu, p.px0, src);
+            r.py0 = __shfl_sync(0xffffffffu, p.py0, src);
+            r.vert = __shfl_sync(0xffffffffu, vert, src) != 0;
+            r.up = r.ystep > 0.0f;
+            r.nrows = 0;
+            const int k = __shfl_sync(0xffffffffu, first_k, src) + q;
+            if (q < total) raster_pair(r, k, y0, W, cpr, rA, rB, xa0, xb1, acc, cmask, carry);
         }
     }
     return static_cast<int>(__reduce_add_sync(0xffffffffu, static_cast<unsigned>(carry)));
@@ -252,7 +274,7 @@ __device__ __forceinline__ int next_marked(const unsigned *cmask, int c, int c_e
 // pixels, and for BINNED an int32 accumulation image of the strip and one
 // bit per chunk.
 template <int THREADS, bool BINNED>
-__global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
+__global__ void __launch_bounds__(THREADS, BINNED ? 512 / THREADS : 1) k_strips(strip_params P) {
     extern __shared__ float4 px[];
     __shared__ int item_slot;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -276,7 +298,11 @@ __global__ void __launch_bounds__(THREADS) k_strips(strip_params P) {
         const int chunks = rows * cpr;
         // Each warp owns a contiguous range of chunks (row-major) for the
         // whole item, so every pixel is always touched by the same thread.
-        const int per = (chunks + nwarps - 1) / nwarps;
+        // Binned: whole rows per warp when the rows divide evenly enough, so
+        // no two warps walk the same segment rows.
+        int per = (chunks + nwarps - 1) / nwarps;
+        if (BINNED && rows >= nwarps && (rows % nwarps == 0 || rows >= 4 * nwarps))
+            per = ((rows + nwarps - 1) / nwarps) * cpr;
         const int cb = min(chunks, warp * per), ce = min(chunks, cb + per);
         for (int ch = cb; ch < ce; ++ch) {
             int ly = ch / cpr, x = ((ch - ly * cpr) << 5) + lane;

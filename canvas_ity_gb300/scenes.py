@@ -223,11 +223,38 @@ def c3(count: int = 4096, base_seed: int = BASE_SEED) -> List[bytes]:
     return [c3_canvas(i, base_seed) for i in range(count)]
 
 
-def c4_request(index: int, base_seed: int = BASE_SEED) -> bytes:
+def c4_request_shape(index: int, base_seed: int = BASE_SEED):
+    """(width, height, paths, clip) of c4_request(index) without building it."""
     rng = _rng(base_seed * 11 + index)
     w, h = _log_uniform(rng, 32, 2048), _log_uniform(rng, 32, 2048)
     paths = int(rng.integers(1, 513))
-    return mixed_canvas(base_seed + 1000003 + index, w, h, paths, rng.uniform() < 0.1)
+    return w, h, paths, bool(rng.uniform() < 0.1)
+
+
+def c4_request(index: int, base_seed: int = BASE_SEED) -> bytes:
+    w, h, paths, clip = c4_request_shape(index, base_seed)
+    return mixed_canvas(base_seed + 1000003 + index, w, h, paths, clip)
+
+
+def c4_parity_sample(count: int = 16, pool: int = 4000, base_seed: int = BASE_SEED):
+    """Indices of c4 requests that cover the distribution's extremes: the
+    largest canvases, the most paths, clipped ones, and the rest spread over
+    the pool."""
+    shapes = [c4_request_shape(i, base_seed) for i in range(pool)]
+    by_px = sorted(range(pool), key=lambda i: -shapes[i][0] * shapes[i][1])
+    by_paths = sorted(range(pool), key=lambda i: -shapes[i][2])
+    clipped = [i for i in range(pool) if shapes[i][3]]
+    chosen = []
+    for i in by_px[:count // 4] + by_paths[:count // 4] + clipped[:count // 8]:
+        if i not in chosen:
+            chosen.append(i)
+    step = max(1, pool // count)
+    for i in range(0, pool, step):
+        if len(chosen) >= count:
+            break
+        if i not in chosen:
+            chosen.append(i)
+    return chosen[:count]
 
 
 def small_scene(config: str, seed: int) -> bytes:

@@ -113,6 +113,41 @@ def test_c2_full_size_vs_oracle(engine):
         assert np.array_equal(got, oracle_images(tb, coverage="binned")[-1])
 
 
+_c4_cache = {}
+
+
+def c4_sample():
+    """16 serving requests of config 4 (sides log-uniform 32-2048, 1-512
+    paths) covering its extremes, with the oracle's reads of each under the
+    reference restatement and under the binned one (computed once, in
+    parallel, for all modes)."""
+    if not _c4_cache:
+        from concurrent.futures import ThreadPoolExecutor
+        ids = scenes.c4_parity_sample(16)
+        tbs = [scenes.c4_request(i) for i in ids]
+        oracle.replay(tbs[0])
+        oracle.replay(tbs[0], ties="sign", trig="cr", coverage="binned")
+        with ThreadPoolExecutor(16) as ex:
+            ref = list(ex.map(lambda t: oracle.replay(t)[0], tbs))
+            binned = list(ex.map(lambda t: oracle.replay(t, ties="sign", trig="cr", coverage="binned")[0], tbs))
+        _c4_cache.update(ids=ids, traces=tbs, ref=ref, binned=binned)
+    return _c4_cache
+
+
+def test_c4_request_sample_vs_oracle(engine):
+    """Config 4's requests, including its largest canvases (up to 2048 x
+    2048) and path counts (up to 512), rendered together in one frame as the
+    server renders them."""
+    c4 = c4_sample()
+    outs = native.render_batch(c4["traces"], G.MODES[engine][0])
+    for i, (tb, raw) in enumerate(zip(c4["traces"], outs)):
+        what = f"c4 request {c4['ids'][i]}"
+        for g, w in zip(G.split_images(tb, raw), G.split_images(tb, c4["ref"][i])):
+            assert_images_close(g, w, what, engine)
+        if engine == "tile":
+            assert raw == c4["binned"][i], what
+
+
 def assert_float_canvas_exact(tb, what, mode):
     """The GPU's final premultiplied linear canvas equals, bit for bit, the
     oracle built with the GPU's order for runs of one cell that the
