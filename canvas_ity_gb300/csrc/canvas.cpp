@@ -22,7 +22,10 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <new>
+#include <unordered_map>
 #include <vector>
 
 namespace canvas_ity {
@@ -84,7 +87,8 @@ struct font_face {
     std::vector<unsigned char> data;
     int cmap, glyf, head, hhea, hmtx, loca, maxp, os_2;
     float scale;
-    font_face() : cmap(0), glyf(0), head(0), hhea(0), hmtx(0), loca(0), maxp(0), os_2(0), scale(0) {}
+    uint64_t hash;   // of the loaded tables (the glyph cache's key)
+    font_face() : cmap(0), glyf(0), head(0), hhea(0), hmtx(0), loca(0), maxp(0), os_2(0), scale(0), hash(0) {}
 };
 
 struct saved_state {
@@ -141,7 +145,7 @@ struct canvas_state {
     void make_paint(const brush &br, bool clamp_edges, bool force_solid, cy_paint &p);
     void make_state(cy_draw_state &s, bool with_shadow);
     void draw_lines(const brush &br, bool clamp_edges, bool force_solid, bool with_shadow);
-    void draw_path(const brush &br);
+    void draw_path(const brush &br, bool with_rule = true);
     void stroke_path(const brush &br);
     void line_to(float x, float y);
     void move_to(float x, float y);
@@ -469,38 +473,71 @@ static int s32at(const bytes &d, int i) {
     return (d[p] << 24 | d[p + 1] << 16 | d[p + 2] << 8 | d[p + 3]);
 }
 
-void canvas_state::glyph_outline(int glyph, float angular) {
+// ---- glyph outlines (add_glyph, hpp:1533-1846) ----
+// A glyph's TrueType record decoded once per font and glyph, for every
+// canvas and request of the process: a composite glyph's components with
+// their transforms, or a simple glyph's points in font units with their
+// on-curve flags and contour ends.  Keyed by a hash of the font's loaded
+// tables and the glyph index, and checked against the table bytes' size.
+struct glyph_rec {
+    bool empty = false;
+    bool composite = false;
+    struct component {
+        int glyph;
+        bool xy_args, more;
+        float a, b, c, d, e, f;
+    };
+    std::vector<component> parts;
+    std::vector<int> ends;              // last point index of each contour
+    std::vector<float> x, y;            // font units
+    std::vector<unsigned char> on;
+};
+
+static std::mutex g_glyph_lock;
+static std::unordered_map<uint64_t, std::shared_ptr<const glyph_rec>> g_glyphs;
+static size_t g_glyph_points = 0;       // points held (the cache stops growing at 64 M)
+
+static std::shared_ptr<const glyph_rec> decode_glyph(const font_face &face, int glyph) {
     const bytes &d = face.data;
+    auto rec = std::make_shared<glyph_rec>();
     int loc_format = u16at(d, face.head + 50);
     int offset = face.glyf + (loc_format ? s32at(d, face.loca + glyph * 4) : u16at(d, face.loca + glyph * 2) * 2);
     int next = face.glyf + (loc_format ? s32at(d, face.loca + glyph * 4 + 4) : u16at(d, face.loca + glyph * 2 + 2) * 2);
-    if (offset == next) return;
+    if (offset == next) {
+        rec->empty = true;
+        return rec;
+    }
     int contours = s16at(d, offset);
     if (contours < 0) {
         // composite glyph: each component under its own transform
+        rec->composite = true;
         offset += 10;
         for (;;) {
             int flags = u16at(d, offset);
-            int component = u16at(d, offset + 2);
-            if (!(flags & 2)) return;
-            float e = static_cast<float>(flags & 1 ? s16at(d, offset + 4) : s8at(d, offset + 4));
-            float f = static_cast<float>(flags & 1 ? s16at(d, offset + 6) : s8at(d, offset + 5));
+            glyph_rec::component cp;
+            cp.glyph = u16at(d, offset + 2);
+            cp.xy_args = (flags & 2) != 0;
+            cp.more = (flags & 32) != 0;
+            cp.a = cp.b = cp.c = cp.d = cp.e = cp.f = 0.0f;
+            if (!cp.xy_args) {
+                rec->parts.push_back(cp);
+                break;
+            }
+            cp.e = static_cast<float>(flags & 1 ? s16at(d, offset + 4) : s8at(d, offset + 4));
+            cp.f = static_cast<float>(flags & 1 ? s16at(d, offset + 6) : s8at(d, offset + 5));
             offset += flags & 1 ? 8 : 6;
-            float a = flags & 200 ? static_cast<float>(s16at(d, offset)) / 16384.0f : 1.0f;
-            float b = flags & 128 ? static_cast<float>(s16at(d, offset + 2)) / 16384.0f : 0.0f;
-            float c = flags & 128 ? static_cast<float>(s16at(d, offset + 4)) / 16384.0f : 0.0f;
-            float dd = flags & 8 ? a
-                     : flags & 64 ? static_cast<float>(s16at(d, offset + 2)) / 16384.0f
-                     : flags & 128 ? static_cast<float>(s16at(d, offset + 6)) / 16384.0f
-                     : 1.0f;
+            cp.a = flags & 200 ? static_cast<float>(s16at(d, offset)) / 16384.0f : 1.0f;
+            cp.b = flags & 128 ? static_cast<float>(s16at(d, offset + 2)) / 16384.0f : 0.0f;
+            cp.c = flags & 128 ? static_cast<float>(s16at(d, offset + 4)) / 16384.0f : 0.0f;
+            cp.d = flags & 8 ? cp.a
+                 : flags & 64 ? static_cast<float>(s16at(d, offset + 2)) / 16384.0f
+                 : flags & 128 ? static_cast<float>(s16at(d, offset + 6)) / 16384.0f
+                 : 1.0f;
             offset += flags & 8 ? 2 : flags & 64 ? 4 : flags & 128 ? 8 : 0;
-            affine sf = fwd, si = inv;
-            transform(a, b, c, dd, e, f);
-            glyph_outline(component, angular);
-            fwd = sf;
-            inv = si;
-            if (!(flags & 32)) return;
+            rec->parts.push_back(cp);
+            if (!cp.more) break;
         }
+        return rec;
     }
     int hmetrics = u16at(d, face.hhea + 34);
     int lsb = glyph < hmetrics ? s16at(d, face.hmtx + glyph * 4 + 2)
@@ -519,8 +556,63 @@ void canvas_state::glyph_outline(int glyph, float angular) {
     int xs = flags_at + flags_size, ys = xs + x_size;
     int x = lsb - x_min, y = 0, fl = 0, rep = 0, idx = 0;
     for (int ct = 0; ct < contours; ++ct) {
-        int begin = idx;
         int end = u16at(d, offset + 10 + ct * 2);
+        for (; idx <= end; ++idx) {
+            if (rep) --rep;
+            else {
+                fl = u8at(d, flags_at++);
+                if (fl & 8) rep = u8at(d, flags_at++);
+            }
+            if (fl & 2) x += (u8at(d, xs) * (fl & 16 ? 1 : -1));
+            else if (!(fl & 16)) x += s16at(d, xs);
+            if (fl & 4) y += (u8at(d, ys) * (fl & 32 ? 1 : -1));
+            else if (!(fl & 32)) y += s16at(d, ys);
+            xs += fl & 2 ? 1 : fl & 16 ? 0 : 2;
+            ys += fl & 4 ? 1 : fl & 32 ? 0 : 2;
+            rec->x.push_back(static_cast<float>(x));
+            rec->y.push_back(static_cast<float>(y));
+            rec->on.push_back(static_cast<unsigned char>(fl & 1));
+        }
+        rec->ends.push_back(end);
+    }
+    return rec;
+}
+
+static std::shared_ptr<const glyph_rec> cached_glyph(const font_face &face, int glyph) {
+    const uint64_t key = (face.hash ^ (static_cast<uint64_t>(glyph) * 0x9e3779b97f4a7c15ull)) ^ face.data.size();
+    {
+        std::lock_guard<std::mutex> hold(g_glyph_lock);
+        auto it = g_glyphs.find(key);
+        if (it != g_glyphs.end()) return it->second;
+    }
+    std::shared_ptr<const glyph_rec> rec = decode_glyph(face, glyph);
+    std::lock_guard<std::mutex> hold(g_glyph_lock);
+    if (g_glyph_points + rec->x.size() <= (size_t(64) << 20)) {
+        g_glyph_points += rec->x.size();
+        g_glyphs.emplace(key, rec);
+    }
+    return rec;
+}
+
+void canvas_state::glyph_outline(int glyph, float angular) {
+    std::shared_ptr<const glyph_rec> rec = cached_glyph(face, glyph);
+    if (rec->empty) return;
+    if (rec->composite) {
+        for (const glyph_rec::component &cp : rec->parts) {
+            if (!cp.xy_args) return;
+            affine sf = fwd, si = inv;
+            transform(cp.a, cp.b, cp.c, cp.d, cp.e, cp.f);
+            glyph_outline(cp.glyph, angular);
+            fwd = sf;
+            inv = si;
+            if (!cp.more) return;
+        }
+        return;
+    }
+    int idx = 0;
+    for (size_t ct = 0; ct < rec->ends.size(); ++ct) {
+        int begin = idx;
+        int end = rec->ends[ct];
         v2 bp = mk(0, 0), ep = mk(0, 0);
         bool bon = false, eon = false;
         // Each contour is emitted as points and cubics: flattened into
@@ -550,19 +642,8 @@ void canvas_state::glyph_outline(int glyph, float angular) {
             }
         };
         for (; idx <= end; ++idx) {
-            if (rep) --rep;
-            else {
-                fl = u8at(d, flags_at++);
-                if (fl & 8) rep = u8at(d, flags_at++);
-            }
-            if (fl & 2) x += (u8at(d, xs) * (fl & 16 ? 1 : -1));
-            else if (!(fl & 16)) x += s16at(d, xs);
-            if (fl & 4) y += (u8at(d, ys) * (fl & 32 ? 1 : -1));
-            else if (!(fl & 32)) y += s16at(d, ys);
-            xs += fl & 2 ? 1 : fl & 16 ? 0 : 2;
-            ys += fl & 4 ? 1 : fl & 32 ? 0 : 2;
-            v2 pt = apply(fwd, mk(static_cast<float>(x), static_cast<float>(y)));
-            int on = fl & 1;
+            v2 pt = apply(fwd, mk(rec->x[static_cast<size_t>(idx)], rec->y[static_cast<size_t>(idx)]));
+            int on = rec->on[static_cast<size_t>(idx)];
             if (idx == begin) {
                 bp = pt;
                 bon = on;
@@ -769,13 +850,15 @@ void canvas_state::draw_lines(const brush &br, bool clamp_edges, bool force_soli
                        static_cast<int>(counts.size()), &p, &s));
 }
 
-void canvas_state::draw_path(const brush &br) {
+// A filled path flattened on the device; with_rule false fills nonzero
+// whatever the fill rule (text, as with strokes and rectangles).
+void canvas_state::draw_path(const brush &br, bool with_rule) {
     if (singular()) return;
     cy_paint p;
     cy_draw_state s;
     make_paint(br, false, false, p);
     make_state(s, true);
-    s.fill_rule = even_odd ? 1 : 0;
+    s.fill_rule = with_rule && even_odd ? 1 : 0;
     counts.resize(path.subs.size());
     for (size_t i = 0; i < path.subs.size(); ++i) counts[i] = static_cast<int>(path.subs[i].count);
     note(cy_fill_path(ctx, reinterpret_cast<const float *>(path.pts.data()), counts.data(),
@@ -1230,14 +1313,30 @@ bool canvas::set_font(unsigned char const *font, int nbytes, float size) {
         }
     }
     if (face.data.empty()) return false;
+    if (font && nbytes) {
+        // FNV-1a of the loaded tables: the key of their glyph outlines
+        uint64_t hsh = 1469598103934665603ull;
+        for (unsigned char ch : face.data) hsh = (hsh ^ ch) * 1099511628211ull;
+        face.hash = hsh;
+    }
     int upem = detail::u16at(face.data, face.head + 18);
     face.scale = size / static_cast<float>(upem);
     return true;
 }
 void canvas::fill_text(char const *text, float x, float y, float maxw) {
+    // hpp:3277-3284: the glyph outlines go to the device as cubics and are
+    // flattened there like any filled path; the current path is left as it was.
     sync_public_state();
-    self->text_outline(text, mk(x, y), maxw, false);
-    self->draw_lines(self->fill, false, false, true);
+    detail::canvas_state &s = *self;
+    detail::polyline saved;
+    saved.pts.swap(s.path.pts);
+    saved.subs.swap(s.path.subs);
+    s.outline_cubics = true;
+    s.text_outline(text, mk(x, y), maxw, false);
+    s.outline_cubics = false;
+    if (!s.path.subs.empty()) s.draw_path(s.fill, false);
+    s.path.pts.swap(saved.pts);
+    s.path.subs.swap(saved.subs);
 }
 void canvas::stroke_text(char const *text, float x, float y, float maxw) {
     sync_public_state();

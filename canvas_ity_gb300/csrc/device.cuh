@@ -375,7 +375,7 @@ __device__ float4 paint_at(const command &c, const paint_src &s, float px, float
         int bottom = static_cast<int>(ceilf(y + scale_y * 2.0f));
         float4 total = none;
         float wsum = 0.0f;
-        const float4 *tex = s.texels + c.pat_first;
+        const float4 *tex = c.pat_ptr ? reinterpret_cast<const float4 *>(c.pat_ptr) : s.texels + c.pat_first;
         // The column weights and wrapped columns are the same for every row
         // of taps: computed once (same values, same order of the sums).
         constexpr int kTaps = 8;

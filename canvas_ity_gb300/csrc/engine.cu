@@ -26,6 +26,7 @@
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <unordered_map>
 #include <atomic>
 #include <chrono>
 #include <vector>
@@ -684,7 +685,7 @@ void frame::gather() {
             if (c.kind == CMD_FILL || c.kind == CMD_CLIP) {
                 c.first += c.geom == 0 ? b.hpts : c.geom == 1 ? b.items : b.groups;
                 c.stop_first += b.stop;
-                c.pat_first += b.tex;
+                if (!c.pat_ptr) c.pat_first += b.tex;
             } else if (c.kind == CMD_PUT) {
                 c.put_first += b.put;
             } else if (c.kind == CMD_GET) {
@@ -1668,7 +1669,146 @@ void bounds_of(const float *xy, size_t n, command &c) {
     c.gy1 = bad ? 1000000000 : clampi(y1) + 1;
 }
 
-int fill_paint(queue &q, const cy_paint *p, command &c) {
+// ---------------------------------------------------- device image cache
+// Pattern and draw_image texels that recur -- the same image drawn on many
+// canvases of a frame, or by many serving requests -- are kept on the device,
+// already linearised and premultiplied (what k_pattern_prep makes of them,
+// hpp:2841-2864), keyed by their size and bytes.  An image is cached the
+// second time it is seen; the first time it goes up with its frame as
+// usual.  The texels live in 32 MiB pool chunks that are never moved or
+// freed while the process runs (frames and captured graphs hold pointers
+// into them); the pool stops growing at 1 GiB per device, after which new
+// images go up with their frames again.
+namespace {
+
+constexpr size_t kTexChunk = size_t(32) << 20;
+constexpr size_t kTexCap = size_t(1) << 30;
+constexpr int kTexDevices = 64;
+
+struct tex_entry {
+    int w = 0, h = 0;
+    std::vector<uchar4> px;          // the source bytes (exact match on lookup)
+    const float4 *dev = nullptr;
+};
+
+struct tex_cache {
+    std::vector<void *> chunks;
+    size_t used = 0;                 // bytes used in the last chunk
+    size_t total = 0;                // bytes of all chunks
+    std::unordered_map<uint64_t, std::vector<tex_entry>> map;
+    std::unordered_map<uint64_t, int> seen;   // hash -> sightings of uncached images
+    cudaStream_t stream = nullptr;
+    void *stage = nullptr;           // device copy of the bytes being converted
+    size_t stage_cap = 0;
+    float *lut = nullptr;
+    int64_t hits = 0, inserts = 0;
+};
+
+std::mutex g_tex_lock;
+tex_cache g_tex[kTexDevices];
+
+uint64_t image_hash(const uchar4 *px, size_t n, int w, int h) {
+    // FNV-1a over the bytes, 8 at a time, seeded with the size.
+    uint64_t x = 1469598103934665603ull ^ (static_cast<uint64_t>(w) << 32 | static_cast<uint32_t>(h));
+    const unsigned char *b = reinterpret_cast<const unsigned char *>(px);
+    size_t bytes = n * 4, i = 0;
+    for (; i + 8 <= bytes; i += 8) {
+        uint64_t v;
+        std::memcpy(&v, b + i, 8);
+        x = (x ^ v) * 1099511628211ull;
+    }
+    for (; i < bytes; ++i) x = (x ^ b[i]) * 1099511628211ull;
+    return x;
+}
+
+// The cached texels of a w x h RGBA8 image on device `dev`, or null when it
+// is not (yet) cached.  Inserting converts the image on the cache's stream
+// and waits for it, so the texels are ready before any frame refers to them.
+const float4 *tex_cache_lookup(int dev, const uchar4 *px, int w, int h) {
+    if (dev < 0 || dev >= kTexDevices) return nullptr;
+    const size_t n = static_cast<size_t>(w) * static_cast<size_t>(h);
+    const size_t need = (n * sizeof(float4) + 255) & ~static_cast<size_t>(255);
+    if (need > kTexChunk) return nullptr;
+    const uint64_t key = image_hash(px, n, w, h);
+    std::lock_guard<std::mutex> hold(g_tex_lock);
+    tex_cache &tc = g_tex[dev];
+    auto it = tc.map.find(key);
+    if (it != tc.map.end())
+        for (const tex_entry &e : it->second)
+            if (e.w == w && e.h == h && std::memcmp(e.px.data(), px, n * 4) == 0) {
+                ++tc.hits;
+                return e.dev;
+            }
+    if (tc.seen.size() > 65536) tc.seen.clear();
+    if (++tc.seen[key] < 2) return nullptr;
+    // second sighting: insert
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != dev) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (tc.chunks.empty() || tc.used + need > kTexChunk) {
+        if (tc.total + kTexChunk > kTexCap) return nullptr;
+        void *chunk = nullptr;
+        if (cudaMalloc(&chunk, kTexChunk) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        tc.chunks.push_back(chunk);
+        tc.total += kTexChunk;
+        tc.used = 0;
+    }
+    if (!tc.stream && cudaStreamCreateWithFlags(&tc.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        tc.stream = nullptr;
+        return nullptr;
+    }
+    if (!tc.lut) {
+        if (cudaMalloc(&tc.lut, 256 * sizeof(float)) != cudaSuccess ||
+            cudaMemcpy(tc.lut, linear_lut_host(), 256 * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            if (tc.lut) cudaFree(tc.lut);
+            tc.lut = nullptr;
+            return nullptr;
+        }
+    }
+    if (tc.stage_cap < n * 4) {
+        if (tc.stage) cudaFree(tc.stage);
+        tc.stage = nullptr;
+        tc.stage_cap = 0;
+        if (cudaMalloc(&tc.stage, n * 4) != cudaSuccess) {
+            cudaGetLastError();
+            tc.stage = nullptr;
+            return nullptr;
+        }
+        tc.stage_cap = n * 4;
+    }
+    float4 *dst = reinterpret_cast<float4 *>(static_cast<char *>(tc.chunks.back()) + tc.used);
+    int ni = static_cast<int>(n);
+    if (cudaMemcpyAsync(tc.stage, px, n * 4, cudaMemcpyHostToDevice, tc.stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    k_pattern_prep<<<(ni + 255) / 256, 256, 0, tc.stream>>>(static_cast<const uchar4 *>(tc.stage), dst, ni, tc.lut);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(tc.stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    tc.used += need;
+    tex_entry e;
+    e.w = w;
+    e.h = h;
+    e.px.assign(px, px + n);
+    e.dev = dst;
+    tc.map[key].push_back(std::move(e));
+    tc.seen.erase(key);
+    ++tc.inserts;
+    return dst;
+}
+
+}  // namespace
+
+int fill_paint(queue &q, const cy_paint *p, command &c, int device) {
     c.paint = p->kind;
     c.clamp = p->clamp_edges;
     for (int i = 0; i < 6; ++i) c.inv[i] = p->inverse[i];
@@ -1677,6 +1817,7 @@ int fill_paint(queue &q, const cy_paint *p, command &c) {
     c.r0 = p->start_radius; c.r1 = p->end_radius;
     c.stop_first = c.stop_count = 0;
     c.pat_first = c.pat_w = c.pat_h = c.pat_rep = 0;
+    c.pat_ptr = 0;
     if (p->kind == CY_PAINT_LINEAR || p->kind == CY_PAINT_RADIAL) {
         if (p->n_stops <= 0) { c.paint = CY_PAINT_NONE; return CY_OK; }
         if (!p->stop_offsets || !p->stop_colors) return CY_EINVAL;
@@ -1692,13 +1833,18 @@ int fill_paint(queue &q, const cy_paint *p, command &c) {
         if (!p->pattern || p->pattern_width <= 0 || p->pattern_height <= 0) return CY_EINVAL;
         size_t n = static_cast<size_t>(p->pattern_width) * static_cast<size_t>(p->pattern_height);
         if (q.texels.size() + n > static_cast<size_t>(INT32_MAX)) return CY_EINVAL;
-        c.pat_first = static_cast<int32_t>(q.texels.size());
         c.pat_w = p->pattern_width;
         c.pat_h = p->pattern_height;
         c.pat_rep = p->repetition;
         const uchar4 *src = reinterpret_cast<const uchar4 *>(p->pattern);
-        q.texels.insert(q.texels.end(), src, src + n);
-        q.bytes += n * 4;
+        if (const float4 *cached = tex_cache_lookup(device, src, p->pattern_width, p->pattern_height)) {
+            c.pat_ptr = static_cast<int64_t>(reinterpret_cast<uintptr_t>(cached));
+            c.pat_first = 0;
+        } else {
+            c.pat_first = static_cast<int32_t>(q.texels.size());
+            q.texels.insert(q.texels.end(), src, src + n);
+            q.bytes += n * 4;
+        }
     } else if (p->kind != CY_PAINT_NONE && p->kind != CY_PAINT_SOLID) {
         return CY_EINVAL;
     }
@@ -1877,7 +2023,7 @@ int queue_draw(cy_ctx *c, const float *points, const int *counts, int n_sub, boo
     cull_rects rects = {static_cast<float>(c->W), static_cast<float>(c->H), cmd.shadow != 0,
                         static_cast<float>(c->W + 2 * cmd.sh_border), static_cast<float>(c->H + 2 * cmd.sh_border),
                         cmd.sh_offx, cmd.sh_offy};
-    int rc = fill_paint(q, paint, cmd);
+    int rc = fill_paint(q, paint, cmd, c->device);
     if (rc == CY_OK) rc = queue_geometry(q, points, counts, n_sub, bezier, cmd, rects);
     if (rc != CY_OK) {
         q.stop_off.resize(stops);
@@ -1989,7 +2135,7 @@ int queue_stroke(cy_ctx *c, const float *points, const int *counts, const int *c
     size_t stops = q.stop_off.size(), tex = q.texels.size();
     fill_state(state, cmd);
     cmd.fill_rule = 0;   // render_main fills the outline nonzero
-    int rc = fill_paint(q, paint, cmd);
+    int rc = fill_paint(q, paint, cmd, c->device);
     if (rc != CY_OK) {
         q.stop_off.resize(stops);
         q.stop_col.resize(stops);
@@ -2049,6 +2195,27 @@ void cy_ctx_set_transient(cy_ctx *c, int transient) {
     if (c) c->transient = transient != 0;
 }
 void cy_set_coverage(int exact) { g_coverage.store(exact ? 1 : 0); }
+
+int cy_image_cache_stats(long long *stats, int n) {
+    if (!stats) return CY_EINVAL;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kTexDevices) {
+        cudaGetLastError();
+        return CY_ENODEV;
+    }
+    std::lock_guard<std::mutex> hold(g_tex_lock);
+    const tex_cache &tc = g_tex[dev];
+    long long entries = 0, texels = 0;
+    for (const auto &kv : tc.map)
+        for (const tex_entry &e : kv.second) {
+            ++entries;
+            texels += static_cast<long long>(e.w) * e.h;
+        }
+    long long v[] = {tc.hits, tc.inserts, entries, texels * 16, static_cast<long long>(tc.total)};
+    int m = static_cast<int>(sizeof(v) / sizeof(v[0]));
+    for (int i = 0; i < n && i < m; ++i) stats[i] = v[i];
+    return m;
+}
 int cy_get_coverage(void) { return g_coverage.load(); }
 void cy_set_deferred(int deferred) { g_deferred = deferred; }
 void cy_set_strip_config(int pixels, int threads) {

@@ -60,6 +60,10 @@ struct __align__(16) command {
     int64_t get_out;
     // conservative bounds of the geometry, device pixels (host-computed)
     int32_t gx0, gy0, gx1, gy1;
+    // pattern texels held by the device image cache (0: pat_first indexes
+    // the frame's own texels)
+    int64_t pat_ptr;
+    int64_t pad_;
 };
 
 // Exact bounds of the nonzero coverage deltas a scan conversion produced.

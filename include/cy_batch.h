@@ -43,6 +43,17 @@ void cy_set_strip_config(int strip_pixels, int threads);
 void cy_set_coverage(int exact);
 int cy_get_coverage(void);
 
+/* Device image cache (no counterpart in the reference, which keeps each
+ * pattern and draw_image source with its canvas): an image (set_pattern,
+ * draw_image; hpp:568-600, 1030-1067) drawn a second time, on any canvas or
+ * request, is kept on the current device already linearised and
+ * premultiplied, and later draws of the same bytes use it instead of
+ * uploading and converting their own copy.  Up to 1 GiB of texels per
+ * device, kept until the process exits.  Statistics for the current device
+ * (first n of): hits, images inserted, images held, texel bytes held, pool
+ * bytes. */
+int cy_image_cache_stats(long long *stats, int n);
+
 /* Build a frame over the queued work of n contexts, upload it and run it
  * once.  engine: 0 tile, 1 plain.  The contexts' queues are consumed by
  * cy_frame_finish. */
