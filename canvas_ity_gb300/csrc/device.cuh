@@ -376,6 +376,43 @@ __device__ float4 paint_at(const command &c, const paint_src &s, float px, float
         float4 total = none;
         float wsum = 0.0f;
         const float4 *tex = c.pat_ptr ? reinterpret_cast<const float4 *>(c.pat_ptr) : s.texels + c.pat_first;
+        if (right - left == 4 && bottom - top == 4) {
+            // The usual case (no minification): 4 x 4 taps with the weights
+            // and wrapped columns in registers; the same sums in the same order.
+            float wx[4];
+            int col[4];
+            int xx = left % c.pat_w;
+            if (xx < 0) xx += c.pat_w;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int px_ = left + j;
+                wx[j] = keys_weight(fabsf(rx * (static_cast<float>(px_) - x)));
+                col[j] = c.clamp ? (px_ < 0 ? 0 : (px_ > c.pat_w - 1 ? c.pat_w - 1 : px_)) : xx;
+                if (++xx == c.pat_w) xx = 0;
+            }
+            int yy = top % c.pat_h;
+            if (yy < 0) yy += c.pat_h;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                int py_ = top + i;
+                float wy = keys_weight(fabsf(ry * (static_cast<float>(py_) - y)));
+                int ry_ = c.clamp ? (py_ < 0 ? 0 : (py_ > c.pat_h - 1 ? c.pat_h - 1 : py_)) : yy;
+                if (++yy == c.pat_h) yy = 0;
+                const float4 *rowp = tex + static_cast<size_t>(ry_) * c.pat_w;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    float w = wx[j] * wy;
+                    float4 t = rowp[col[j]];
+                    total.x = total.x + t.x * w;
+                    total.y = total.y + t.y * w;
+                    total.z = total.z + t.z * w;
+                    total.w = total.w + t.w * w;
+                    wsum += w;
+                }
+            }
+            float r = 1.0f / wsum;
+            return make_float4(total.x * r, total.y * r, total.z * r, total.w * r);
+        }
         // The column weights and wrapped columns are the same for every row
         // of taps: computed once (same values, same order of the sums).
         constexpr int kTaps = 8;
