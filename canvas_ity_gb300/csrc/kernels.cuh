@@ -376,23 +376,42 @@ struct bin_tables {
 
 template <bool EMIT, bool CLIPPED>
 __global__ void k_bin(job_tables t, bin_tables bt, int total_segments) {
-    int stride = gridDim.x * blockDim.x;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < total_segments; s += stride) {
-        float2 a, b;
-        int ji = segment_of<CLIPPED>(t, s, a, b);
-        const scan_job &j = t.jobs[ji];
-        if (!j.binned) continue;
-        dda_piece p;
-        if (!dda_setup(a, b, p)) continue;
-        int r0, r1;
-        dda_rows(p, j.rows, r0, r1);
-        if (r0 > r1) continue;
-        for (int band = r0 / j.band_h; band <= r1 / j.band_h; ++band) {
-            int bin = j.bin_base + band;
+    // A warp's 32 consecutive segments mostly share their job and bands:
+    // lanes adding to the same bin are grouped, so each bin takes one
+    // atomic per warp, and each lane writes at the group's base plus its rank.
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total_segments; base += stride) {
+        const int s = base + lane;
+        int bin0 = 0, nb = 0;
+        float2 a = f2(0.0f, 0.0f), b = a;
+        if (s < total_segments) {
+            int ji = segment_of<CLIPPED>(t, s, a, b);
+            const scan_job &j = t.jobs[ji];
+            dda_piece p;
+            if (j.binned && dda_setup(a, b, p)) {
+                int r0, r1;
+                dda_rows(p, j.rows, r0, r1);
+                if (r0 <= r1) {
+                    bin0 = j.bin_base + r0 / j.band_h;
+                    nb = r1 / j.band_h - r0 / j.band_h + 1;
+                }
+            }
+        }
+        const int rounds = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(nb)));
+        for (int k = 0; k < rounds; ++k) {
+            const int bin = k < nb ? bin0 + k : -1;
+            const unsigned peers = __match_any_sync(0xffffffffu, bin);
+            if (bin < 0) continue;
+            const int leader = __ffs(peers) - 1;
+            const int rank = __popc(peers & ((1u << lane) - 1u));
             if (!EMIT) {
-                atomicAdd(bt.cnt + bin, 1);
+                if (lane == leader) atomicAdd(bt.cnt + bin, __popc(peers));
             } else {
-                int64_t at = bt.off[bin] + atomicAdd(bt.cur + bin, 1);
+                int first = 0;
+                if (lane == leader) first = atomicAdd(bt.cur + bin, __popc(peers));
+                first = __shfl_sync(peers, first, leader);
+                int64_t at = bt.off[bin] + first + rank;
                 if (at < bt.off[bin + 1]) bt.seg[at] = make_float4(a.x, a.y, b.x, b.y);
             }
         }

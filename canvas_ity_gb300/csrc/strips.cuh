@@ -367,6 +367,11 @@ __global__ void __launch_bounds__(THREADS, BINNED ? 512 / THREADS : 1) k_strips(
             }
             if (BINNED) {
                 if (cb >= ce || (!clearing && (c.gy1 < wy0 || c.gy0 > wy1))) continue;
+                // the draw's fields every pixel needs, read once
+                const int rule = c.fill_rule, paint = c.paint;
+                const float alpha = c.alpha;
+                const float4 solid = make_float4(c.color[0], c.color[1], c.color[2], c.color[3]);
+                const float *vis_plane = e.vis;
                 const int carry0 = raster_chunks(P, e, W, cv.H, y0, cb, ce, cpr, acc, cmask, lane);
                 __syncwarp();
                 const int rA = cb / cpr, rB = (ce - 1) / cpr;
@@ -378,7 +383,7 @@ __global__ void __launch_bounds__(THREADS, BINNED ? 512 / THREADS : 1) k_strips(
                     int *arow = acc + ly * W;
                     while (ch < c_hi) {
                         const bool marked = (cmask[ch >> 5] >> (ch & 31)) & 1u;
-                        if (!marked && !clearing && cover_of(static_cast<float>(carry) * kAccInv, c.fill_rule) < kVisible) {
+                        if (!marked && !clearing && cover_of(static_cast<float>(carry) * kAccInv, rule) < kVisible) {
                             // no area here and the sum so far is invisible:
                             // on to the next chunk that holds area
                             ch = next_marked(cmask, ch + 1, c_hi);
@@ -401,11 +406,13 @@ __global__ void __launch_bounds__(THREADS, BINNED ? 512 / THREADS : 1) k_strips(
                         if (marked) carry = __shfl_sync(0xffffffffu, sum, 31);
                         ++ch;
                         if (x >= W) continue;
-                        float cov = cover_of(static_cast<float>(sum) * kAccInv, c.fill_rule);
-                        float vis = e.vis ? e.vis[static_cast<size_t>(y) * W + x] : 1.0f;
+                        float cov = cover_of(static_cast<float>(sum) * kAccInv, rule);
+                        float vis = vis_plane ? vis_plane[static_cast<size_t>(y) * W + x] : 1.0f;
                         if ((cov >= kVisible || clearing) && vis >= kVisible) {
-                            float4 pp = paint_at(c, P.src, static_cast<float>(x) + 0.5f, static_cast<float>(y) + 0.5f);
-                            float kk = cov * c.alpha;
+                            // paint_pixel (hpp:2265-2377); a solid colour is the brush's own
+                            float4 pp = paint == 1 ? solid
+                                      : paint_at(c, P.src, static_cast<float>(x) + 0.5f, static_cast<float>(y) + 0.5f);
+                            float kk = cov * alpha;
                             float4 fore = make_float4(pp.x * kk, pp.y * kk, pp.z * kk, pp.w * kk);
                             px[ly * W + x] = blend(px[ly * W + x], fore, op, vis);
                         }
