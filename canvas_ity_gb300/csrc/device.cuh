@@ -254,16 +254,18 @@ __device__ __forceinline__ void dda_row(const dda_piece &p, int k, Emit &emit) {
 }
 
 // Clip one polyline segment to [0,width] x [0,height] the way the
-// reference's Sutherland-Hodgman pass and clamp do (hpp:2204-2239): the part
-// left of x = 0 (right of x = width) is replaced by its projection onto that
-// edge; parts above y = 0 or below y = height contribute nothing.  Returns
-// up to three pieces (main, left edge, right edge).
-__device__ __forceinline__ int clip_segment(float2 a, float2 b, float width, float height, float2 *pa,
-                                            float2 *pb) {
-    if (!(isfinite(a.x) && isfinite(a.y) && isfinite(b.x) && isfinite(b.y))) return 0;
-    float2 ma = a, mb = b;
-    bool has_main = true, has_left = false, has_right = false;
-    float2 la, lb, ra, rb;
+// reference's Sutherland-Hodgman pass and clamp do (hpp:2204-2239), summed
+// over a polygon: the part left of x = 0 is replaced by its projection onto
+// that edge; parts above y = 0 or below y = height contribute nothing, and
+// so does the part right of x = width, whose projection onto that edge adds
+// only to cells at x >= width, which no pixel reads.  Up to two pieces in
+// fixed slots (0 inside, 1 the left edge, each clamped); returns the mask of
+// the slots filled, none for a segment with a non-finite end.
+__device__ __forceinline__ unsigned clip_segment(float2 a, float2 b, float width, float height, float2 (&pa)[2],
+                                                 float2 (&pb)[2]) {
+    if (!(isfinite(a.x) && isfinite(a.y) && isfinite(b.x) && isfinite(b.y))) return 0u;
+    float2 ma = a, mb = b, la = a, lb = b;
+    bool has_main = true, has_left = false;
     // x >= 0
     {
         float fs = ma.x, ts = mb.x;
@@ -279,56 +281,35 @@ __device__ __forceinline__ int clip_segment(float2 a, float2 b, float width, flo
             else { la = f2(0.0f, I.y); lb = f2(0.0f, mb.y); mb = I; }
         }
     }
-    // y >= 0 (parts above project onto a horizontal edge: no coverage)
-    auto clip_y0 = [](bool &has, float2 &u, float2 &v) {
+    // keep where dir * (y - place) >= 0; the rest lies on a horizontal edge
+    auto keep_y = [](bool &has, float2 &u, float2 &v, float fs, float ts) {
         if (!has) return;
-        float fs = u.y, ts = v.y;
         if (fs < 0.0f && ts < 0.0f) { has = false; return; }
         if (fs * ts < 0.0f) {
             float2 I = mix2(u, v, fs / (fs - ts));
             if (fs < 0.0f) u = I; else v = I;
         }
     };
-    clip_y0(has_main, ma, mb);
-    clip_y0(has_left, la, lb);
-    // x <= width
+    keep_y(has_main, ma, mb, ma.y, mb.y);
+    keep_y(has_left, la, lb, la.y, lb.y);
+    // x <= width: the part beyond is dropped
     if (has_main) {
         float fs = width - ma.x, ts = width - mb.x;
         if (fs < 0.0f && ts < 0.0f) {
             has_main = false;
-            has_right = true;
-            ra = f2(width, ma.y);
-            rb = f2(width, mb.y);
         } else if (fs * ts < 0.0f) {
             float2 I = mix2(ma, mb, fs / (fs - ts));
-            has_right = true;
-            if (fs < 0.0f) { ra = f2(width, ma.y); rb = f2(width, I.y); ma = I; }
-            else { ra = f2(width, I.y); rb = f2(width, mb.y); mb = I; }
+            if (fs < 0.0f) ma = I; else mb = I;
         }
     }
-    // y <= height
-    auto clip_yh = [height](bool &has, float2 &u, float2 &v) {
-        if (!has) return;
-        float fs = height - u.y, ts = height - v.y;
-        if (fs < 0.0f && ts < 0.0f) { has = false; return; }
-        if (fs * ts < 0.0f) {
-            float2 I = mix2(u, v, fs / (fs - ts));
-            if (fs < 0.0f) u = I; else v = I;
-        }
-    };
-    clip_yh(has_main, ma, mb);
-    clip_yh(has_left, la, lb);
-    clip_yh(has_right, ra, rb);
-    int n = 0;
-    auto put = [&](float2 u, float2 v) {
-        pa[n] = f2(lo(hi(u.x, 0.0f), width), lo(hi(u.y, 0.0f), height));
-        pb[n] = f2(lo(hi(v.x, 0.0f), width), lo(hi(v.y, 0.0f), height));
-        ++n;
-    };
-    if (has_main) put(ma, mb);
-    if (has_left) put(la, lb);
-    if (has_right) put(ra, rb);
-    return n;
+    keep_y(has_main, ma, mb, height - ma.y, height - mb.y);
+    keep_y(has_left, la, lb, height - la.y, height - lb.y);
+    auto clamp2 = [&](float2 u) { return f2(lo(hi(u.x, 0.0f), width), lo(hi(u.y, 0.0f), height)); };
+    pa[0] = clamp2(ma);
+    pb[0] = clamp2(mb);
+    pa[1] = clamp2(la);
+    pb[1] = clamp2(lb);
+    return (has_main ? 1u : 0u) | (has_left ? 2u : 0u);
 }
 
 // Coverage of an accumulated signed area s under a fill rule: nonzero

@@ -376,10 +376,12 @@ struct frame {
     std::vector<clip_op> clips;
     int max_level = -1;
     int64_t total_rows = 0, total_segs = 0;
-    // Jobs scanned straight from their polylines (tab_nc) and jobs that go
-    // through the clip passes first (tab_cl): (first point, job index).
-    std::vector<int2> tab_nc, tab_cl;
-    int64_t nc_segs = 0, cl_points = 0;
+    // Run jobs scanned straight from their polylines (tab_nc), binned jobs
+    // (tab_bn, every segment clipped on its own) and run jobs that go through
+    // the clip passes first (tab_cl): (first point, job index).
+    std::vector<int2> tab_nc, tab_bn, tab_cl;
+    std::vector<int32_t> bn_idx;   // tab_bn's block index (job_entry)
+    int64_t nc_segs = 0, bn_segs = 0, cl_points = 0;
     int64_t pass_n[5] = {};    // clip pass sizes (input of pass 0 .. output of pass 3)
     int n_items = 0;
     int strip_pixels = 4096;
@@ -476,8 +478,9 @@ struct frame {
         max_level = -1;
         total_rows = total_segs = 0;
         tab_nc.clear();
+        tab_bn.clear();
         tab_cl.clear();
-        nc_segs = cl_points = 0;
+        nc_segs = bn_segs = cl_points = 0;
         for (int64_t &v : pass_n) v = 0;
         n_items = 0;
         binned = false;
@@ -572,7 +575,7 @@ int frame::clip_passes(job_tables &t) {
     clip_pass P;
     std::memset(&P, 0, sizeof(P));
     P.jobs = jobs_dev.as<scan_job>();
-    P.tab = tabs_dev.as<int2>() + tab_nc.size();
+    P.tab = tabs_dev.as<int2>() + tab_nc.size() + tab_bn.size();
     P.n_tab = static_cast<int>(tab_cl.size());
     P.src_pts[0] = t.pts[0];
     P.src_pts[1] = t.pts[1];
@@ -1015,7 +1018,9 @@ int frame::prepare() {
         j.geom = c.geom;
         j.line_first = c.line_first;
         j.seg_count = c.line_count;
-        j.clip = needs_clip(c, wd, ht, ox, oy) ? 1 : 0;
+        // binned coverage clips each segment on its own in k_bin: no
+        // polygon passes
+        j.clip = !to_bins && needs_clip(c, wd, ht, ox, oy) ? 1 : 0;
         j.rows = rows_n;
         j.cols = cols_n;
         j.width = wd;
@@ -1081,18 +1086,38 @@ int frame::prepare() {
         if (j.clip) {
             tab_cl.push_back(make_int2(static_cast<int>(cl_points), static_cast<int>(ji)));
             cl_points += j.seg_count;
+        } else if (j.binned) {
+            tab_bn.push_back(make_int2(static_cast<int>(bn_segs), static_cast<int>(ji)));
+            bn_segs += j.seg_count;
         } else {
             tab_nc.push_back(make_int2(static_cast<int>(nc_segs), static_cast<int>(ji)));
             nc_segs += j.seg_count;
         }
     }
     pass_n[0] = cl_points;
-    if (!tab_nc.empty() || !tab_cl.empty()) {
-        size_t nt = tab_nc.size() + tab_cl.size();
-        if (!tabs_dev.ensure(nt * sizeof(int2))) return fail(CY_ENOMEM, __LINE__);
-        std::vector<int2> both(tab_nc);
-        both.insert(both.end(), tab_cl.begin(), tab_cl.end());
-        if (!ok(cudaMemcpyAsync(tabs_dev.p, both.data(), nt * sizeof(int2), cudaMemcpyHostToDevice, stream)) ||
+    // Block index of the binned table: entry holding segment b << kTabShift
+    // for every block b, and one more.
+    bn_idx.clear();
+    if (!tab_bn.empty()) {
+        const int64_t nblk = (bn_segs >> cyg::kTabShift) + 2;
+        bn_idx.resize(static_cast<size_t>(nblk));
+        size_t e = 0;
+        for (int64_t b = 0; b < nblk; ++b) {
+            const int64_t target = std::min<int64_t>(b << cyg::kTabShift, bn_segs - 1);
+            while (e + 1 < tab_bn.size() && tab_bn[e + 1].x <= target) ++e;
+            bn_idx[static_cast<size_t>(b)] = static_cast<int32_t>(e);
+        }
+    }
+    if (!tab_nc.empty() || !tab_bn.empty() || !tab_cl.empty()) {
+        size_t nt = tab_nc.size() + tab_bn.size() + tab_cl.size();
+        if (!tabs_dev.ensure(nt * sizeof(int2) + bn_idx.size() * sizeof(int32_t))) return fail(CY_ENOMEM, __LINE__);
+        std::vector<int2> all_tabs(tab_nc);
+        all_tabs.insert(all_tabs.end(), tab_bn.begin(), tab_bn.end());
+        all_tabs.insert(all_tabs.end(), tab_cl.begin(), tab_cl.end());
+        if (!ok(cudaMemcpyAsync(tabs_dev.p, all_tabs.data(), nt * sizeof(int2), cudaMemcpyHostToDevice, stream)) ||
+            (!bn_idx.empty() && !ok(cudaMemcpyAsync(tabs_dev.as<int2>() + nt, bn_idx.data(),
+                                                     bn_idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                                     stream))) ||
             !ok(cudaStreamSynchronize(stream)))
             return status;
     }
@@ -1205,7 +1230,15 @@ int frame::run() {
         t.row_cur = row_cur.as<int32_t>();
         int rc = clip_passes(t);
         if (rc) return rc;
-        int segs_nc = static_cast<int>(nc_segs), segs_cl = static_cast<int>(pass_n[4]);
+        int segs_nc = static_cast<int>(nc_segs), segs_bn = static_cast<int>(bn_segs),
+            segs_cl = static_cast<int>(pass_n[4]);
+        // the binned jobs' own table
+        job_tables tb = t;
+        tb.tab = tabs_dev.as<int2>() + tab_nc.size();
+        tb.n_tab = static_cast<int>(tab_bn.size());
+        tb.tab_idx = bn_idx.empty() ? nullptr
+                                    : reinterpret_cast<const int32_t *>(tabs_dev.as<int2>() + tab_nc.size() +
+                                                                         tab_bn.size() + tab_cl.size());
         // Segments per warp round: halved while that leaves fewer than 48
         // warps per SM of work.
         auto per_warp = [](int segs) {
@@ -1227,7 +1260,7 @@ int frame::run() {
         bin_tables bt;
         std::memset(&bt, 0, sizeof(bt));
         const size_t nb = static_cast<size_t>(n_bins);
-        auto bin_grid = [](int segs) { return std::max(1, std::min((segs + 255) / 256, 152 * 8)); };
+        const int bin_blocks = std::max(1, std::min((segs_bn + 255) / 256, 152 * 8));
         if (nb > 0) {
             bt.cnt = bin_cnt.as<int32_t>();
             bt.cur = bin_cur.as<int32_t>();
@@ -1235,11 +1268,10 @@ int frame::run() {
             if (!ok(cudaMemsetAsync(bin_cnt.p, 0, (nb + 1) * 4, stream)) ||
                 !ok(cudaMemsetAsync(bin_cur.p, 0, (nb + 1) * 4, stream)))
                 return status;
-            if (segs_nc > 0) k_bin<false, false><<<bin_grid(segs_nc), 256, 0, stream>>>(t, bt, segs_nc);
-            if (segs_cl > 0) k_bin<false, true><<<bin_grid(segs_cl), 256, 0, stream>>>(t, bt, segs_cl);
+            if (segs_bn > 0) k_bin<false><<<bin_blocks, 256, 0, stream>>>(tb, bt, segs_bn);
             rc = scan64(bin_cnt.as<int32_t>(), bin_off.as<int64_t>(), static_cast<int>(nb) + 1);
             if (rc) return rc;
-            launches += 2 + (segs_nc > 0 ? 2 : 0) + (segs_cl > 0 ? 2 : 0) + scan_launch_count(static_cast<int64_t>(nb) + 1);
+            launches += 2 + (segs_bn > 0 ? 2 : 0) + scan_launch_count(static_cast<int64_t>(nb) + 1);
         }
         if (!sized) {
             sized = true;
@@ -1289,8 +1321,7 @@ int frame::run() {
         if (segs_cl > 0) k_runs<true, true><<<grid_cl, kRunsWarps * 32, 0, stream>>>(t, segs_cl, spw_cl);
         if (nb > 0) {
             bt.seg = bin_seg.as<float4>();
-            if (segs_nc > 0) k_bin<true, false><<<bin_grid(segs_nc), 256, 0, stream>>>(t, bt, segs_nc);
-            if (segs_cl > 0) k_bin<true, true><<<bin_grid(segs_cl), 256, 0, stream>>>(t, bt, segs_cl);
+            if (segs_bn > 0) k_bin<true><<<bin_blocks, 256, 0, stream>>>(tb, bt, segs_bn);
         }
         int rgrid = static_cast<int>(std::min<size_t>((nr + kRowsWarps - 1) / kRowsWarps, 152 * 32));
         if (!ok(cudaMemsetAsync(n_long.p, 0, 4, stream))) return status;
@@ -1889,10 +1920,15 @@ bool valid_counts(const int *counts, int n, size_t &total) {
 
 // The rectangles a command's geometry is scanned against: the canvas, and
 // for a shadow the padded canvas with the points moved by the shadow offset.
+// keep_left: a polygon wholly left of the canvas is kept, for a draw whose
+// coverage may be binned -- clipped segment by segment, its projection onto
+// x = 0 adds pieces whose rounded sums need not cancel to zero as the
+// polygon clip's empty result does.
 struct cull_rects {
     float w, h;
     bool shadow;
     float sw, sh, sx, sy;
+    bool keep_left;
 };
 
 // Whether the Sutherland-Hodgman clip (hpp:2204-2235) leaves nothing of a
@@ -1913,7 +1949,7 @@ bool culled(const float2 *p, int n, const cull_rects &r, float margin) {
                 out = out && d < -margin;
                 in = in && d >= margin;
             }
-            if (out) return true;
+            if (out) return !(e == 0 && r.keep_left);
             if (!in) return false;
         }
         return false;
@@ -2022,7 +2058,7 @@ int queue_draw(cy_ctx *c, const float *points, const int *counts, int n_sub, boo
     fill_state(state, cmd);
     cull_rects rects = {static_cast<float>(c->W), static_cast<float>(c->H), cmd.shadow != 0,
                         static_cast<float>(c->W + 2 * cmd.sh_border), static_cast<float>(c->H + 2 * cmd.sh_border),
-                        cmd.sh_offx, cmd.sh_offy};
+                        cmd.sh_offx, cmd.sh_offy, true};
     int rc = fill_paint(q, paint, cmd, c->device);
     if (rc == CY_OK) rc = queue_geometry(q, points, counts, n_sub, bezier, cmd, rects);
     if (rc != CY_OK) {
@@ -2432,7 +2468,7 @@ int cy_clip_path(cy_ctx *c, const float *points, const int *counts, int n_sub, i
     std::memset(&cmd, 0, sizeof(cmd));
     cmd.kind = CMD_CLIP;
     cmd.fill_rule = fill_rule == 1 ? 1 : 0;
-    cull_rects rects = {static_cast<float>(c->W), static_cast<float>(c->H), false, 0.0f, 0.0f, 0.0f, 0.0f};
+    cull_rects rects = {static_cast<float>(c->W), static_cast<float>(c->H), false, 0.0f, 0.0f, 0.0f, 0.0f, false};
     int rc = queue_geometry(q, points, counts, n_sub, true, cmd, rects);
     if (rc != CY_OK) return rc;
     int id = 0;
@@ -2899,7 +2935,7 @@ int cy_frame_stats(cy_frame *fr, long long *stats, int n) {
     frame &f = *fr->f;
     long long pixels = 0;
     for (cy_ctx *c : f.cvs) pixels += static_cast<long long>(c->W) * c->H;
-    long long v[] = {pixels, static_cast<long long>(f.all.cmds.size()), f.nc_segs + f.pass_n[4], f.n_runs, f.total_rows,
+    long long v[] = {pixels, static_cast<long long>(f.all.cmds.size()), f.nc_segs + f.bn_segs + f.pass_n[4], f.n_runs, f.total_rows,
                      f.main_runs, f.main_rows, f.shadow_floats, f.get_total, f.h2d_bytes, f.launches,
                      static_cast<long long>(f.sjobs.size()), static_cast<long long>(f.clips.size()),
                      f.n_bin_entries, f.binned ? 1LL : 0LL};

@@ -156,7 +156,7 @@ struct scan_job {
     int32_t geom;          // 0: host polylines, 1: GPU-flattened polylines
     int32_t line_first;    // first polyline point
     int32_t seg_count;     // polyline points (= segments, each closing on its predecessor)
-    int32_t clip;          // 1: points may leave [0,width] x [0,height]
+    int32_t clip;          // 1: points may leave [0,width] x [0,height] (runs jobs only)
     int32_t row_base;      // first row of this job in the shared row arrays
     int32_t rows, cols;    // rows and cells per row of the (padded) canvas
     float width, height;   // clip rectangle [0,width] x [0,height]
@@ -211,10 +211,13 @@ __device__ __forceinline__ poly_point clip_point(const clip_pass &P, int k) {
     if (FIRST) {
         int c = table_find(P.tab, P.n_tab, k);
         const scan_job &j = P.jobs[P.tab[c].y];
-        int g = j.geom ? 1 : 0;
+        // a select, not an index into the parameter arrays: an index would
+        // copy them to local memory
+        const float2 *pts = j.geom ? P.src_pts[1] : P.src_pts[0];
+        const int32_t *prev = j.geom ? P.src_prev[1] : P.src_prev[0];
         int i = j.line_first + (k - P.tab[c].x);
-        int pi = P.src_prev[g][i];
-        float2 a = P.src_pts[g][pi], b = P.src_pts[g][i];
+        int pi = prev[i];
+        float2 a = pts[pi], b = pts[i];
         q.from = f2(j.offx + a.x, j.offy + a.y);   // scan's add(offset, point) (hpp:2205)
         q.to = f2(j.offx + b.x, j.offy + b.y);
         q.job = P.tab[c].y;
@@ -290,9 +293,8 @@ __global__ void k_clip_link(clip_pass P) {
         if (FIRST) {
             int c = table_find(P.tab, P.n_tab, k);
             const scan_job &j = P.jobs[P.tab[c].y];
-            int g = j.geom ? 1 : 0;
             int i = j.line_first + (k - P.tab[c].x);
-            int pi = P.src_prev[g][i];
+            int pi = (j.geom ? P.src_prev[1] : P.src_prev[0])[i];
             start = pi >= i;
             last = k + (pi - i);
         } else {
@@ -312,6 +314,7 @@ struct job_tables {
     // unclipped jobs: segments straight from the polylines
     const int2 *tab;          // (first segment, job)
     int n_tab;
+    const int32_t *tab_idx;   // or null: entry holding segment b << kTabShift, b = 0 .. last + 1
     const float2 *pts[2];
     const int32_t *prev[2];
     // clipped jobs: the last clip pass's polygons (offset already applied)
@@ -324,27 +327,54 @@ struct job_tables {
     run *runs;
 };
 
-// Segment s of the scan (its end points moved by the job's offset, as scan
-// does with add(offset, point), hpp:2205) clamped to the job's rectangle as
-// scan does before add_runs (hpp:2236-2238).  Returns the job index.
+constexpr int kTabShift = 10;
+
+// The table entry holding segment s: a search between the entries of its
+// block of 2^kTabShift segments when the table has a block index.
+__device__ __forceinline__ int job_entry(const job_tables &t, int s) {
+    if (!t.tab_idx) return table_find(t.tab, t.n_tab, s);
+    const int b = s >> kTabShift;
+    int lo_i = t.tab_idx[b], hi_i = t.tab_idx[b + 1] + 1;   // tab[lo_i].x <= s < tab[hi_i].x
+    while (hi_i - lo_i > 1) {
+        int mid = (lo_i + hi_i) >> 1;
+        if (t.tab[mid].x <= s) lo_i = mid; else hi_i = mid;
+    }
+    return lo_i;
+}
+
+// Segment s of table entry c, its end points moved by the job's offset as
+// scan does with add(offset, point) (hpp:2205).  Returns the job index.
+__device__ __forceinline__ int segment_at(const job_tables &t, int c, int s, float2 &a, float2 &b) {
+    const int ji = t.tab[c].y;
+    const scan_job &jj = t.jobs[ji];
+    int k = jj.line_first + (s - t.tab[c].x);
+    // a select, not an index into the parameter arrays: an index would copy
+    // them to local memory
+    const float2 *pts = jj.geom ? t.pts[1] : t.pts[0];
+    const int32_t *prev = jj.geom ? t.prev[1] : t.prev[0];
+    float2 pb = pts[k];
+    float2 pa = pts[prev[k]];
+    a = f2(jj.offx + pa.x, jj.offy + pa.y);
+    b = f2(jj.offx + pb.x, jj.offy + pb.y);
+    return ji;
+}
+
+// Segment s of the scan (the table's, or the last clip pass's polygons).
 template <bool CLIPPED>
-__device__ __forceinline__ int segment_of(const job_tables &t, int s, float2 &a, float2 &b) {
-    int ji;
+__device__ __forceinline__ int segment_raw(const job_tables &t, int s, float2 &a, float2 &b) {
     if (CLIPPED) {
-        ji = t.cl_job[s];
         a = t.cl_pts[t.cl_prev[s]];
         b = t.cl_pts[s];
-    } else {
-        int c = table_find(t.tab, t.n_tab, s);
-        ji = t.tab[c].y;
-        const scan_job &jj = t.jobs[ji];
-        int k = jj.line_first + (s - t.tab[c].x);
-        int g = jj.geom ? 1 : 0;
-        float2 pb = t.pts[g][k];
-        float2 pa = t.pts[g][t.prev[g][k]];
-        a = f2(jj.offx + pa.x, jj.offy + pa.y);
-        b = f2(jj.offx + pb.x, jj.offy + pb.y);
+        return t.cl_job[s];
     }
+    return segment_at(t, job_entry(t, s), s, a, b);
+}
+
+// The same segment clamped to the job's rectangle as scan does before
+// add_runs (hpp:2236-2238).
+template <bool CLIPPED>
+__device__ __forceinline__ int segment_of(const job_tables &t, int s, float2 &a, float2 &b) {
+    int ji = segment_raw<CLIPPED>(t, s, a, b);
     const scan_job &j = t.jobs[ji];
     a = f2(lo(hi(a.x, 0.0f), j.width), lo(hi(a.y, 0.0f), j.height));
     b = f2(lo(hi(b.x, 0.0f), j.width), lo(hi(b.y, 0.0f), j.height));
@@ -374,45 +404,55 @@ struct bin_tables {
     float4 *seg;           // entries: (a.x, a.y, b.x, b.y)
 };
 
-template <bool EMIT, bool CLIPPED>
+template <bool EMIT>
 __global__ void k_bin(job_tables t, bin_tables bt, int total_segments) {
-    // A warp's 32 consecutive segments mostly share their job and bands:
-    // lanes adding to the same bin are grouped, so each bin takes one
-    // atomic per warp, and each lane writes at the group's base plus its rank.
+    // Segment s of the binned jobs' table, clipped on its own (clip_segment:
+    // the part left of the rectangle becomes its projection on x = 0, as the
+    // reference's polygon clip and clamp make it in sum, hpp:2204-2239;
+    // segments with a non-finite end are dropped).  Up to two pieces per
+    // segment in fixed slots, each listed in every band it crosses.  A warp's
+    // 32 consecutive segments mostly share their job and bands: per slot,
+    // lanes adding to the same bin are grouped, so each bin takes one atomic
+    // per warp, and each lane writes at the group's base plus its rank.
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total_segments; base += stride) {
         const int s = base + lane;
-        int bin0 = 0, nb = 0;
-        float2 a = f2(0.0f, 0.0f), b = a;
+        float2 pa[2], pb[2];
+        int pbin[2] = {0, 0}, pnb[2] = {0, 0};
         if (s < total_segments) {
-            int ji = segment_of<CLIPPED>(t, s, a, b);
-            const scan_job &j = t.jobs[ji];
-            dda_piece p;
-            if (j.binned && dda_setup(a, b, p)) {
+            float2 a, b;
+            const scan_job &j = t.jobs[segment_raw<false>(t, s, a, b)];
+            const unsigned has = clip_segment(a, b, j.width, j.height, pa, pb);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                dda_piece p;
+                if (!(has >> i & 1u) || !dda_setup(pa[i], pb[i], p)) continue;
                 int r0, r1;
                 dda_rows(p, j.rows, r0, r1);
-                if (r0 <= r1) {
-                    bin0 = j.bin_base + r0 / j.band_h;
-                    nb = r1 / j.band_h - r0 / j.band_h + 1;
-                }
+                if (r0 > r1) continue;
+                pbin[i] = j.bin_base + r0 / j.band_h;
+                pnb[i] = r1 / j.band_h - r0 / j.band_h + 1;
             }
         }
-        const int rounds = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(nb)));
-        for (int k = 0; k < rounds; ++k) {
-            const int bin = k < nb ? bin0 + k : -1;
-            const unsigned peers = __match_any_sync(0xffffffffu, bin);
-            if (bin < 0) continue;
-            const int leader = __ffs(peers) - 1;
-            const int rank = __popc(peers & ((1u << lane) - 1u));
-            if (!EMIT) {
-                if (lane == leader) atomicAdd(bt.cnt + bin, __popc(peers));
-            } else {
-                int first = 0;
-                if (lane == leader) first = atomicAdd(bt.cur + bin, __popc(peers));
-                first = __shfl_sync(peers, first, leader);
-                int64_t at = bt.off[bin] + first + rank;
-                if (at < bt.off[bin + 1]) bt.seg[at] = make_float4(a.x, a.y, b.x, b.y);
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int rounds = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(pnb[i])));
+            for (int k = 0; k < rounds; ++k) {
+                const int bin = k < pnb[i] ? pbin[i] + k : -1;
+                const unsigned peers = __match_any_sync(0xffffffffu, bin);
+                if (bin < 0) continue;
+                const int leader = __ffs(peers) - 1;
+                const int rank = __popc(peers & ((1u << lane) - 1u));
+                if (!EMIT) {
+                    if (lane == leader) atomicAdd(bt.cnt + bin, __popc(peers));
+                } else {
+                    int first = 0;
+                    if (lane == leader) first = atomicAdd(bt.cur + bin, __popc(peers));
+                    first = __shfl_sync(peers, first, leader);
+                    int64_t at = bt.off[bin] + first + rank;
+                    if (at < bt.off[bin + 1]) bt.seg[at] = make_float4(pa[i].x, pa[i].y, pb[i].x, pb[i].y);
+                }
             }
         }
     }

@@ -683,33 +683,34 @@ __device__ void blur_line_fused(float *line, size_t stride, int n, int r, float 
 
 // Radius known at compile time: the three rings live in registers (every
 // ring index is a constant once a block of RING steps is unrolled).  RING is
-// the smallest power of two holding a pass's window [x - R - 2, x + R + 1].
+// exactly the size of a pass's window [x - R - 2, x + R + 1]: 2R + 4.
+template <int RING>
+__device__ __forceinline__ constexpr int ring_at(int v) { return ((v % RING) + RING) % RING; }
+
 template <int R, int RING>
 __device__ __forceinline__ float blur_step_reg(const float (&ring)[RING], float &acc, int x, int n, float w1,
                                                float w2, int k) {
     // k is the step's position in the unrolled block; x % RING == k % RING.
-    constexpr int M = RING - 1;
     if (x == 0) {
-        float a = R + 1 < n ? w1 * ring[(k + R + 1) & M] : 0.0f;
+        float a = R + 1 < n ? w1 * ring[ring_at<RING>(k + R + 1)] : 0.0f;
 #pragma unroll
         for (int i = 0; i <= R; ++i)
-            if (i < n) a += (w1 + w2) * ring[(k + i) & M];
+            if (i < n) a += (w1 + w2) * ring[ring_at<RING>(k + i)];
         acc = a;
         return a;
     }
     float a = acc;
-    if (x >= R + 1) a -= w2 * ring[(k - R - 1) & M];
-    if (x >= R + 2) a -= w1 * ring[(k - R - 2) & M];
-    if (x + R < n) a += w2 * ring[(k + R) & M];
-    if (x + R + 1 < n) a += w1 * ring[(k + R + 1) & M];
+    if (x >= R + 1) a -= w2 * ring[ring_at<RING>(k - R - 1)];
+    if (x >= R + 2) a -= w1 * ring[ring_at<RING>(k - R - 2)];
+    if (x + R < n) a += w2 * ring[ring_at<RING>(k + R)];
+    if (x + R + 1 < n) a += w1 * ring[ring_at<RING>(k + R + 1)];
     acc = a;
     return a;
 }
 
 template <int R>
 __device__ void blur_line_reg(float *line, size_t stride, int n, float w1, float w2) {
-    constexpr int RING = 2 * R + 4 <= 16 ? 16 : 32;
-    constexpr int M = RING - 1;
+    constexpr int RING = 2 * R + 4;
     constexpr int L = R + 1;
     float r0[RING], r1[RING], r2[RING];
     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
@@ -726,8 +727,9 @@ __device__ void blur_line_reg(float *line, size_t stride, int n, float w1, float
             int t = t0 + k;
             if (t < n) r0[k] = in[k];
             int x1 = t - L, x2 = t - 2 * L, x3 = t - 3 * L;
-            if (x1 >= 0 && x1 < n) r1[(k - L) & M] = blur_step_reg<R, RING>(r0, a0, x1, n, w1, w2, k - L);
-            if (x2 >= 0 && x2 < n) r2[(k - 2 * L) & M] = blur_step_reg<R, RING>(r1, a1, x2, n, w1, w2, k - 2 * L);
+            if (x1 >= 0 && x1 < n) r1[ring_at<RING>(k - L)] = blur_step_reg<R, RING>(r0, a0, x1, n, w1, w2, k - L);
+            if (x2 >= 0 && x2 < n)
+                r2[ring_at<RING>(k - 2 * L)] = blur_step_reg<R, RING>(r1, a1, x2, n, w1, w2, k - 2 * L);
             if (x3 >= 0 && x3 < n)
                 line[static_cast<size_t>(x3) * stride] = blur_step_reg<R, RING>(r2, a2, x3, n, w1, w2, k - 3 * L);
         }

@@ -33,11 +33,12 @@ void cy_set_deferred(int deferred);
 void cy_set_strip_config(int strip_pixels, int threads);
 
 /* Coverage of the tile engine's draws, for frames prepared afterwards in
- * any thread.  0 (default), binned: each draw's segments are listed per band
- * of rows and accumulated per strip in shared memory as fixed-point signed
- * areas (add_runs' cell areas, hpp:2109-2170, with no sorted runs in
- * memory); coverage is within 1e-5 of the reference's and RGBA8 within
- * +-1 LSB.  1, exact: row-sorted runs summed in the reference's order
+ * any thread.  0 (default), binned: each draw's segments are clipped to the
+ * canvas one by one (the polygon clip's result, hpp:2204-2239, in sum),
+ * listed per band of rows and accumulated per strip in shared memory as
+ * fixed-point signed areas (add_runs' cell areas, hpp:2109-2170, with no
+ * sorted runs in memory); coverage is within 1e-5 of the reference's and
+ * RGBA8 within +-1 LSB.  1, exact: row-sorted runs summed in the reference's order
  * (lines_to_runs and render_main, hpp:2193-2253, 2551-2605), so the float
  * canvas is the reference's bit for bit.  The plain engine is always exact. */
 void cy_set_coverage(int exact);
@@ -102,7 +103,8 @@ void cy_frame_workspace_release(void);
 int cy_frame_set_profiling(cy_frame *frame, int on);
 int cy_frame_profile(cy_frame *frame, float *phase_ms, int n);
 
-/* Frame statistics (first n of): pixels, commands, segments, runs, rows,
+/* Frame statistics (first n of): pixels, commands, segments (scanned: run
+ * jobs' after the polygon clip, binned draws' as given), runs, rows,
  * runs of draws, rows of draws, shadow image floats, read-back bytes,
  * uploaded bytes, kernel launches per run, shadows, clips, binned segment
  * entries, binned (1) or exact (0) coverage. */

@@ -1137,8 +1137,82 @@ void canvas::scan_segment_binned(vec2 from, vec2 to) {
     } while (now.y != to.y);
 }
 
-// scan() of the draw itself (no offset, no padding) into `acc`: the same
-// Sutherland-Hodgman clip and clamp, then the binned cell walk.
+// One polyline segment clipped to [0,width] x [0,height] on its own, as the
+// binned coverage does it: the polygon clip of scan (hpp:2204-2239) followed
+// by the clamp replaces the part of an edge left of x = 0 by its projection
+// onto that side, and parts above y = 0 or below y = height become
+// horizontal and add nothing; per segment the same pieces come out (inside,
+// left side), each clamped.  The part right of x = width is dropped: its
+// projection onto that side adds only to cells at x >= width, which no pixel
+// reads.  A segment with a non-finite end gives none.  In exact arithmetic
+// the pieces of all segments add up to the clipped polygon's coverage; in
+// float they differ from it by rounding only.
+static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec2 *pb) {
+    if (!(std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(b.x) && std::isfinite(b.y))) return 0;
+    vec2 ma = a, mb = b, la{}, lb{};
+    bool has_main = true, has_left = false;
+    {
+        float fs = ma.x, ts = mb.x;
+        if (fs < 0.0f && ts < 0.0f) {
+            has_main = false;
+            has_left = true;
+            la = mk(0.0f, ma.y);
+            lb = mk(0.0f, mb.y);
+        } else if (fs * ts < 0.0f) {
+            vec2 cut = mix(ma, mb, fs / (fs - ts));
+            has_left = true;
+            if (fs < 0.0f) {
+                la = mk(0.0f, ma.y);
+                lb = mk(0.0f, cut.y);
+                ma = cut;
+            } else {
+                la = mk(0.0f, cut.y);
+                lb = mk(0.0f, mb.y);
+                mb = cut;
+            }
+        }
+    }
+    auto keep_below = [](bool &has, vec2 &u, vec2 &v, float place, float dir) {
+        // keep the part where dir * (y - place) >= 0
+        if (!has) return;
+        float fs = (u.y - place) * dir, ts = (v.y - place) * dir;
+        if (fs < 0.0f && ts < 0.0f) {
+            has = false;
+            return;
+        }
+        if (fs * ts < 0.0f) {
+            vec2 cut = mix(u, v, fs / (fs - ts));
+            if (fs < 0.0f) u = cut;
+            else v = cut;
+        }
+    };
+    keep_below(has_main, ma, mb, 0.0f, 1.0f);
+    keep_below(has_left, la, lb, 0.0f, 1.0f);
+    if (has_main) {
+        float fs = width - ma.x, ts = width - mb.x;
+        if (fs < 0.0f && ts < 0.0f) {
+            has_main = false;
+        } else if (fs * ts < 0.0f) {
+            vec2 cut = mix(ma, mb, fs / (fs - ts));
+            if (fs < 0.0f) ma = cut;
+            else mb = cut;
+        }
+    }
+    keep_below(has_main, ma, mb, height, -1.0f);
+    keep_below(has_left, la, lb, height, -1.0f);
+    int n = 0;
+    auto put = [&](vec2 u, vec2 v) {
+        pa[n] = mk(lo(hi(u.x, 0.0f), width), lo(hi(u.y, 0.0f), height));
+        pb[n] = mk(lo(hi(v.x, 0.0f), width), lo(hi(v.y, 0.0f), height));
+        ++n;
+    };
+    if (has_main) put(ma, mb);
+    if (has_left) put(la, lb);
+    return n;
+}
+
+// scan() of the draw itself (no offset, no padding) into `acc`: each
+// segment clipped on its own, then the binned cell walk of every piece.
 void canvas::scan_binned() {
     acc.assign(static_cast<size_t>(W) * static_cast<size_t>(H), 0);
     float width = static_cast<float>(W), height = static_cast<float>(H);
@@ -1146,29 +1220,13 @@ void canvas::scan_binned() {
     for (size_t s = 0; s < lines.subs.size(); ++s) {
         size_t begin = end;
         end += lines.subs[s].count;
-        scratch.pts.clear();
-        for (size_t i = begin; i < end; ++i) scratch.pts.push_back(add(mk(0.0f, 0.0f), lines.pts[i]));
-        for (int edge = 0; edge < 4; ++edge) {
-            vec2 normal = mk(edge == 0 ? 1.0f : edge == 2 ? -1.0f : 0.0f,
-                             edge == 1 ? 1.0f : edge == 3 ? -1.0f : 0.0f);
-            float place = edge == 2 ? width : edge == 3 ? height : 0.0f;
-            size_t first = scratch.pts.size();
-            for (size_t i = 0; i < first; ++i) {
-                vec2 from = scratch.pts[(i ? i : first) - 1];
-                vec2 to = scratch.pts[i];
-                float fs = dot(from, normal) + place;
-                float ts = dot(to, normal) + place;
-                if (fs * ts < 0.0f) scratch.pts.push_back(mix(from, to, fs / (fs - ts)));
-                if (ts >= 0.0f) scratch.pts.push_back(to);
-            }
-            scratch.pts.erase(scratch.pts.begin(), scratch.pts.begin() + static_cast<ptrdiff_t>(first));
-        }
-        size_t last = scratch.pts.size();
-        for (size_t i = 0; i < last; ++i) {
-            vec2 from = scratch.pts[(i ? i : last) - 1];
-            vec2 to = scratch.pts[i];
-            scan_segment_binned(mk(lo(hi(from.x, 0.0f), width), lo(hi(from.y, 0.0f), height)),
-                                mk(lo(hi(to.x, 0.0f), width), lo(hi(to.y, 0.0f), height)));
+        size_t n = end - begin;
+        for (size_t i = 0; i < n; ++i) {
+            vec2 from = add(mk(0.0f, 0.0f), lines.pts[begin + (i ? i : n) - 1]);
+            vec2 to = add(mk(0.0f, 0.0f), lines.pts[begin + i]);
+            vec2 pa[2], pb[2];
+            int pieces = clip_segment(from, to, width, height, pa, pb);
+            for (int k = 0; k < pieces; ++k) scan_segment_binned(pa[k], pb[k]);
         }
     }
 }
