@@ -356,7 +356,7 @@ struct frame {
     int64_t n_groups = 0, n_styles = 0, n_dash = 0;
     // Device stroke expansion: flattened centre lines occupy flat_pts[0,
     // nflat), the outlines follow at nflat; dashed centre lines are apart.
-    int64_t nflat = 0, n_outline = 0, n_dashed = 0, n_pieces = 0, n_chunks = 0;
+    int64_t nflat = 0, n_outline = 0, n_dashed = 0, n_pieces = 0, n_chunks = 0, n_jpos = 0;
     bool any_dash = false;
     // The sizing in prepare() flattened the centre lines and ran every stroke
     // pass up to the outline counts; the first run then only writes the
@@ -395,7 +395,7 @@ struct frame {
     dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
     dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, st_err, pc_cnt, pc_base, pc_list, wk_cnt, wk_base,
-        wk_chunks, jn_cnt, jn_alpha, jn_sum, jn_off, st_goff;
+        wk_chunks, jn_cnt, jn_alpha, jn_sum, jn_off, jn_pbase, jn_pchunk, st_goff;
     hbuf staging, offs_host, rowoff_host, get_host, stoff_host, binoff_host;
     char *d = nullptr;
     size_t o_cmd = 0, o_hpts = 0, o_hprev = 0, o_bez = 0, o_items = 0, o_soff = 0, o_scol = 0, o_tex = 0, o_put = 0;
@@ -461,7 +461,7 @@ struct frame {
         keep_reads = false;
         n_hpts = n_bez = n_items_all = n_stop = n_tex = n_put = 0;
         n_groups = n_styles = n_dash = 0;
-        nflat = n_outline = n_dashed = n_pieces = n_chunks = 0;
+        nflat = n_outline = n_dashed = n_pieces = n_chunks = n_jpos = 0;
         any_dash = false;
         geometry_ready = false;
         cmd_cv.clear();
@@ -497,7 +497,7 @@ struct frame {
                      &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev, &dash_cnt, &dash_off, &dash_pts,
                      &dash_subs, &dash_nsub, &st_err, &pc_cnt, &pc_base, &pc_list, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt,
-                     &jn_alpha, &jn_sum, &jn_off, &st_goff, &bin_cnt, &bin_cur, &bin_off, &bin_seg, &clip_dev};
+                     &jn_alpha, &jn_sum, &jn_off, &jn_pbase, &jn_pchunk, &st_goff, &bin_cnt, &bin_cur, &bin_off, &bin_seg, &clip_dev};
         for (dbuf *x : b) x->release();
         staging.release();
         stoff_host.release();
@@ -851,26 +851,44 @@ int frame::stroke_passes(bool sizing) {
     if (sizing) {
         if (!read_back(hb, wk_base.as<int32_t>() + npc, 4)) return status;
         n_chunks = hb[0];
-        if (n_chunks < 0 || n_chunks > (static_cast<int64_t>(1) << 26)) return fail(CY_ENOMEM, __LINE__);
+        // below 2^26 chunks, their packed walk positions (at most 32 each) fit an int32
+        if (n_chunks < 0 || n_chunks >= (static_cast<int64_t>(1) << 26)) return fail(CY_ENOMEM, __LINE__);
         size_t nc = static_cast<size_t>(n_chunks) + 1;
-        if (!wk_chunks.ensure(nc * sizeof(walk_chunk)) || !jn_cnt.ensure(nc * 32 * 4) ||
-            !jn_alpha.ensure(nc * 32 * 4) || !jn_sum.ensure(nc * 4) ||
-            !jn_off.ensure(nc * 8))
+        if (!wk_chunks.ensure(nc * sizeof(walk_chunk)) || !jn_sum.ensure(nc * 4) || !jn_pbase.ensure(nc * 4))
             return fail(CY_ENOMEM, __LINE__);
     }
     k_walk<<<std::max(1, (npc + kStrokeWarps - 1) / kStrokeWarps), kStrokeWarps * 32, 0, stream>>>(
         stroke_args(), pc_list.as<stroke_piece>(), npc, wk_base.as<int32_t>(), wk_chunks.as<walk_chunk>());
     const int nch = static_cast<int>(n_chunks);
-    const int jgrid = std::max(1, (nch + kStrokeWarps - 1) / kStrokeWarps);
-    k_join<false><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(), nch,
-                                                           jn_cnt.as<int32_t>(), jn_alpha.as<float>(),
-                                                           jn_sum.as<int32_t>(), nullptr,
-                                                           nullptr, nullptr, 0, 0);
+    // the chunks' walk positions, packed (k_chunk_positions)
+    k_chunk_lanes<<<std::max(1, (nch + 255) / 256), 256, 0, stream>>>(wk_chunks.as<walk_chunk>(), nch,
+                                                                     jn_sum.as<int32_t>());
     if (!ok(cudaMemsetAsync(jn_sum.as<int32_t>() + nch, 0, 4, stream))) return status;
-    if (int rc = scan64(jn_sum.as<int32_t>(), jn_off.as<int64_t>(), nch + 1)) return rc;
+    if (int rc = scan(jn_sum.as<int32_t>(), jn_pbase.as<int32_t>(), nch + 1)) return rc;
+    if (sizing) {
+        if (!read_back(hb, jn_pbase.as<int32_t>() + nch, 4)) return status;
+        n_jpos = hb[0];
+        if (n_jpos < 0 || n_jpos > static_cast<int64_t>(n_chunks) * 32) return fail(CY_ENOMEM, __LINE__);
+        size_t np1 = static_cast<size_t>(n_jpos) + 1;
+        if (!jn_pchunk.ensure(np1 * 4) || !jn_cnt.ensure(np1 * 4) || !jn_alpha.ensure(np1 * 4) ||
+            !jn_off.ensure(np1 * 8))
+            return fail(CY_ENOMEM, __LINE__);
+    }
+    const int njp = static_cast<int>(n_jpos);
+    k_chunk_positions<<<std::max(1, (nch + 7) / 8), 256, 0, stream>>>(wk_chunks.as<walk_chunk>(), nch,
+                                                                    jn_pbase.as<int32_t>(), jn_pchunk.as<int32_t>());
+    const int jgrid = std::max(1, (njp + kStrokeWarps * 32 - 1) / (kStrokeWarps * 32));
+    k_join<false><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(),
+                                                           jn_pbase.as<int32_t>(), jn_pchunk.as<int32_t>(), njp,
+                                                           jn_cnt.as<int32_t>(), jn_alpha.as<float>(), nullptr,
+                                                           nullptr, nullptr, 0, 0);
+    if (!ok(cudaMemsetAsync(jn_cnt.as<int32_t>() + njp, 0, 4, stream))) return status;
+    if (int rc = scan64(jn_cnt.as<int32_t>(), jn_off.as<int64_t>(), njp + 1)) return rc;
     k_group_off<<<(ng + 1 + 255) / 256, 256, 0, stream>>>(pc_base.as<int32_t>(), wk_base.as<int32_t>(),
-                                                         jn_off.as<int64_t>(), ng, st_goff.as<int64_t>());
-    launches += 6 + scan_launch_count(ng + 1) + scan_launch_count(npc + 1) + scan_launch_count(nch + 1);
+                                                         jn_pbase.as<int32_t>(), jn_off.as<int64_t>(), ng,
+                                                         st_goff.as<int64_t>());
+    launches += 8 + scan_launch_count(ng + 1) + scan_launch_count(npc + 1) + scan_launch_count(nch + 1) +
+                scan_launch_count(njp + 1);
     if (sizing) {
         int64_t *g64 = static_cast<int64_t *>(stoff_host.p);
         int32_t *errp = reinterpret_cast<int32_t *>(g64 + ng + 1);
@@ -895,10 +913,11 @@ int frame::stroke_passes(bool sizing) {
 
 // The outlines from the counted joins (k_join's write pass).
 int frame::stroke_write() {
-    const int nch = static_cast<int>(n_chunks);
-    const int jgrid = std::max(1, (nch + kStrokeWarps - 1) / kStrokeWarps);
-    k_join<true><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(), nch,
-                                                          jn_cnt.as<int32_t>(), jn_alpha.as<float>(), nullptr,
+    const int njp = static_cast<int>(n_jpos);
+    const int jgrid = std::max(1, (njp + kStrokeWarps * 32 - 1) / (kStrokeWarps * 32));
+    k_join<true><<<jgrid, kStrokeWarps * 32, 0, stream>>>(stroke_args(), wk_chunks.as<walk_chunk>(),
+                                                          jn_pbase.as<int32_t>(), jn_pchunk.as<int32_t>(), njp,
+                                                          jn_cnt.as<int32_t>(), jn_alpha.as<float>(),
                                                           jn_off.as<int64_t>(),
                                                           flat_pts.as<float2>() + nflat, flat_prev.as<int32_t>() + nflat,
                                                           static_cast<int32_t>(nflat), n_outline);

@@ -492,31 +492,48 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_walk(stroke_in in, const 
     }
 }
 
-// k_join: one warp per chunk.  EMIT=false writes each position's point
-// count to jcnt[32 * chunk + lane] (and a round join's factor to
-// jalpha[32 * chunk + lane]) and each chunk's total to csum[chunk];
-// EMIT=true writes the joins (and caps) at coff[chunk] + the counts of the
-// lanes before, with prev links: the point before, except for a polygon's
-// first point, linked to the polygon's last.
+// The walk positions of every chunk, packed: pos_base[c] (an exclusive
+// scan of the chunks' lane counts) is chunk c's first packed position, and
+// pos_chunk[p] the chunk of packed position p.  A piece of a few points
+// makes a chunk of a few lanes; packed, the joins of many such chunks share
+// a warp.
+__global__ void k_chunk_lanes(const walk_chunk *__restrict__ chunks, int n_chunks, int32_t *__restrict__ lanes) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < n_chunks) lanes[c] = chunks[c].n;
+}
+
+__global__ void k_chunk_positions(const walk_chunk *__restrict__ chunks, int n_chunks,
+                                  const int32_t *__restrict__ pos_base, int32_t *__restrict__ pos_chunk) {
+    const int lane = threadIdx.x & 31;
+    const int c = static_cast<int>((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+    if (c >= n_chunks) return;
+    if (lane < chunks[c].n) pos_chunk[pos_base[c] + lane] = c;
+}
+
+// k_join: one thread per packed walk position.  EMIT=false writes the
+// position's point count to jcnt[p] (and a round join's factor to
+// jalpha[p]); EMIT=true writes the join (or cap) at joff[p] (the exclusive
+// scan of the counts), with prev links: the point before, except for a
+// polygon's first point, linked to the polygon's last.
 template <bool EMIT>
 __global__ void __launch_bounds__(kStrokeWarps * 32) k_join(stroke_in in, const walk_chunk *__restrict__ chunks,
-                                                            int n_chunks, int32_t *__restrict__ jcnt,
-                                                            float *__restrict__ jalpha,
-                                                            int32_t *__restrict__ csum, const int64_t *__restrict__ coff,
+                                                            const int32_t *__restrict__ pos_base,
+                                                            const int32_t *__restrict__ pos_chunk, int n_pos,
+                                                            int32_t *__restrict__ jcnt, float *__restrict__ jalpha,
+                                                            const int64_t *__restrict__ joff,
                                                             float2 *__restrict__ out, int32_t *__restrict__ prev,
                                                             int32_t base, int64_t cap) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int c = blockIdx.x * kStrokeWarps + w;
-    if (c >= n_chunks) return;
+    const int p = static_cast<int>(static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x);
+    if (p >= n_pos) return;
+    const int c = pos_chunk[p];
+    const int lane = p - pos_base[c];
     const walk_chunk h = chunks[c];
     const stroke_style s = in.styles[h.style];
     const float2 *pp = piece_points(in, h.pts);
     const bool backward = h.flags & 1, closed = h.flags & 2;
     const int cnt = h.cnt;
     const int pos = h.pos0 + lane;
-    const bool valid = lane < h.n;
-    const bool is_cap = valid && !closed && !(h.flags & 4) && pos == cnt;
+    const bool is_cap = !closed && !(h.flags & 4) && pos == cnt;
     // the two accepted points before this lane's position
     unsigned below = h.acc & ((1u << lane) - 1u);
     int p1 = h.c1, p2 = h.c2;
@@ -539,41 +556,34 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_join(stroke_in in, const 
     if (!EMIT) {
         if (join) n = stroke_join<false>(jp, unit2(din), len2(din), unit2(dout), len2(dout), s, nullptr, 0, alpha);
         else if (capped) n = stroke_cap<false>(jp, unit2(din), s, nullptr, 0);
-        jalpha[32LL * c + lane] = alpha;
+        jalpha[p] = alpha;
         if (n > (1 << 24)) {   // a join or cap far beyond any canvas (line width ~1e11)
             atomicOr(in.error, 1);
             n = 0;
         }
-        jcnt[32LL * c + lane] = n;
-        int t = warp_sum(n);
-        if (lane == 0) csum[c] = t;
+        jcnt[p] = n;
         return;
     }
-    n = valid ? jcnt[32LL * c + lane] : 0;
-    int incl = n;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        int t = __shfl_up_sync(full, incl, d);
-        if (lane >= d) incl += t;
-    }
-    const int64_t at = coff[c] + incl - n;
+    n = jcnt[p];
+    const int64_t at = joff[p];
     if (n == 0 || at < 0 || at + n > cap) return;
-    alpha = jalpha[32LL * c + lane];
+    alpha = jalpha[p];
     if (join) stroke_join<true>(jp, unit2(din), len2(din), unit2(dout), len2(dout), s, out + at, n, alpha);
     else stroke_cap<true>(jp, unit2(din), s, out + at, n);
-    const int64_t first = coff[h.poly0], last = coff[h.poly1] - 1;
+    const int64_t first = joff[pos_base[h.poly0]], last = joff[pos_base[h.poly1]] - 1;
     for (int k = 0; k < n; ++k) {
         int64_t e = at + k;
         prev[e] = base + static_cast<int32_t>(e == first ? last : e - 1);
     }
 }
 
-// Output range of each group: goff[g] = coff of its first piece's first
-// chunk (g <= n).
+// Output range of each group: goff[g] = the offset of its first piece's
+// first chunk's first position (g <= n).
 __global__ void k_group_off(const int32_t *__restrict__ piece_base, const int32_t *__restrict__ chunk_base,
-                            const int64_t *__restrict__ coff, int n, int64_t *__restrict__ goff) {
+                            const int32_t *__restrict__ pos_base, const int64_t *__restrict__ joff, int n,
+                            int64_t *__restrict__ goff) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g <= n) goff[g] = coff[chunk_base[piece_base[g]]];
+    if (g <= n) goff[g] = joff[pos_base[chunk_base[piece_base[g]]]];
 }
 
 }  // namespace cyg

@@ -128,25 +128,38 @@ static polys device_outline(const float *points, const int *counts, const int *c
     const int nch = wbase[npc];
     std::vector<walk_chunk> chunks(nch + 1);
     run_warps(npc, kStrokeWarps, [&] { k_walk(si, pieces.data(), npc, wbase.data(), chunks.data()); });
-    std::vector<int32_t> jcnt(32 * (nch + 1)), csum(nch + 1);
-    std::vector<float> jalpha(32 * (nch + 1));
-    std::vector<int64_t> coff(nch + 2);
-    run_warps(nch, kStrokeWarps, [&] {
-        k_join<false>(si, chunks.data(), nch, jcnt.data(), jalpha.data(), csum.data(), nullptr, nullptr, nullptr, 0, 0);
+    std::vector<int32_t> lanes(nch + 1), pos_base(nch + 2);
+    run_threads(nch, 256, [&] { k_chunk_lanes(chunks.data(), nch, lanes.data()); });
+    pos_base[0] = 0;
+    for (int c = 0; c < nch; ++c) pos_base[c + 1] = pos_base[c] + lanes[c];
+    const int njp = pos_base[nch];
+    std::vector<int32_t> pos_chunk(njp + 1, -1);
+    run_threads(nch * 32, 256, [&] { k_chunk_positions(chunks.data(), nch, pos_base.data(), pos_chunk.data()); });
+    for (int p = 0; p < njp; ++p)
+        if (pos_chunk[p] < 0) {
+            std::fprintf(stderr, "unmapped position %d\n", p);
+            std::exit(2);
+        }
+    std::vector<int32_t> jcnt(njp + 1);
+    std::vector<float> jalpha(njp + 1);
+    std::vector<int64_t> joff(njp + 2);
+    run_threads(njp, kStrokeWarps * 32, [&] {
+        k_join<false>(si, chunks.data(), pos_base.data(), pos_chunk.data(), njp, jcnt.data(), jalpha.data(), nullptr,
+                      nullptr, nullptr, 0, 0);
     });
-    coff[0] = 0;
-    for (int c = 0; c < nch; ++c) coff[c + 1] = coff[c] + csum[c];
+    joff[0] = 0;
+    for (int p = 0; p < njp; ++p) joff[p + 1] = joff[p] + jcnt[p];
     if (err) {
         std::fprintf(stderr, "stroke error flag\n");
         std::exit(2);
     }
-    const int64_t n = coff[nch];
+    const int64_t n = joff[njp];
     const int base = 1000;
     std::vector<float2> out(n + 1);
     std::vector<int32_t> prev(n + 1, -7);
-    run_warps(nch, kStrokeWarps, [&] {
-        k_join<true>(si, chunks.data(), nch, jcnt.data(), jalpha.data(), nullptr, coff.data(), out.data(), prev.data(),
-                     base, n);
+    run_threads(njp, kStrokeWarps * 32, [&] {
+        k_join<true>(si, chunks.data(), pos_base.data(), pos_chunk.data(), njp, jcnt.data(), jalpha.data(), joff.data(),
+                     out.data(), prev.data(), base, n);
     });
     // polygons from the links: prev of a polygon's first point is its last
     for (int64_t k = 0; k < n;) {
