@@ -192,8 +192,13 @@ __device__ int raster_chunks(const strip_params &P, const strip_cmd &e, int W, i
             const float4 sg = P.bin_seg[ei];
             int band = b0;
             while (band < b1 && ei >= off[band + 1]) ++band;
-            // the warp's rows inside the entry's band
+            // the warp's rows inside the entry's band, and inside the rows
+            // the segment can touch, [floor(min y), ceil(max y)] (a cheap
+            // test before the setup: most entries of a band lie in other
+            // warps' rows)
             int ylo = max(ya, band * band_h), yhi = min(yb, (band + 1) * band_h - 1);
+            ylo = max(ylo, static_cast<int>(floorf(fminf(sg.y, sg.w))));
+            yhi = min(yhi, static_cast<int>(ceilf(fmaxf(sg.y, sg.w))));
             if (ylo <= yhi && dda_setup(f2(sg.x, sg.y), f2(sg.z, sg.w), p)) {
                 int n = p.nrows < H + 2 ? p.nrows : H + 2;
                 int py0 = static_cast<int>(p.py0);
