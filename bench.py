@@ -256,6 +256,66 @@ def reference_arm(args, world, rank):
         dist.destroy_process_group()
 
 
+def time_frame(frame, runs, torch):
+    """Device milliseconds per run of a captured frame (CUDA events on the
+    frame's stream, after warm-up)."""
+    stream = torch.cuda.ExternalStream(frame.stream())
+    frame.capture()
+    for _ in range(3):
+        frame.run()
+    frame.sync()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(runs):
+        frame.run()
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b) / runs
+
+
+def tiger_bench(args, native, T, torch):
+    """The reference's own demo drawing (demos/tiger/tiger.cpp: a 733 x 757
+    tiger, about 300 fills and strokes), from its recorded call list: one
+    tiger per frame (latency), a batch of tigers in one frame (throughput),
+    the public replay call end to end, and the oracle port on one host
+    thread (best of 5), beside the reference's own time for it."""
+    import numpy as np
+    import oracle
+    tb = T.load(os.path.join(HERE, "tests", "golden", "ref_demos", "tiger.trace.z"))
+    w, h = T.canvas_size(tb)
+    want = np.frombuffer(T.parse(tb).expected_images()[-1][2].tobytes(), np.uint8).reshape(-1, 4).astype(np.int16)
+    cpu_best = min(_timed(lambda: oracle.replay(tb)) for _ in range(5))
+    f = native.Frame([tb], 0)
+    single_ms = time_frame(f, 20, torch)
+    f.finish()
+    f.close()
+    native.replay(tb)
+    e2e_s = min(_timed(lambda: native.replay(tb)) for _ in range(10))
+    n = args.tiger_canvases
+    f = native.Frame([tb] * n, 0)
+    batch_ms = time_frame(f, max(args.steps, 3), torch)
+    outs = f.finish()
+    f.close()
+    d = np.abs(np.frombuffer(outs[0], np.uint8).reshape(-1, 4).astype(np.int16) - want)
+    same = all(o == outs[0] for o in outs)
+    return {"canvas": f"{w}x{h}, the reference's demos/tiger/tiger.cpp as recorded (tests/golden/ref_demos)",
+            "single_ms": round(single_ms, 3), "single_e2e_ms": round(e2e_s * 1e3, 3),
+            "batch": {"canvases": n, "ms_per_frame": round(batch_ms, 3),
+                      "ms_per_tiger": round(batch_ms / n, 4),
+                      "mpix_s": round(n * w * h / (batch_ms / 1e3) / 1e6, 1)},
+            "cpu_single_thread_ms": round(cpu_best * 1e3, 2), "cpu_kind": "port",
+            "parity_vs_reference": {"max_lsb": int(d.max(initial=0)),
+                                    "pixels_differing": int(np.any(d != 0, axis=1).sum()),
+                                    "all_batch_canvases_identical": same},
+            "coverage": args.coverage}
+
+
+def _timed(fn):
+    t0 = time.perf_counter()
+    fn()
+    return time.perf_counter() - t0
+
+
 def gpu_arm(args, world, rank, local):
     import numpy as np
 
@@ -401,6 +461,7 @@ def gpu_arm(args, world, rank, local):
         f.finish()
         f.close()
     plain = pixels_of(sample) / (plain_ms / 1e3) / 1e6 if plain_ms > 0 else None
+    tiger = tiger_bench(args, native, T, torch) if rank == 0 and args.tiger_canvases > 0 else None
     # Serving: Poisson arrivals of mixed-size requests (cycled from the
     # generated pool), continuous batching under a 150 GB admission budget
     # (rank 0).  Each stated rate is offered for --serve-seconds of arrivals
@@ -483,6 +544,7 @@ def gpu_arm(args, world, rank, local):
         "plain_per_canvas": {"value": round(plain, 2) if plain else None, "unit": "Mpix/s",
                              "sample_canvases": len(sample)},
         "batched_over_plain": round(value / plain, 2) if plain else None,
+        "tiger": tiger,
         "phases_ms": {k: round(v, 3) for k, v in phases.items()},
         "roofline": roofline,
         "cpu_baseline": cpu,
@@ -509,6 +571,7 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--parity-sample", type=int, default=32)
     ap.add_argument("--single-sample", type=int, default=24, help="canvases of the single-thread CPU baseline")
+    ap.add_argument("--tiger-canvases", type=int, default=256, help="tigers per frame in the demo timing (0: none)")
     ap.add_argument("--autotune", type=int, default=1, help="pick the strip configuration by timing (1) or not (0)")
     ap.add_argument("--serve-requests", type=int, default=240, help="requests per arrival rate (0: no serving run)")
     ap.add_argument("--serve-workers", type=int, default=4)

@@ -7,12 +7,18 @@ Runs only where the reference sources are present.  Steps:
      reference's get_image_data / is_point_in_path / measure_text answers;
   3. store each call list zlib-compressed as ref_tests/<name>.trace.z and
      write manifest.json with the golden hash of every test, read from the
-     reference's table (test/test.cpp:2185-2261), and the hash the
-     reference produced here.
+     reference's table (test/test.cpp:2185-2261), the hash the reference
+     produced here, and the SHA-256 of the PNG file its own writer made of
+     the test's image (test.cpp's --pngs, write_png at test.cpp:2415-2511);
+  4. run the reference's tiger demo (demos/tiger/tiger.cpp) compiled against
+     the same recording canvas: its first canvas's call list goes to
+     ref_demos/tiger.trace.z, and the SHA-256 of the tiger.tga its own TGA
+     writer made (tiger.cpp:4333-4345) to the manifest's "demos".
 
 Usage: python tests/golden/make_golden.py REFERENCE_ROOT   (or CY_REFERENCE_ROOT set)
 """
 import glob
+import hashlib
 import json
 import os
 import re
@@ -39,8 +45,8 @@ def main() -> None:
     os.makedirs(out_dir, exist_ok=True)
     with tempfile.TemporaryDirectory() as tmp:
         env = dict(os.environ, CY_RECORD_DIR=tmp)
-        log = subprocess.run([os.path.join(REPO, "oracle", "_ref", "ref_recorder"), "--plain"],
-                             env=env, check=True, capture_output=True, text=True).stdout
+        log = subprocess.run([os.path.join(REPO, "oracle", "_ref", "ref_recorder"), "--plain", "--pngs"],
+                             env=env, cwd=tmp, check=True, capture_output=True, text=True).stdout
         lines = [l for l in log.splitlines() if re.match(r"\s*\d+/\d+ \[", l)]
         traces = sorted(glob.glob(os.path.join(tmp, "trace_*.bin")))
         if len(lines) != len(traces):
@@ -53,13 +59,31 @@ def main() -> None:
                 raw = f.read()
             with open(os.path.join(out_dir, name + ".trace.z"), "wb") as f:
                 f.write(zlib.compress(raw, 9))
+            with open(os.path.join(tmp, name + ".png"), "rb") as f:
+                png = f.read()
             entry = dict(name=name, trace="ref_tests/" + name + ".trace.z",
-                         reference_hash=int(m.group(2), 16), reference_passed=m.group(1) == "PASS")
+                         reference_hash=int(m.group(2), 16), reference_passed=m.group(1) == "PASS",
+                         reference_png_sha256=hashlib.sha256(png).hexdigest(), reference_png_bytes=len(png))
             entry.update(table[name])
             manifest.append(entry)
+    demos = []
+    demo_dir = os.path.join(HERE, "ref_demos")
+    os.makedirs(demo_dir, exist_ok=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        env = dict(os.environ, CY_RECORD_DIR=tmp)
+        subprocess.run([os.path.join(REPO, "oracle", "_ref", "ref_tiger_recorder")], env=env, cwd=tmp, check=True,
+                       capture_output=True)
+        with open(os.path.join(tmp, "trace_000.bin"), "rb") as f:   # the first trial's canvas
+            raw = f.read()
+        with open(os.path.join(demo_dir, "tiger.trace.z"), "wb") as f:
+            f.write(zlib.compress(raw, 9))
+        with open(os.path.join(tmp, "tiger.tga"), "rb") as f:
+            tga = f.read()
+        demos.append(dict(name="tiger", trace="ref_demos/tiger.trace.z", width=733, height=757,
+                          reference_tga_sha256=hashlib.sha256(tga).hexdigest(), reference_tga_bytes=len(tga)))
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
-        json.dump({"source": "canvas_ity test/test.cpp via oracle/ref/recorder.cpp",
-                   "tests": manifest}, f, indent=1)
+        json.dump({"source": "canvas_ity test/test.cpp and demos/tiger/tiger.cpp via oracle/ref/recorder.cpp",
+                   "tests": manifest, "demos": demos}, f, indent=1)
     print(f"wrote {len(manifest)} fixtures")
 
 

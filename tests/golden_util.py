@@ -15,8 +15,21 @@ def manifest() -> List[dict]:
         return json.load(f)["tests"]
 
 
+def demos() -> List[dict]:
+    """The reference's demo programs recorded (the tiger): call list, size
+    and the SHA-256 of the image file the demo itself wrote."""
+    with open(os.path.join(GOLDEN, "manifest.json")) as f:
+        return json.load(f).get("demos", [])
+
+
 def load_fixture(entry: dict) -> bytes:
     return T.load(os.path.join(GOLDEN, entry["trace"]))
+
+
+def final_image(trace_bytes: bytes) -> np.ndarray:
+    """The reference's answer to the call list's last get_image_data: for the
+    recorded tests and demos, the whole canvas read after drawing."""
+    return T.parse(trace_bytes).expected_images()[-1][2]
 
 
 def split_images(trace_bytes: bytes, raw: bytes) -> List[np.ndarray]:

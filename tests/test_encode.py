@@ -2,8 +2,11 @@
 reference's own writers make of the same get_image_data pixels -- the test
 harness's uncompressed PNG (test/test.cpp:2415-2511) and the tiger demo's
 TGA (demos/tiger/tiger.cpp:4336-4343), restated here with zlib's CRC-32 and
-Adler-32."""
+Adler-32.  The restatements are pinned to the files the reference's writers
+made (SHA-256 in tests/golden/manifest.json): the PNG of every recorded
+reference test and the tiger demo's tiger.tga."""
 import ctypes
+import hashlib
 import struct
 import zlib
 
@@ -12,6 +15,7 @@ import pytest
 
 from canvas_ity_gb300 import native, scenes
 from canvas_ity_gb300 import trace as T
+import golden_util as G
 
 
 def ref_png(rgba: bytes, w: int, h: int) -> bytes:
@@ -46,6 +50,64 @@ def test_reference_png_restatement_is_a_valid_stream():
     n = struct.unpack(">I", png[at:at + 4])[0]
     rows = zlib.decompress(png[at + 8:at + 8 + n])
     assert rows == b"".join(b"\x00" + rgba[y * 20:(y + 1) * 20] for y in range(h))
+
+
+def sha(b: bytes) -> str:
+    return hashlib.sha256(b).hexdigest()
+
+
+MANIFEST = G.manifest()
+DEMOS = G.demos()
+
+
+@pytest.mark.parametrize("entry", MANIFEST, ids=[e["name"] for e in MANIFEST])
+def test_png_restatement_is_the_reference_writer(entry):
+    """ref_png of a test's final image is the file the reference's own
+    write_png made of it (test.cpp --pngs)."""
+    img = G.final_image(G.load_fixture(entry))
+    h, w = img.shape[:2]
+    png = ref_png(img.tobytes(), w, h)
+    assert len(png) == entry["reference_png_bytes"]
+    assert sha(png) == entry["reference_png_sha256"]
+
+
+@pytest.mark.parametrize("demo", DEMOS, ids=[d["name"] for d in DEMOS])
+def test_tga_restatement_is_the_tiger_writer(demo):
+    img = G.final_image(G.load_fixture(demo))
+    tga = ref_tga(img.tobytes(), demo["width"], demo["height"])
+    assert len(tga) == demo["reference_tga_bytes"]
+    assert sha(tga) == demo["reference_tga_sha256"]
+
+
+# small reference tests whose canvases the GPU packs as PNG (exact coverage,
+# where the canvas is the reference's byte for byte)
+PNG_CASES = [e for e in MANIFEST if e["name"] in ("fill_rectangle", "linear_gradient", "shadow_blur", "fill_text",
+                                                  "example_smiley", "draw_image")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("entry", PNG_CASES, ids=[e["name"] for e in PNG_CASES])
+def test_gpu_png_is_the_reference_file(entry):
+    tb = G.load_fixture(entry)
+    w, h = T.canvas_size(tb)
+    G.use_mode("tile_exact")
+    try:
+        got = native.encode_image(tb, native.PNG, 0, 0, w, h)
+    finally:
+        G.use_mode("tile")
+    assert sha(got) == entry["reference_png_sha256"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("demo", DEMOS, ids=[d["name"] for d in DEMOS])
+def test_gpu_tga_is_the_tiger_file(demo):
+    tb = G.load_fixture(demo)
+    G.use_mode("tile_exact")
+    try:
+        got = native.encode_image(tb, native.TGA, 0, 0, demo["width"], demo["height"])
+    finally:
+        G.use_mode("tile")
+    assert sha(got) == demo["reference_tga_sha256"]
 
 
 def test_encode_rejects_bad_arguments():

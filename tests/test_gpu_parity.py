@@ -175,6 +175,26 @@ def test_reference_suite_bytes_identical(engine, entry):
         assert np.array_equal(g, w), f"{entry['name']} read {i}: {int((g != w).any(axis=-1).sum())} pixels differ"
 
 
+DEMOS = G.demos()
+
+
+@pytest.mark.parametrize("demo", DEMOS, ids=[d["name"] for d in DEMOS])
+def test_reference_demo(engine, stroke, demo):
+    """The reference's tiger demo (demos/tiger/tiger.cpp, 733 x 757): the
+    RGBA8 canvas within the contract of the reference's own bytes (equal to
+    them in the exact modes), byte-identical to the mode's oracle, and the
+    float canvas bit for bit the oracle's."""
+    tb = G.load_fixture(demo)
+    got = G.split_images(tb, native.replay(tb)[0])[-1]
+    want = G.final_image(tb)
+    assert_images_close(got, want, demo["name"], engine)
+    if engine != "tile":
+        assert np.array_equal(got, want)
+    mine = oracle_images(tb, ties="sign", trig=trig(), coverage=G.oracle_coverage(engine))[-1]
+    assert np.array_equal(got, mine)
+    assert_float_canvas_exact(tb, demo["name"], engine)
+
+
 @pytest.mark.parametrize("seed", range(8))
 def test_rgba8_identical_to_oracle_on_workload(engine, stroke, seed):
     """RGBA8 bytes of many-canvas workload canvases equal the oracle's with

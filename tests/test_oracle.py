@@ -35,6 +35,23 @@ def test_oracle_matches_reference_fixture(entry):
     assert cy_hash.hamming(cy_hash.hash_image(got[-1]), entry["golden_hash"]) <= 5
 
 
+DEMOS = G.demos()
+
+
+@pytest.mark.parametrize("demo", DEMOS, ids=[d["name"] for d in DEMOS])
+def test_oracle_matches_reference_demo(demo):
+    """The reference's tiger demo (demos/tiger/tiger.cpp, 733 x 757, its
+    headline drawing): the oracle reproduces the reference's bytes, and the
+    binned restatement stays within the contract."""
+    tb = G.load_fixture(demo)
+    want = G.final_image(tb)
+    assert want.shape == (demo["height"], demo["width"], 4)
+    got = G.split_images(tb, oracle.replay(tb)[0])[-1]
+    assert np.array_equal(got, want)
+    binned = G.split_images(tb, oracle.replay(tb, ties="sign", trig="cr", coverage="binned")[0])[-1]
+    G.assert_within_contract(binned, want, demo["name"])
+
+
 def test_get_image_data_known_answer():
     """test/test.cpp:1800-1826: strided, offset read of a 10x10 checker."""
     entry = next(e for e in MANIFEST if e["name"] == "get_image_data")
