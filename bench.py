@@ -419,7 +419,7 @@ def gpu_arm(args, world, rank, local):
     # End to end through the public C ABI (cy_render_traces): call lists in
     # host memory to RGBA8 reads in host memory, every step replaying,
     # uploading, rendering and reading back all canvases; frames of about
-    # 64 Mpx are pipelined so host work overlaps device work.  The output
+    # 32 Mpx are pipelined so host work overlaps device work.  The output
     # buffer and its per-canvas offsets (the sizes of the recorded
     # get_image_data calls) are the caller's, prepared once.
     t_e2e = 0.0

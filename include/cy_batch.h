@@ -134,7 +134,7 @@ int cy_frame_collect(cy_frame *frame, unsigned char *out, size_t cap, size_t *of
 int cy_frame_finish_views(cy_frame *frame, const unsigned char **data, size_t *offsets);
 
 /* End to end over many call lists: replay on the host, upload, render and
- * read back, in frames of about `frame_pixels` canvas pixels (0: 64 Mi).
+ * read back, in frames of about `frame_pixels` canvas pixels (0: 32 Mi).
  * While the device renders one frame, the host replays and stages the
  * next, and copies out the one before.  Canvas i's reads (compact RGBA8
  * rectangles in call order) are written to out[offsets[i] .. offsets[i+1]);
