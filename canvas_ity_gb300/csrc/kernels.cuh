@@ -447,11 +447,14 @@ __global__ void k_bin(job_tables t, bin_tables bt, int total_segments) {
                 if (!EMIT) {
                     if (lane == leader) atomicAdd(bt.cnt + bin, __popc(peers));
                 } else {
+                    // the bin's range is read before the atomic, so the two
+                    // round trips overlap
+                    const int64_t o0 = bt.off[bin], o1 = bt.off[bin + 1];
                     int first = 0;
                     if (lane == leader) first = atomicAdd(bt.cur + bin, __popc(peers));
                     first = __shfl_sync(peers, first, leader);
-                    int64_t at = bt.off[bin] + first + rank;
-                    if (at < bt.off[bin + 1]) bt.seg[at] = make_float4(pa[i].x, pa[i].y, pb[i].x, pb[i].y);
+                    int64_t at = o0 + first + rank;
+                    if (at < o1) bt.seg[at] = make_float4(pa[i].x, pa[i].y, pb[i].x, pb[i].y);
                 }
             }
         }
