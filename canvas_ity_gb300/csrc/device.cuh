@@ -255,12 +255,21 @@ __device__ __forceinline__ void dda_row(const dda_piece &p, int k, Emit &emit) {
 
 // Clip one polyline segment to [0,width] x [0,height] the way the
 // reference's Sutherland-Hodgman pass and clamp do (hpp:2204-2239), summed
-// over a polygon: the part left of x = 0 is replaced by its projection onto
+// over a polygon (far-off ends aside, crossing2): the part left of x = 0 is replaced by its projection onto
 // that edge; parts above y = 0 or below y = height contribute nothing, and
 // so does the part right of x = width, whose projection onto that edge adds
 // only to cells at x >= width, which no pixel reads.  Up to two pieces in
 // fixed slots (0 inside, 1 the left edge, each clamped); returns the mask of
 // the slots filled, none for a segment with a non-finite end.
+// Where u -> v crosses an edge, fs and ts the signed distances of u and v
+// from it: the reference's u + t (v - u) (hpp:2220-2221), except when u lies
+// 2^24 or more beyond the edge and v nearer, where that loses the crossing
+// to cancellation (1e30 and 48 differ by nothing in float): then from v.
+__device__ __forceinline__ float2 crossing2(float2 u, float2 v, float fs, float ts) {
+    return fabsf(fs) >= 16777216.0f && fabsf(fs) > fabsf(ts) ? mix2(v, u, ts / (ts - fs))
+                                                             : mix2(u, v, fs / (fs - ts));
+}
+
 __device__ __forceinline__ unsigned clip_segment(float2 a, float2 b, float width, float height, float2 (&pa)[2],
                                                  float2 (&pb)[2]) {
     if (!(isfinite(a.x) && isfinite(a.y) && isfinite(b.x) && isfinite(b.y))) return 0u;
@@ -275,7 +284,7 @@ __device__ __forceinline__ unsigned clip_segment(float2 a, float2 b, float width
             la = f2(0.0f, ma.y);
             lb = f2(0.0f, mb.y);
         } else if (fs * ts < 0.0f) {
-            float2 I = mix2(ma, mb, fs / (fs - ts));
+            float2 I = crossing2(ma, mb, fs, ts);
             has_left = true;
             if (fs < 0.0f) { la = f2(0.0f, ma.y); lb = f2(0.0f, I.y); ma = I; }
             else { la = f2(0.0f, I.y); lb = f2(0.0f, mb.y); mb = I; }
@@ -286,7 +295,7 @@ __device__ __forceinline__ unsigned clip_segment(float2 a, float2 b, float width
         if (!has) return;
         if (fs < 0.0f && ts < 0.0f) { has = false; return; }
         if (fs * ts < 0.0f) {
-            float2 I = mix2(u, v, fs / (fs - ts));
+            float2 I = crossing2(u, v, fs, ts);
             if (fs < 0.0f) u = I; else v = I;
         }
     };
@@ -298,7 +307,7 @@ __device__ __forceinline__ unsigned clip_segment(float2 a, float2 b, float width
         if (fs < 0.0f && ts < 0.0f) {
             has_main = false;
         } else if (fs * ts < 0.0f) {
-            float2 I = mix2(ma, mb, fs / (fs - ts));
+            float2 I = crossing2(ma, mb, fs, ts);
             if (fs < 0.0f) ma = I; else mb = I;
         }
     }

@@ -1698,8 +1698,10 @@ namespace {
 
 void bounds_of(const float *xy, size_t n, command &c) {
     float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+    bool finite = true;
     for (size_t i = 0; i < n; ++i) {
         float x = xy[2 * i], y = xy[2 * i + 1];
+        finite = finite && std::isfinite(x) && std::isfinite(y);
         if (x < x0) x0 = x;
         if (x > x1) x1 = x;
         if (y < y0) y0 = y;
@@ -1711,8 +1713,11 @@ void bounds_of(const float *xy, size_t n, command &c) {
         if (v > 1.0e9f) return 1000000000;
         return static_cast<int>(floorf(v));
     };
-    // NaN coordinates make the bounds unknown: use the whole canvas.
-    bool bad = !(x0 <= x1) || !(y0 <= y1);
+    // A non-finite coordinate makes the bounds unknown: the whole canvas,
+    // and the polygon clip, which leaves such points out and joins their
+    // neighbours as the reference's does (hpp:2218-2223); without the clip a
+    // NaN point would leave its polygon open.
+    bool bad = !finite || !(x0 <= x1) || !(y0 <= y1);
     c.gx0 = bad ? -1000000000 : clampi(x0);
     c.gy0 = bad ? -1000000000 : clampi(y0);
     c.gx1 = bad ? 1000000000 : clampi(x1) + 1;

@@ -359,6 +359,33 @@ __device__ __forceinline__ int segment_at(const job_tables &t, int c, int s, flo
     return ji;
 }
 
+// Segment s of a binned job: the segment ending at its point k, from the
+// nearest point before k with finite coordinates.  A non-finite point is
+// left out and its neighbours joined, as the polygon clip drops it (its
+// comparisons fail for NaN, hpp:2218-2223): the segment ending at it is
+// dropped (false), and the one leaving it starts further back.
+__device__ __forceinline__ bool binned_segment(const job_tables &t, int c, int s, float2 &a, float2 &b, int &ji) {
+    ji = t.tab[c].y;
+    const scan_job &jj = t.jobs[ji];
+    const int k = jj.line_first + (s - t.tab[c].x);
+    const float2 *pts = jj.geom ? t.pts[1] : t.pts[0];
+    const int32_t *prev = jj.geom ? t.prev[1] : t.prev[0];
+    auto finite = [](float2 p) { return isfinite(p.x) && isfinite(p.y); };
+    float2 pb = pts[k];
+    b = f2(jj.offx + pb.x, jj.offy + pb.y);
+    if (!finite(b)) return false;
+    int j = prev[k];
+    float2 pa = pts[j];
+    a = f2(jj.offx + pa.x, jj.offy + pa.y);
+    // the links of a subpath form a cycle through k: the walk ends there
+    for (int guard = 0; !finite(a) && j != k && guard < jj.seg_count; ++guard) {
+        j = prev[j];
+        pa = pts[j];
+        a = f2(jj.offx + pa.x, jj.offy + pa.y);
+    }
+    return finite(a) && j != k;
+}
+
 // Segment s of the scan (the table's, or the last clip pass's polygons).
 template <bool CLIPPED>
 __device__ __forceinline__ int segment_raw(const job_tables &t, int s, float2 &a, float2 &b) {
@@ -420,9 +447,10 @@ __global__ void k_bin(job_tables t, bin_tables bt, int total_segments) {
         const int s = base + lane;
         float2 pa[2], pb[2];
         int pbin[2] = {0, 0}, pnb[2] = {0, 0};
-        if (s < total_segments) {
-            float2 a, b;
-            const scan_job &j = t.jobs[segment_raw<false>(t, s, a, b)];
+        float2 a, b;
+        int ji = 0;
+        if (s < total_segments && binned_segment(t, job_entry(t, s), s, a, b, ji)) {
+            const scan_job &j = t.jobs[ji];
             const unsigned has = clip_segment(a, b, j.width, j.height, pa, pb);
 #pragma unroll
             for (int i = 0; i < 2; ++i) {

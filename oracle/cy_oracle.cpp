@@ -1147,6 +1147,15 @@ void canvas::scan_segment_binned(vec2 from, vec2 to) {
 // reads.  A segment with a non-finite end gives none.  In exact arithmetic
 // the pieces of all segments add up to the clipped polygon's coverage; in
 // float they differ from it by rounding only.
+// Where u -> v crosses an edge, fs and ts the signed distances of u and v
+// from it: the reference's u + t (v - u) (hpp:2220-2221), except when u lies
+// 2^24 or more beyond the edge and v nearer, where that loses the crossing
+// to cancellation (1e30 and 48 differ by nothing in float): then from v.
+static inline vec2 crossing(vec2 u, vec2 v, float fs, float ts) {
+    return std::fabs(fs) >= 16777216.0f && std::fabs(fs) > std::fabs(ts) ? mix(v, u, ts / (ts - fs))
+                                                                         : mix(u, v, fs / (fs - ts));
+}
+
 static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec2 *pb) {
     if (!(std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(b.x) && std::isfinite(b.y))) return 0;
     vec2 ma = a, mb = b, la{}, lb{};
@@ -1159,7 +1168,7 @@ static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec
             la = mk(0.0f, ma.y);
             lb = mk(0.0f, mb.y);
         } else if (fs * ts < 0.0f) {
-            vec2 cut = mix(ma, mb, fs / (fs - ts));
+            vec2 cut = crossing(ma, mb, fs, ts);
             has_left = true;
             if (fs < 0.0f) {
                 la = mk(0.0f, ma.y);
@@ -1181,7 +1190,7 @@ static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec
             return;
         }
         if (fs * ts < 0.0f) {
-            vec2 cut = mix(u, v, fs / (fs - ts));
+            vec2 cut = crossing(u, v, fs, ts);
             if (fs < 0.0f) u = cut;
             else v = cut;
         }
@@ -1193,7 +1202,7 @@ static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec
         if (fs < 0.0f && ts < 0.0f) {
             has_main = false;
         } else if (fs * ts < 0.0f) {
-            vec2 cut = mix(ma, mb, fs / (fs - ts));
+            vec2 cut = crossing(ma, mb, fs, ts);
             if (fs < 0.0f) ma = cut;
             else mb = cut;
         }
@@ -1212,18 +1221,27 @@ static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec
 }
 
 // scan() of the draw itself (no offset, no padding) into `acc`: each
-// segment clipped on its own, then the binned cell walk of every piece.
+// segment clipped on its own, then the binned cell walk of every piece.  A
+// point with a non-finite coordinate is left out and its neighbours joined,
+// as the polygon clip drops it (its comparisons fail for NaN, hpp:2218-2223):
+// the segment ending at it is skipped, and the one leaving it starts from
+// the nearest finite point before it.
 void canvas::scan_binned() {
     acc.assign(static_cast<size_t>(W) * static_cast<size_t>(H), 0);
     float width = static_cast<float>(W), height = static_cast<float>(H);
+    auto finite = [](vec2 p) { return std::isfinite(p.x) && std::isfinite(p.y); };
     size_t end = 0;
     for (size_t s = 0; s < lines.subs.size(); ++s) {
         size_t begin = end;
         end += lines.subs[s].count;
         size_t n = end - begin;
         for (size_t i = 0; i < n; ++i) {
-            vec2 from = add(mk(0.0f, 0.0f), lines.pts[begin + (i ? i : n) - 1]);
             vec2 to = add(mk(0.0f, 0.0f), lines.pts[begin + i]);
+            if (!finite(to)) continue;
+            size_t j = (i ? i : n) - 1;
+            while (!finite(lines.pts[begin + j]) && j != i) j = (j ? j : n) - 1;
+            if (j == i) continue;
+            vec2 from = add(mk(0.0f, 0.0f), lines.pts[begin + j]);
             vec2 pa[2], pb[2];
             int pieces = clip_segment(from, to, width, height, pa, pb);
             for (int k = 0; k < pieces; ++k) scan_segment_binned(pa[k], pb[k]);

@@ -103,3 +103,32 @@ def use_mode(mode: str) -> None:
 
 def oracle_coverage(mode: str) -> str:
     return "binned" if mode == "tile" else "runs"
+
+
+def far_point_scene(bad: float) -> bytes:
+    """Three fills on a 64 x 48 canvas, two of them with one vertex at `bad`
+    (a non-finite value, or a point far off the canvas): one in x, one in y."""
+    t = T.TraceWriter(64, 48)
+    t.set_color(T.FILL_STYLE, 0.2, 0.4, 0.8, 1.0)
+    t.begin_path()
+    t.move_to(5, 5)
+    t.line_to(50, 8)
+    t.line_to(bad, 30)
+    t.line_to(40, 44)
+    t.line_to(6, 40)
+    t.close_path()
+    t.fill()
+    t.set_color(T.FILL_STYLE, 0.9, 0.3, 0.1, 0.7)
+    t.begin_path()
+    t.move_to(-20, 10)
+    t.line_to(30, bad)
+    t.line_to(60, 30)
+    t.close_path()
+    t.fill()
+    t.begin_path()
+    t.move_to(10, 10)
+    t.line_to(20, 12)
+    t.line_to(14, 30)
+    t.close_path()
+    t.fill()
+    return t.finish()

@@ -52,6 +52,37 @@ def test_oracle_matches_reference_demo(demo):
     G.assert_within_contract(binned, want, demo["name"])
 
 
+def _image(raw, w=64, h=48):
+    return np.frombuffer(raw, np.uint8).reshape(h, w, 4)
+
+
+@pytest.mark.parametrize("bad", [float("nan"), float("inf"), -float("inf")], ids=["nan", "inf", "-inf"])
+def test_binned_leaves_out_non_finite_points_like_the_polygon_clip(bad):
+    """The reference's polygon clip drops a point whose comparisons fail and
+    joins its neighbours; the binned clip, segment by segment, does the same
+    (the segment leaving the point starts from the finite point before it),
+    so no row is left open."""
+    tb = G.far_point_scene(bad)
+    exact = oracle.replay(tb)[0]
+    binned = oracle.replay(tb, ties="sign", trig="cr", coverage="binned")[0]
+    G.assert_within_contract(_image(binned), _image(exact), f"binned, vertex at {bad}")
+    if oracle.reference_available():
+        assert exact == oracle.reference_replay(tb)[0]
+
+
+@pytest.mark.parametrize("far", [1e9, 1e12, 1e30])
+def test_binned_crossings_hold_for_far_points(far):
+    """From about 1e9 on, the reference's clip loses a far point's crossing
+    with the canvas edge to cancellation (a + t (b - a) with b far away), and
+    the exact oracle keeps that.  The binned clip takes crossings from the
+    nearer end: it draws what a moderately far point (1e6) on nearly the same
+    line draws."""
+    want = _image(oracle.replay(G.far_point_scene(1e6))[0])
+    got = _image(oracle.replay(G.far_point_scene(far), ties="sign", trig="cr", coverage="binned")[0])
+    G.assert_within_contract(got, want, f"binned, vertex at {far}")
+    assert not np.array_equal(_image(oracle.replay(G.far_point_scene(far))[0]), want)
+
+
 def test_get_image_data_known_answer():
     """test/test.cpp:1800-1826: strided, offset read of a 10x10 checker."""
     entry = next(e for e in MANIFEST if e["name"] == "get_image_data")
