@@ -1716,8 +1716,13 @@ void bounds_of(const float *xy, size_t n, command &c) {
     // A non-finite coordinate makes the bounds unknown: the whole canvas,
     // and the polygon clip, which leaves such points out and joins their
     // neighbours as the reference's does (hpp:2218-2223); without the clip a
-    // NaN point would leave its polygon open.
+    // NaN point would leave its polygon open.  So does a coordinate of 2^20
+    // or more: the clip's crossing with such a far point cancels
+    // (hpp:2220-2221) and can land anywhere on the canvas, outside the
+    // points' own bounds.
     bool bad = !finite || !(x0 <= x1) || !(y0 <= y1);
+    if (!bad && std::max(std::max(std::fabs(x0), std::fabs(x1)), std::max(std::fabs(y0), std::fabs(y1))) >= 1048576.0f)
+        bad = true;
     c.gx0 = bad ? -1000000000 : clampi(x0);
     c.gy0 = bad ? -1000000000 : clampi(y0);
     c.gx1 = bad ? 1000000000 : clampi(x1) + 1;
