@@ -394,7 +394,7 @@ struct frame {
     dbuf bin_cnt, bin_cur, bin_off, bin_seg, clip_dev;
     dbuf tabs_dev, cp_cnt, cp_off, cp_pts[2], cp_prev[2], cp_job[2];
     dbuf sj_dev, sh_img, sh_scratch, rects, scv_dev, items_dev, ext_dev, counter, get_dev, lut_dev;
-    dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, st_err, pc_cnt, pc_base, pc_list, wk_cnt, wk_base,
+    dbuf dash_cnt, dash_off, dash_pts, dash_subs, dash_nsub, dash_st, st_err, pc_cnt, pc_base, pc_list, wk_cnt, wk_base,
         wk_chunks, jn_cnt, jn_alpha, jn_sum, jn_off, jn_pbase, jn_pchunk, st_goff;
     hbuf staging, offs_host, rowoff_host, get_host, stoff_host, binoff_host;
     char *d = nullptr;
@@ -496,7 +496,7 @@ struct frame {
                      &row_off, &row_cur, &row_len, &row_meta, &long_rows, &n_long, &runs, &sums, &tabs_dev, &cp_cnt, &cp_off,
                      &cp_pts[0], &cp_pts[1], &cp_prev[0], &cp_prev[1], &cp_job[0], &cp_job[1], &sj_dev, &sh_img, &sh_scratch, &rects,
                      &scv_dev, &items_dev, &ext_dev, &counter, &get_dev, &lut_dev, &dash_cnt, &dash_off, &dash_pts,
-                     &dash_subs, &dash_nsub, &st_err, &pc_cnt, &pc_base, &pc_list, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt,
+                     &dash_subs, &dash_nsub, &dash_st, &st_err, &pc_cnt, &pc_base, &pc_list, &wk_cnt, &wk_base, &wk_chunks, &jn_cnt,
                      &jn_alpha, &jn_sum, &jn_off, &jn_pbase, &jn_pchunk, &st_goff, &bin_cnt, &bin_cur, &bin_off, &bin_seg, &clip_dev};
         for (dbuf *x : b) x->release();
         staging.release();
@@ -781,6 +781,7 @@ stroke_in frame::stroke_args() const {
     si.dash_subs = dash_subs.as<int2>();
     si.dash_off = dash_off.as<int32_t>();
     si.dash_nsub = dash_nsub.as<int32_t>();
+    si.dash_state_at = dash_st.as<dash_state>();
     si.nflat = static_cast<int32_t>(nflat);
     si.n = static_cast<int>(n_groups);
     si.error = st_err.as<int32_t>();
@@ -805,6 +806,9 @@ int frame::stroke_passes(bool sizing) {
         any_dash = false;
         for (cy_ctx *cv : cvs)
             for (const stroke_style &st : cv->q.styles) any_dash = any_dash || st.dash_n > 0;
+        // the dash walk's state at every centre-line point (k_dash)
+        if (any_dash && !dash_st.ensure(static_cast<size_t>(nflat + 1) * sizeof(dash_state)))
+            return fail(CY_ENOMEM, __LINE__);
         if (!ok(cudaMemsetAsync(st_err.p, 0, 4, stream))) return status;
     }
     auto read_back = [&](void *dst, const void *src, size_t bytes) {

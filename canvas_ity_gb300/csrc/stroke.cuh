@@ -123,6 +123,15 @@ __device__ int stroke_cap(float2 point, float2 in_dir, const stroke_style &s, fl
 }
 
 // Inputs of the stroke kernels.
+// The dash walk's state where a centre-line segment starts (hpp:1880-1888
+// and the loop of 1889-1925): the write pass replays each segment from it.
+struct dash_state {
+    float next;                  // distance left in the current pattern entry
+    int32_t seg;                 // current pattern entry
+    int32_t np, ns, first;       // points and dashes written so far, first point of the open dash
+    int32_t emit;                // 1 while inside a dash
+};
+
 struct stroke_in {
     const float2 *flat;          // flattened centre lines (flattening output)
     const int32_t *item_off;     // flattening offsets per flat_item
@@ -133,6 +142,7 @@ struct stroke_in {
     int2 *dash_subs;             // (count, closed) per dash, group g's at dash_off[g]
     const int32_t *dash_off;
     int32_t *dash_nsub;          // dashes per group
+    dash_state *dash_state_at;   // per centre-line point of a dashed group: the state where its segment starts
     int32_t nflat;               // centre-line points before the dashed ones in slot numbering
     int n;
     int32_t *error;              // set to 1 when a subpath exceeds a cap
@@ -146,15 +156,20 @@ __device__ __forceinline__ int warp_sum(int v) {
     return v;
 }
 
-// Dash pass, one warp per subpath: the lanes measure 32 segments at a time
-// (the user-space lengths of hpp:1895), lane 0 carries the pattern phase
-// through them in order.  EMIT=false writes each group's dashed point count
-// (0 without a pattern); EMIT=true writes the dashes.
+// Dash pass, one warp per subpath.  Counting (EMIT=false): the lanes
+// measure 32 segments at a time (the user-space lengths of hpp:1895), lane 0
+// carries the pattern phase through them in order -- a float running sum,
+// so it stays sequential -- and records the walk's state where each segment
+// starts (and after the last one); each group's dashed point count goes to
+// `counts` (0 without a pattern).  Writing (EMIT=true): every lane replays
+// its own segments from their recorded states, so the writes run 32 wide,
+// then lane 0 closes the last dash.
 template <bool EMIT>
 __global__ void __launch_bounds__(kStrokeWarps * 32) k_dash(stroke_in in, int32_t *__restrict__ counts) {
     __shared__ float lens[kStrokeWarps][32];
     __shared__ float2 ends[kStrokeWarps][33];   // the chunk's points (segment ends)
     __shared__ float pat[kStrokeWarps][64];     // the pattern, when it has at most 64 entries
+    __shared__ dash_state states[kStrokeWarps][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int g = blockIdx.x * kStrokeWarps + w;
     if (g >= in.n) return;
@@ -172,93 +187,116 @@ __global__ void __launch_bounds__(kStrokeWarps * 32) k_dash(stroke_in in, int32_
     }
     const int a = in.item_off[gr.head], n = in.item_off[gr.end] - a;
     const float2 *pts = in.flat + a;
-    int o = 0, cap = 0;
-    float2 *out = nullptr;
-    int2 *subs = nullptr;
-    if (EMIT) {
-        o = in.dash_off[g];
-        cap = in.dash_off[g + 1] - o;
-        out = in.dash_pts + o;
-        subs = in.dash_subs + o;
-        if (cap <= 0) {
-            if (lane == 0) in.dash_nsub[g] = 0;
-            return;
-        }
-    }
-    // lane 0's state (hpp:1880-1888)
-    int np = 0, ns = 0, first = 0, seg = s.dash_start;
-    bool emit = (~s.dash_start & 1) != 0;
-    const bool merge_emit = emit;
-    float next = s.dash_next;
-    bool over = false;
-    for (int c = 0; c + 1 < n; c += 32) {
-        int i = c + lane;
-        float line = 0.0f;
-        if (i < n) ends[w][lane] = pts[i];
-        if (lane == 0 && c + 32 < n) ends[w][32] = pts[c + 32];
-        if (i + 1 < n) line = len2(sub2(xform(s.inv, pts[i + 1]), xform(s.inv, pts[i])));
-        lens[w][lane] = line;
-        __syncwarp();
-        if (lane == 0 && !over) {
-            int m = min(32, n - 1 - c);
-            for (int k = 0; k < m; ++k) {
-                float2 from = ends[w][k], to = ends[w][k + 1];
-                float len = lens[w][k];
-                if (emit) {
-                    if (EMIT && np < cap) out[np] = from;
-                    ++np;
-                }
-                while (next < len) {
-                    if (np >= kDashCap) {
-                        over = true;
-                        break;
-                    }
-                    if (EMIT && np < cap) out[np] = mix2(from, to, next / len);
-                    ++np;
-                    if (emit) {
-                        if (EMIT && ns < cap) subs[ns] = make_int2(np - first, 0);
-                        ++ns;
-                        first = np;
-                    }
-                    seg = seg + 1 < s.dash_n ? seg + 1 : 0;
-                    emit = !emit;
-                    next += dash[seg];
-                }
-                if (over) break;
-                next -= len;
-            }
-        }
-        __syncwarp();
-    }
-    int count = 0;   // dashed point count of the rotation below (lane 0)
-    if (lane == 0 && !over && n > 0) {
-        if (emit) {
-            if (EMIT && np < cap) out[np] = pts[n - 1];
-            ++np;
-            if (EMIT && ns < cap) subs[ns] = make_int2(np - first, 0);
-            ++ns;
-            if (gr.closed && merge_emit) {
-                if (ns == 1) {
-                    if (EMIT) subs[0].y = 1;
-                } else {
-                    count = np - first;
-                    if (EMIT) subs[0].x += count;
-                    --ns;
-                }
-            }
-        }
-    }
+    dash_state *state_at = in.dash_state_at + a;
+    const bool merge_emit = (~s.dash_start & 1) != 0;
     if (!EMIT) {
+        // lane 0's state (hpp:1880-1888)
+        int np = 0, ns = 0, first = 0, seg = s.dash_start;
+        bool emit = merge_emit;
+        float next = s.dash_next;
+        bool over = false;
+        for (int c = 0; c + 1 < n; c += 32) {
+            const int i = c + lane, m = min(32, n - 1 - c);
+            float line = 0.0f;
+            if (i < n) ends[w][lane] = pts[i];
+            if (lane == 0 && c + 32 < n) ends[w][32] = pts[c + 32];
+            if (i + 1 < n) line = len2(sub2(xform(s.inv, pts[i + 1]), xform(s.inv, pts[i])));
+            lens[w][lane] = line;
+            __syncwarp();
+            if (lane == 0 && !over) {
+                for (int k = 0; k < m; ++k) {
+                    states[w][k] = dash_state{next, seg, np, ns, first, emit ? 1 : 0};
+                    const float len = lens[w][k];
+                    if (emit) ++np;
+                    while (next < len) {
+                        if (np >= kDashCap) {
+                            over = true;
+                            break;
+                        }
+                        ++np;
+                        if (emit) {
+                            ++ns;
+                            first = np;
+                        }
+                        seg = seg + 1 < s.dash_n ? seg + 1 : 0;
+                        emit = !emit;
+                        next += dash[seg];
+                    }
+                    if (over) break;
+                    next -= len;
+                }
+            }
+            __syncwarp();
+            if (lane < m) state_at[c + lane] = states[w][lane];
+            __syncwarp();
+        }
         if (lane == 0) {
+            if (n > 0 && !over) state_at[n - 1] = dash_state{next, seg, np, ns, first, emit ? 1 : 0};
+            if (emit && !over && n > 0) ++np;   // the last dash ends at the last point
             if (over) atomicOr(in.error, 1);
             counts[g] = over ? 0 : np;
         }
         return;
     }
+    const int o = in.dash_off[g], cap = in.dash_off[g + 1] - o;
+    float2 *out = in.dash_pts + o;
+    int2 *subs = in.dash_subs + o;
+    if (cap <= 0) {
+        if (lane == 0) in.dash_nsub[g] = 0;
+        return;
+    }
+    // every segment from the state where it starts (the loop of hpp:1889-1925)
+    for (int i = lane; i + 1 < n; i += 32) {
+        const dash_state st = state_at[i];
+        const float2 from = pts[i], to = pts[i + 1];
+        const float len = len2(sub2(xform(s.inv, to), xform(s.inv, from)));
+        int np = st.np, ns = st.ns, first = st.first, seg = st.seg;
+        bool emit = st.emit != 0;
+        float next = st.next;
+        if (emit) {
+            if (np < cap) out[np] = from;
+            ++np;
+        }
+        while (next < len && np < cap) {
+            out[np] = mix2(from, to, next / len);
+            ++np;
+            if (emit) {
+                if (ns < cap) subs[ns] = make_int2(np - first, 0);
+                ++ns;
+                first = np;
+            }
+            seg = seg + 1 < s.dash_n ? seg + 1 : 0;
+            emit = !emit;
+            next += dash[seg];
+        }
+    }
+    __syncwarp();
+    int count = 0, np = 0, ns = 0;   // (lane 0) the rotation below, the totals
+    if (lane == 0 && n > 0) {
+        const dash_state st = state_at[n - 1];
+        np = st.np;
+        ns = st.ns;
+        if (st.emit) {
+            if (np < cap) out[np] = pts[n - 1];
+            ++np;
+            if (ns < cap) subs[ns] = make_int2(np - st.first, 0);
+            ++ns;
+            if (gr.closed && merge_emit) {
+                if (ns == 1) {
+                    subs[0].y = 1;
+                } else {
+                    count = np - st.first;
+                    subs[0].x += count;
+                    --ns;
+                }
+            }
+        }
+    }
     // Closed subpath whose first and last dashes are drawn: the last dash
     // moves in front of the first (std::rotate by three reversals).
     count = __shfl_sync(0xffffffffu, count, 0);
     np = __shfl_sync(0xffffffffu, np, 0);
+    __syncwarp();
     if (count > 0 && np == cap) {
         auto reverse = [&](int lo_, int hi_) {
             int len = hi_ - lo_;

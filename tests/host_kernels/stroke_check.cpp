@@ -101,6 +101,8 @@ static polys device_outline(const float *points, const int *counts, const int *c
     si.dash_subs = dsubs.data();
     si.dash_off = doff.data();
     si.dash_nsub = dnsub.data();
+    std::vector<dash_state> dstate(static_cast<size_t>(nflat) + 1);
+    si.dash_state_at = dstate.data();
     si.nflat = nflat;
     si.n = ng;
     si.error = &err;
