@@ -433,11 +433,13 @@ struct bin_tables {
 
 template <bool EMIT>
 __global__ void k_bin(job_tables t, bin_tables bt, int total_segments) {
-    // Segment s of the binned jobs' table, clipped on its own (clip_segment:
+    // Segment s of the binned jobs' table (binned_segment: non-finite points
+    // left out, their neighbours joined), clipped on its own (clip_segment:
     // the part left of the rectangle becomes its projection on x = 0, as the
-    // reference's polygon clip and clamp make it in sum, hpp:2204-2239;
-    // segments with a non-finite end are dropped).  Up to two pieces per
-    // segment in fixed slots, each listed in every band it crosses.  A warp's
+    // reference's polygon clip and clamp make it in sum, hpp:2204-2239; the
+    // parts above, below and right of it add to no pixel and are dropped).
+    // Up to two pieces per segment in fixed slots, each listed in every band
+    // it crosses.  A warp's
     // 32 consecutive segments mostly share their job and bands: per slot,
     // lanes adding to the same bin are grouped, so each bin takes one atomic
     // per warp, and each lane writes at the group's base plus its rank.
