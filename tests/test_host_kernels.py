@@ -100,6 +100,18 @@ def test_stroke_kernels_match_host_expansion(tmp_path):
         objs.append(obj)
     scene = str(tmp_path / "strokes.trace")
     _stroke_scene(scene)
+    # and two canvases of the many-canvas workload: long dashed polylines
+    # (dash walks over many 32-segment chunks), every join and cap kind
+    from canvas_ity_gb300 import scenes
+    workload = []
+    for i in (0, 1):
+        path = str(tmp_path / f"c3_{i}.trace")
+        with open(path, "wb") as f:
+            f.write(scenes.c3_canvas(i))
+        workload.append(path)
     out = _run(tmp_path, [os.path.join(HERE, "stroke_check.cpp")], std="c++20", objects=objs, args=[scene],
                libs=["-L", libdir, f"-Wl,-rpath,{libdir}", "-lcudart", "-lpthread"])
     assert out == "commands 6, differing 0", out
+    out = subprocess.run([str(tmp_path / "check"), *workload], check=True, capture_output=True,
+                         text=True).stdout.strip()
+    assert out.endswith("differing 0") and not out.startswith("commands 0"), out
