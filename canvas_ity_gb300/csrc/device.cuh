@@ -43,9 +43,10 @@ __device__ int tessellate(float2 p1, float2 c1, float2 c2, float2 p2, float angu
     const bool stroking = angular > -1.0f;
     tess_frame stack[22];
     int depth = 0, n = 0;
-    stack[depth++] = {p1, c1, c2, p2, 20};
-    while (depth > 0) {
-        tess_frame f = stack[--depth];
+    // the whole curve is the first frame, held in registers: a curve that
+    // is flat at once (most join and cap arcs) never touches the stack
+    tess_frame f = {p1, c1, c2, p2, 20};
+    for (;;) {
         for (;;) {
             float2 seg = sub2(f.p2, f.p1);
             float2 e1 = sub2(f.c1, f.p1), e3 = sub2(f.p2, f.c2);
@@ -84,6 +85,8 @@ __device__ int tessellate(float2 p1, float2 c1, float2 c2, float2 p2, float angu
             stack[depth++] = {sp, r1, r2, f.p2, f.limit - 1};
             f = {f.p1, l1, l2, sp, f.limit - 1};
         }
+        if (depth == 0) break;
+        f = stack[--depth];
     }
     return n;
 }
