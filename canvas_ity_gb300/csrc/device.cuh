@@ -256,14 +256,6 @@ __device__ __forceinline__ void dda_row(const dda_piece &p, int k, Emit &emit) {
     dda_cells(p, entry, ex, ps, pe, e2);
 }
 
-// Clip one polyline segment to [0,width] x [0,height] the way the
-// reference's Sutherland-Hodgman pass and clamp do (hpp:2204-2239), summed
-// over a polygon (far-off ends aside, crossing2): the part left of x = 0 is replaced by its projection onto
-// that edge; parts above y = 0 or below y = height contribute nothing, and
-// so does the part right of x = width, whose projection onto that edge adds
-// only to cells at x >= width, which no pixel reads.  Up to two pieces in
-// fixed slots (0 inside, 1 the left edge, each clamped); returns the mask of
-// the slots filled, none for a segment with a non-finite end.
 // Where u -> v crosses an edge, fs and ts the signed distances of u and v
 // from it: the reference's u + t (v - u) (hpp:2220-2221), except when u lies
 // 2^24 or more beyond the edge and v nearer, where that loses the crossing
@@ -273,6 +265,15 @@ __device__ __forceinline__ float2 crossing2(float2 u, float2 v, float fs, float 
                                                              : mix2(u, v, fs / (fs - ts));
 }
 
+// Clip one polyline segment to [0,width] x [0,height] the way the
+// reference's Sutherland-Hodgman pass and clamp do (hpp:2204-2239), summed
+// over a polygon (far-off ends aside, crossing2): the part left of x = 0 is
+// replaced by its projection onto that edge, clamped to [0, height]; parts
+// above y = 0 or below y = height contribute nothing, and so does the part
+// right of x = width, whose projection onto that edge adds only to cells at
+// x >= width, which no pixel reads.  Up to two pieces in fixed slots (0
+// inside, 1 the left edge, each clamped); returns the mask of the slots
+// filled, none for a segment with a non-finite end.
 __device__ __forceinline__ unsigned clip_segment(float2 a, float2 b, float width, float height, float2 (&pa)[2],
                                                  float2 (&pb)[2]) {
     if (!(isfinite(a.x) && isfinite(a.y) && isfinite(b.x) && isfinite(b.y))) return 0u;
@@ -303,7 +304,6 @@ __device__ __forceinline__ unsigned clip_segment(float2 a, float2 b, float width
         }
     };
     keep_y(has_main, ma, mb, ma.y, mb.y);
-    keep_y(has_left, la, lb, la.y, lb.y);
     // x <= width: the part beyond is dropped
     if (has_main) {
         float fs = width - ma.x, ts = width - mb.x;
@@ -315,7 +315,8 @@ __device__ __forceinline__ unsigned clip_segment(float2 a, float2 b, float width
         }
     }
     keep_y(has_main, ma, mb, height - ma.y, height - mb.y);
-    keep_y(has_left, la, lb, height - la.y, height - lb.y);
+    // The left piece lies on x = 0: clamping its ends to [0, height] is its
+    // clip to the rectangle, exactly (a crossing would be interpolated).
     auto clamp2 = [&](float2 u) { return f2(lo(hi(u.x, 0.0f), width), lo(hi(u.y, 0.0f), height)); };
     pa[0] = clamp2(ma);
     pb[0] = clamp2(mb);

@@ -38,7 +38,9 @@ void cy_set_strip_config(int strip_pixels, int threads);
  * listed per band of rows and accumulated per strip in shared memory as
  * fixed-point signed areas (add_runs' cell areas, hpp:2109-2170, with no
  * sorted runs in memory); coverage is within 1e-5 of the reference's and
- * RGBA8 within +-1 LSB.  1, exact: row-sorted runs summed in the reference's order
+ * RGBA8 within +-1 LSB while paths stay within a few hundred pixels of the
+ * canvas (further out, the reference's own clip rounding grows with the
+ * coordinates, and the binned clip's projection onto x = 0 is exact).  1, exact: row-sorted runs summed in the reference's order
  * (lines_to_runs and render_main, hpp:2193-2253, 2551-2605), so the float
  * canvas is the reference's bit for bit.  The plain engine is always exact. */
 void cy_set_coverage(int exact);

@@ -1137,16 +1137,6 @@ void canvas::scan_segment_binned(vec2 from, vec2 to) {
     } while (now.y != to.y);
 }
 
-// One polyline segment clipped to [0,width] x [0,height] on its own, as the
-// binned coverage does it: the polygon clip of scan (hpp:2204-2239) followed
-// by the clamp replaces the part of an edge left of x = 0 by its projection
-// onto that side, and parts above y = 0 or below y = height become
-// horizontal and add nothing; per segment the same pieces come out (inside,
-// left side), each clamped.  The part right of x = width is dropped: its
-// projection onto that side adds only to cells at x >= width, which no pixel
-// reads.  A segment with a non-finite end gives none.  In exact arithmetic
-// the pieces of all segments add up to the clipped polygon's coverage; in
-// float they differ from it by rounding only.
 // Where u -> v crosses an edge, fs and ts the signed distances of u and v
 // from it: the reference's u + t (v - u) (hpp:2220-2221), except when u lies
 // 2^24 or more beyond the edge and v nearer, where that loses the crossing
@@ -1156,6 +1146,17 @@ static inline vec2 crossing(vec2 u, vec2 v, float fs, float ts) {
                                                                          : mix(u, v, fs / (fs - ts));
 }
 
+// One polyline segment clipped to [0,width] x [0,height] on its own, as the
+// binned coverage does it: the polygon clip of scan (hpp:2204-2239) followed
+// by the clamp replaces the part of an edge left of x = 0 by its projection
+// onto that side, and parts above y = 0 or below y = height become
+// horizontal and add nothing; per segment the same pieces come out (inside,
+// left side), each clamped.  The left piece lies on x = 0, so clamping its
+// ends to [0, height] clips it exactly.  The part right of x = width is
+// dropped: its projection onto that side adds only to cells at x >= width,
+// which no pixel reads.  A segment with a non-finite end gives none.  In
+// exact arithmetic the pieces of all segments add up to the clipped
+// polygon's coverage; in float they differ from it by rounding only.
 static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec2 *pb) {
     if (!(std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(b.x) && std::isfinite(b.y))) return 0;
     vec2 ma = a, mb = b, la{}, lb{};
@@ -1196,7 +1197,6 @@ static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec
         }
     };
     keep_below(has_main, ma, mb, 0.0f, 1.0f);
-    keep_below(has_left, la, lb, 0.0f, 1.0f);
     if (has_main) {
         float fs = width - ma.x, ts = width - mb.x;
         if (fs < 0.0f && ts < 0.0f) {
@@ -1208,7 +1208,6 @@ static int clip_segment(vec2 a, vec2 b, float width, float height, vec2 *pa, vec
         }
     }
     keep_below(has_main, ma, mb, height, -1.0f);
-    keep_below(has_left, la, lb, height, -1.0f);
     int n = 0;
     auto put = [&](vec2 u, vec2 v) {
         pa[n] = mk(lo(hi(u.x, 0.0f), width), lo(hi(u.y, 0.0f), height));

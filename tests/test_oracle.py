@@ -83,6 +83,27 @@ def test_binned_crossings_hold_for_far_points(far):
     assert not np.array_equal(_image(oracle.replay(G.far_point_scene(far))[0]), want)
 
 
+@pytest.mark.parametrize("span", [300.0, 1e4, 1e5])
+def test_binned_projection_of_far_polygons_is_exact(span):
+    """A rotated square whose corners lie `span` away around the canvas
+    covers every pixel.  Its edges left of the canvas project onto x = 0,
+    and clamping such a piece to [0, height] clips it exactly, so every
+    pixel's binned coverage is exactly 1; the others add nothing."""
+    w, h = 160, 128
+    t = T.TraceWriter(w, h)
+    t.set_color(T.FILL_STYLE, 1.0, 1.0, 1.0, 1.0)
+    t.begin_path()
+    for k in range(4):
+        a = 0.3 + k * np.pi / 2
+        p = (w / 2 + span * np.cos(a), h / 2 + span * np.sin(a))
+        (t.move_to if k == 0 else t.line_to)(*p)
+    t.close_path()
+    t.fill()
+    tb = t.finish()
+    cov = oracle.replay_linear(tb, w, h, coverage="binned")[..., 3]
+    assert (cov == 1.0).all()
+
+
 def test_get_image_data_known_answer():
     """test/test.cpp:1800-1826: strided, offset read of a 10x10 checker."""
     entry = next(e for e in MANIFEST if e["name"] == "get_image_data")
