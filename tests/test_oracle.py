@@ -104,6 +104,32 @@ def test_binned_projection_of_far_polygons_is_exact(span):
     assert (cov == 1.0).all()
 
 
+def test_binned_wholly_left_subpath_cancels_exactly():
+    """A subpath wholly left of the canvas projects onto x = 0 as a closed
+    chain of vertical pieces.  Where its y values are 2 or more they are
+    multiples of 2^-22 (a float's step there), so every piece's fixed-point
+    sum is exact and the chain cancels to nothing: the float canvas is the
+    same bit for bit as without the subpath."""
+    def scene(extra):
+        t = T.TraceWriter(96, 80)
+        t.set_color(T.FILL_STYLE, 0.3, 0.6, 0.9, 1.0)
+        t.begin_path()
+        t.move_to(10.3, 12.7)
+        t.line_to(80.1, 20.2)
+        t.line_to(60.4, 70.9)
+        t.close_path()
+        if extra:
+            t.move_to(-50.25, 5.5)
+            t.line_to(-10.75, 60.125)
+            t.line_to(-30.5, 79.0)
+            t.close_path()
+        t.fill()
+        return t.finish()
+    a = oracle.replay_linear(scene(False), 96, 80, coverage="binned")
+    b = oracle.replay_linear(scene(True), 96, 80, coverage="binned")
+    assert np.array_equal(a, b)
+
+
 def test_get_image_data_known_answer():
     """test/test.cpp:1800-1826: strided, offset read of a 10x10 checker."""
     entry = next(e for e in MANIFEST if e["name"] == "get_image_data")
